@@ -1,0 +1,113 @@
+"""Build recipe for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+* ``build_oracle()`` compiles ``oracle/sf_oracle.c`` -- the plain-C
+  restatement of the reference algorithms -- into ``oracle/liboracle.so``.
+  It runs wherever the tests run (build host and GPU host).
+* ``build_ref()`` compiles golden-vector adapters (``oracle/ref_src/*.cc``)
+  against the reference's own headers where they lie, into
+  ``oracle/_ref/``.  It needs the reference checkout and therefore only runs
+  on the build host; ``tests/golden/gen_golden.py`` uses the result to write
+  the committed fixtures.
+
+The reference is compiled with its generic one-lane ``VectorizedArray``
+(ISA macros undefined, empty ``x86intrin.h`` stand-in), so the reference's
+lane-interleaved DG vectors coincide with the cell-major layout used here.
+Two DG headers are copied into ``oracle/_ref/patched/`` and patched at build
+time (PATCHES below); nothing of the reference is stored in the repository.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = os.environ.get("SF_REFERENCE_ROOT", "/root/reference")
+REF_INC = os.path.join(REF_ROOT, "legacy", "include")
+REF_SRC = os.path.join(REF_ROOT, "legacy", "src")
+OUT_REF = os.path.join(HERE, "_ref")
+
+# (file, 1-based line, expected text, replacement)
+PATCHES = [
+    # periodic x-wrap neighbour: '+ dofs_per_cell' must be '* dofs_per_cell'
+    ("evaluation_dg_laplacian.h", 270,
+     "(ii - (n_cells[0] - 1) * n_lanes) + dofs_per_cell",
+     "(ii - (n_cells[0] - 1) * n_lanes) * dofs_per_cell"),
+    # final x sweep integrates with the forward shape matrix; use transpose
+    ("evaluation_dg_laplacian.h", 482,
+     "apply_1d_matvec_kernel<nn, 1, 0, true, false, VectorizedArray<Number>>",
+     "apply_1d_matvec_kernel<nn, 1, 0, false, false, VectorizedArray<Number>>"),
+    ("evaluation_dg_advect.h", 435,
+     "(ii-(n_cells[0]-1)*n_lanes)+dofs_per_cell",
+     "(ii-(n_cells[0]-1)*n_lanes)*dofs_per_cell"),
+]
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+
+
+def build_oracle(force: bool = False) -> str:
+    out = os.path.join(HERE, "liboracle.so")
+    src = os.path.join(HERE, "sf_oracle.c")
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "sf_oracle.h"))):
+        return out
+    tmp = out + ".tmp%d" % os.getpid()
+    _run(["gcc", "-O2", "-std=c11", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src, "-lm"])
+    os.replace(tmp, out)
+    return out
+
+
+def _patch_headers() -> str:
+    pdir = os.path.join(OUT_REF, "patched")
+    os.makedirs(pdir, exist_ok=True)
+    by_file = {}
+    for fname, line, old, new in PATCHES:
+        by_file.setdefault(fname, []).append((line, old, new))
+    for fname, edits in by_file.items():
+        with open(os.path.join(REF_INC, fname)) as f:
+            lines = f.readlines()
+        for line, old, new in edits:
+            if old not in lines[line - 1]:
+                raise RuntimeError("reference %s:%d does not contain %r" % (fname, line, old))
+            lines[line - 1] = lines[line - 1].replace(old, new)
+        with open(os.path.join(pdir, fname), "w") as f:
+            f.writelines(lines)
+    return pdir
+
+
+def build_ref() -> list[str]:
+    """Compile the golden-vector adapters against the reference headers."""
+    if not os.path.isdir(REF_INC):
+        raise FileNotFoundError("reference checkout not found at %s" % REF_ROOT)
+    os.makedirs(OUT_REF, exist_ok=True)
+    pdir = _patch_headers()
+    shim = os.path.join(HERE, "ref_src")
+    flags = ["g++", "-O2", "-std=c++14", "-fPIC", "-shared", "-w",
+             "-U__SSE2__", "-U__SSE__", "-U__AVX__", "-U__AVX2__", "-U__AVX512F__",
+             "-I", shim]
+    outs = []
+    # the DG headers put an OpenMP 'private' clause that the access macro of
+    # ref_shim.h would rewrite, so they are built without OpenMP (serial)
+    for name, extra, omp in [("ref_kernel", [REF_INC], False),
+                             ("ref_cell_gll", [REF_INC, REF_SRC], True),
+                             ("ref_cell_hermite", [REF_INC], False),
+                             ("ref_dg", [pdir, REF_INC], False)]:
+        inc = ["-fopenmp"] if omp else []
+        for d in extra:
+            inc += ["-I", d]
+        out = os.path.join(OUT_REF, "lib%s.so" % name)
+        _run(flags + inc + ["-o", out, os.path.join(shim, name + ".cc")])
+        outs.append(out)
+    return outs
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    if len(sys.argv) > 1 and sys.argv[1] == "ref":
+        for o in build_ref():
+            print(o)

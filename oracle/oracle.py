@@ -1,0 +1,218 @@
+"""ctypes bindings of the FP64 CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module; it is the checker, never the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+SFO_MAX_N = 10
+BASIS_GLL, BASIS_HERMITE = 0, 1
+
+
+class Shape(C.Structure):
+    _fields_ = [
+        ("degree", C.c_int), ("n", C.c_int), ("basis", C.c_int),
+        ("xq", C.c_double * SFO_MAX_N), ("wq", C.c_double * SFO_MAX_N),
+        ("xgll", C.c_double * SFO_MAX_N),
+        ("S", C.c_double * (SFO_MAX_N * SFO_MAX_N)),
+        ("D", C.c_double * (SFO_MAX_N * SFO_MAX_N)),
+        ("Sinv", C.c_double * (SFO_MAX_N * SFO_MAX_N)),
+        ("face_v", (C.c_double * SFO_MAX_N) * 2),
+        ("face_d", (C.c_double * SFO_MAX_N) * 2),
+        ("hermite_d0", C.c_double),
+        ("S_eo", C.c_double * (SFO_MAX_N * SFO_MAX_N)),
+        ("D_eo", C.c_double * (SFO_MAX_N * SFO_MAX_N)),
+        ("Sinv_eo", C.c_double * (SFO_MAX_N * SFO_MAX_N)),
+        ("face_eo", C.c_double * (2 * SFO_MAX_N)),
+    ]
+
+
+class Mesh(C.Structure):
+    _fields_ = [("degree", C.c_int), ("basis", C.c_int), ("n_cells", C.c_int * 3),
+                ("length", C.c_double * 3), ("deform", C.c_double),
+                ("dirichlet", C.c_int)]
+
+
+class DG(C.Structure):
+    _fields_ = [("degree", C.c_int), ("n_cells", C.c_int * 3), ("h", C.c_double * 3),
+                ("penalty", C.c_double), ("velocity", C.c_double * 3),
+                ("inverse_mass", C.c_int)]
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = C.CDLL(path)
+        L.sfo_shape_init.argtypes = [C.c_int, C.c_int, C.POINTER(Shape)]
+        L.sfo_apply_1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp,
+                                   C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.sfo_cont_n_dofs.argtypes = [C.POINTER(Mesh)]
+        L.sfo_cont_n_dofs.restype = C.c_longlong
+        L.sfo_cont_geometry.argtypes = [C.POINTER(Mesh), _dp]
+        L.sfo_cont_apply.argtypes = [C.POINTER(Mesh), _dp, C.c_void_p, _dp, _dp, C.c_int]
+        L.sfo_cont_kappa_grad.argtypes = [C.POINTER(Mesh), _dp, _dp, _dp, _dp]
+        L.sfo_cont_diagonal.argtypes = [C.POINTER(Mesh), _dp, C.c_void_p, _dp]
+        L.sfo_cell_apply.argtypes = [C.POINTER(Shape), _dp, C.c_int, _dp, _dp]
+        L.sfo_dg_n_dofs.argtypes = [C.POINTER(DG)]
+        L.sfo_dg_n_dofs.restype = C.c_longlong
+        for f in ("sfo_dg_sipg_apply", "sfo_dg_advect_apply", "sfo_dg_advect_apply_transpose"):
+            getattr(L, f).argtypes = [C.POINTER(DG), _dp, _dp]
+        L.sfo_dg_sipg_diagonal.argtypes = [C.POINTER(DG), _dp]
+        L.sfo_chebyshev_update.argtypes = [C.c_longlong, _dp, _dp, _dp, _dp, _dp, _dp,
+                                           C.c_double, C.c_double]
+        _lib = L
+    return _lib
+
+
+def shape(degree: int, basis: int = BASIS_GLL) -> Shape:
+    s = Shape()
+    if lib().sfo_shape_init(degree, basis, C.byref(s)) != 0:
+        raise ValueError("unsupported degree %d" % degree)
+    return s
+
+
+def shape_arrays(degree: int, basis: int = BASIS_GLL) -> dict:
+    s = shape(degree, basis)
+    n = degree + 1
+    st = (n + 1) // 2
+
+    def mat(a):
+        return np.array(a[: n * n], dtype=np.float64).reshape(n, n)
+
+    return {
+        "xq": np.array(s.xq[:n]), "wq": np.array(s.wq[:n]), "xgll": np.array(s.xgll[:n]),
+        "S": mat(s.S), "D": mat(s.D), "Sinv": mat(s.Sinv),
+        "face_v": np.array([s.face_v[0][:n], s.face_v[1][:n]]),
+        "face_d": np.array([s.face_d[0][:n], s.face_d[1][:n]]),
+        "hermite_d0": s.hermite_d0,
+        "S_eo": np.array(s.S_eo[: n * st]), "D_eo": np.array(s.D_eo[: n * st]),
+        "Sinv_eo": np.array(s.Sinv_eo[: n * st]), "face_eo": np.array(s.face_eo[: 2 * n]),
+    }
+
+
+def apply_1d(nn, type_, cor, add, coef_eo, x, out_init=None, do_dg=0, dg=None, face=None):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros(nn) if out_init is None else np.array(out_init, dtype=np.float64)
+    addp = out.ctypes.data if add else None
+    dgp = np.ascontiguousarray(dg, dtype=np.float64) if dg is not None else None
+    facep = np.zeros(4) if face is None else np.array(face, dtype=np.float64)
+    lib().sfo_apply_1d(nn, 1, type_, int(cor), int(add), np.ascontiguousarray(coef_eo, dtype=np.float64),
+                       x, out, addp, do_dg, dgp.ctypes.data if dgp is not None else None,
+                       facep.ctypes.data)
+    return out, facep
+
+
+def mesh(degree, n_cells, basis=BASIS_GLL, length=(1.0, 1.0, 1.0), deform=0.0, dirichlet=1):
+    m = Mesh()
+    m.degree = degree
+    m.basis = basis
+    for d in range(3):
+        m.n_cells[d] = n_cells[d]
+        m.length[d] = length[d]
+    m.deform = deform
+    m.dirichlet = dirichlet
+    return m
+
+
+def cont_n_dofs(m: Mesh) -> int:
+    return int(lib().sfo_cont_n_dofs(C.byref(m)))
+
+
+def cont_geometry(m: Mesh) -> np.ndarray:
+    n = m.degree + 1
+    C_ = m.n_cells[0] * m.n_cells[1] * m.n_cells[2]
+    G = np.zeros(C_ * 6 * n ** 3)
+    lib().sfo_cont_geometry(C.byref(m), G)
+    return G
+
+
+def cont_apply(m: Mesh, G, x, kappa=None, n_threads=0):
+    y = np.zeros(cont_n_dofs(m))
+    k = np.ascontiguousarray(kappa, dtype=np.float64) if kappa is not None else None
+    lib().sfo_cont_apply(C.byref(m), np.ascontiguousarray(G), k.ctypes.data if k is not None else None,
+                         np.ascontiguousarray(x, dtype=np.float64), y, n_threads)
+    return y
+
+
+def cont_kappa_grad(m: Mesh, G, u, lam):
+    n = m.degree + 1
+    C_ = m.n_cells[0] * m.n_cells[1] * m.n_cells[2]
+    dk = np.zeros(C_ * n ** 3)
+    lib().sfo_cont_kappa_grad(C.byref(m), np.ascontiguousarray(G), np.ascontiguousarray(u, dtype=np.float64),
+                              np.ascontiguousarray(lam, dtype=np.float64), dk)
+    return dk
+
+
+def cont_diagonal(m: Mesh, G, kappa=None):
+    d = np.zeros(cont_n_dofs(m))
+    k = np.ascontiguousarray(kappa, dtype=np.float64) if kappa is not None else None
+    lib().sfo_cont_diagonal(C.byref(m), np.ascontiguousarray(G), k.ctypes.data if k is not None else None, d)
+    return d
+
+
+def cell_apply(degree, basis, G, x, geo_stride):
+    s = shape(degree, basis)
+    out = np.zeros((degree + 1) ** 3)
+    lib().sfo_cell_apply(C.byref(s), np.ascontiguousarray(G, dtype=np.float64), geo_stride,
+                         np.ascontiguousarray(x, dtype=np.float64), out)
+    return out
+
+
+def dg(degree, n_cells, h, penalty=1.0, velocity=(1.0, 0.5, 0.25), inverse_mass=1):
+    g = DG()
+    g.degree = degree
+    for d in range(3):
+        g.n_cells[d] = n_cells[d]
+        g.h[d] = h[d]
+        g.velocity[d] = velocity[d]
+    g.penalty = penalty
+    g.inverse_mass = inverse_mass
+    return g
+
+
+def dg_n_dofs(g: DG) -> int:
+    return int(lib().sfo_dg_n_dofs(C.byref(g)))
+
+
+def _dg_call(name, g, x):
+    y = np.zeros(dg_n_dofs(g))
+    getattr(lib(), name)(C.byref(g), np.ascontiguousarray(x, dtype=np.float64), y)
+    return y
+
+
+def dg_sipg_apply(g, x):
+    return _dg_call("sfo_dg_sipg_apply", g, x)
+
+
+def dg_advect_apply(g, x):
+    return _dg_call("sfo_dg_advect_apply", g, x)
+
+
+def dg_advect_apply_transpose(g, x):
+    return _dg_call("sfo_dg_advect_apply_transpose", g, x)
+
+
+def dg_sipg_diagonal(g):
+    d = np.zeros(dg_n_dofs(g))
+    lib().sfo_dg_sipg_diagonal(C.byref(g), d)
+    return d
+
+
+def chebyshev_update(ax, b, dinv, x_old, t, c_np, c_tm):
+    x_new = np.zeros_like(x_old)
+    t = np.array(t, dtype=np.float64)
+    lib().sfo_chebyshev_update(len(x_old), ax, b, dinv, x_old, x_new, t, c_np, c_tm)
+    return x_new, t

@@ -1,0 +1,94 @@
+/*
+ * Golden-vector adapter for the reference's DG operators
+ * (legacy/include/evaluation_dg_laplacian.h, evaluation_dg_advect.h),
+ * compiled from copies that oracle/build.py patches at build time
+ * (see oracle/build.py: PATCHES).  TEST INFRASTRUCTURE ONLY.
+ */
+#include "ref_shim.h"
+#include "evaluation_dg_laplacian.h"
+#include "evaluation_dg_advect.h"
+
+template <typename Ev>
+static void set_geometry(Ev &ev, const double *h)
+{
+  for (int d = 0; d < 3; ++d) ev.jacobian_data[d] = 1. / h[d];
+  ev.jxw_data[0] = h[0] * h[1] * h[2];
+}
+
+/* mode 0: y = A x;  mode 1: fused Chebyshev step with rhs b, inverse
+ * diagonal dinv, coefficients c_np, c_tm; x_new -> y, t updated in place */
+template <int p>
+static void sipg(const int *nc, const double *h, int mode, const double *x,
+                 const double *b, const double *dinv, double *t, double c_np,
+                 double c_tm, double *y)
+{
+  EvaluationDGLaplacian<3, p, double> ev;
+  ev.blx = 2; ev.bly = 2; ev.blz = 2;
+  unsigned int n_cells[3] = {(unsigned)nc[0], (unsigned)nc[1], (unsigned)nc[2]};
+  ev.initialize(n_cells);
+  set_geometry(ev, h);
+  const std::size_t N = ev.n_elements() * ev.dofs_per_cell;
+  AlignedVector<double> src(N), xo(N), dg(N), yo(N), tmp(N);
+  for (std::size_t i = 0; i < N; ++i) xo[i] = x[i];
+  if (mode == 0) {
+    ev.template do_cheby_iter<false>(src, xo, dg, yo, tmp, 0., 0.);
+  } else {
+    for (std::size_t i = 0; i < N; ++i) { ev.sol_rhs[i] = b[i]; src[i] = b[i]; dg[i] = dinv[i]; tmp[i] = t[i]; }
+    ev.template do_cheby_iter<true>(src, xo, dg, yo, tmp, c_np, c_tm);
+    for (std::size_t i = 0; i < N; ++i) t[i] = tmp[i];
+  }
+  for (std::size_t i = 0; i < N; ++i) y[i] = yo[i];
+}
+
+/* y = M^-1 K x with the reference's velocity (1, 0.15, -0.05) */
+template <int p>
+static void advect(const int *nc, const double *h, const double *x, double *y)
+{
+  EvaluationDGAdvection<3, p, double> ev;
+  ev.blx = 2; ev.bly = 2; ev.blz = 2;
+  unsigned int n_cells[3] = {(unsigned)nc[0], (unsigned)nc[1], (unsigned)nc[2]};
+  ev.initialize(n_cells);
+  set_geometry(ev, h);
+  const std::size_t N = ev.n_elements() * ev.dofs_per_cell;
+  AlignedVector<double> src(N), upd(N), np(N), tm(N);
+  for (std::size_t i = 0; i < N; ++i) src[i] = x[i];
+  ev.template do_rk_stage<false>(src, upd, np, tm, 0., 0., 0.);
+  for (std::size_t i = 0; i < N; ++i) y[i] = np[i];
+}
+
+template <int p>
+static void face_tables(double *face_eo, double *Sinv_eo)
+{
+  EvaluationDGAdvection<3, p, double> ev;
+  ev.blx = 2; ev.bly = 2; ev.blz = 2;
+  unsigned int n_cells[3] = {1, 1, 1};
+  ev.initialize(n_cells);
+  const int n = p + 1, st = (n + 1) / 2;
+  for (int i = 0; i < 2 * n; ++i) face_eo[i] = ev.shape_values_on_face_eo[i][0];
+  for (int i = 0; i < n * st; ++i) Sinv_eo[i] = ev.inv_shape_values_eo[i][0];
+}
+
+#define SF_DISPATCH(fn, ...)                                                   \
+  switch (degree) {                                                            \
+  case 1: fn<1>(__VA_ARGS__); return 0;                                        \
+  case 2: fn<2>(__VA_ARGS__); return 0;                                        \
+  case 3: fn<3>(__VA_ARGS__); return 0;                                        \
+  case 4: fn<4>(__VA_ARGS__); return 0;                                        \
+  case 5: fn<5>(__VA_ARGS__); return 0;                                        \
+  case 6: fn<6>(__VA_ARGS__); return 0;                                        \
+  case 7: fn<7>(__VA_ARGS__); return 0;                                        \
+  case 8: fn<8>(__VA_ARGS__); return 0;                                        \
+  default: return -1;                                                          \
+  }
+
+extern "C" int sfref_dg_sipg(int degree, const int *nc, const double *h, int mode,
+                             const double *x, const double *b, const double *dinv,
+                             double *t, double c_np, double c_tm, double *y)
+{ SF_DISPATCH(sipg, nc, h, mode, x, b, dinv, t, c_np, c_tm, y) }
+
+extern "C" int sfref_dg_advect(int degree, const int *nc, const double *h,
+                               const double *x, double *y)
+{ SF_DISPATCH(advect, nc, h, x, y) }
+
+extern "C" int sfref_dg_tables(int degree, double *face_eo, double *Sinv_eo)
+{ SF_DISPATCH(face_tables, face_eo, Sinv_eo) }

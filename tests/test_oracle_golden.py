@@ -1,0 +1,129 @@
+"""The CPU oracle against the golden vectors made by the reference's own code.
+
+These pins are what every GPU parity test inherits: the CUDA library is
+compared with the oracle, and the oracle is compared here with the reference
+(tests/golden/gen_golden.py).  Tolerances are relative, FP64.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_tables(golden, p):
+    g = golden("tables.npz")
+    n = p + 1
+    a = O.shape_arrays(p, O.BASIS_GLL)
+    np.testing.assert_allclose(a["xq"], g["gauss_x_%d" % n], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(a["wq"], g["gauss_w_%d" % n], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(a["xgll"], g["gll_x_%d" % n], rtol=0, atol=1e-15)
+    scale = np.abs(g["gll_D_eo_%d" % p]).max()
+    np.testing.assert_allclose(a["S_eo"], g["gll_S_eo_%d" % p], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(a["D_eo"], g["gll_D_eo_%d" % p], rtol=0, atol=1e-15 * scale)
+    np.testing.assert_allclose(a["face_eo"], g["face_eo_%d" % p], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(a["Sinv_eo"], g["Sinv_eo_%d" % p], rtol=0, atol=1e-14)
+    h = O.shape_arrays(p, O.BASIS_HERMITE)
+    np.testing.assert_allclose(h["S_eo"], g["herm_S_eo_%d" % p], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(h["D_eo"], g["herm_D_eo_%d" % p], rtol=0, atol=1e-15 * scale)
+    assert abs(h["hermite_d0"] - g["herm_d0_%d" % p][0]) <= 1e-13 * abs(g["herm_d0_%d" % p][0])
+
+
+def test_kernel1d(golden):
+    g = golden("kernel1d.npz")
+    k = 0
+    while "k%03d_meta" % k in g:
+        nn, t, c, a, dgm = (int(v) for v in g["k%03d_meta" % k])
+        y, f = O.apply_1d(nn, t, c, a, g["k%03d_coef" % k], g["k%03d_x" % k],
+                          out_init=g["k%03d_o" % k], do_dg=dgm, dg=g["k%03d_dg" % k],
+                          face=g["k%03d_fin" % k])
+        assert rel(y, g["k%03d_y" % k]) < 1e-14, (nn, t, c, a, dgm)
+        if dgm and c:
+            assert rel(f[: 2 * dgm], g["k%03d_fout" % k][: 2 * dgm]) < 1e-14
+        k += 1
+    assert k >= 80
+
+
+def test_kernel_even_odd_vs_plain():
+    """even-odd kernel against the plain n x n contraction
+    (the cross-check of test_multiplication.cc:912-1021)"""
+    rng = np.random.default_rng(3)
+    for p in range(1, 9):
+        n = p + 1
+        a = O.shape_arrays(p, O.BASIS_GLL)
+        x = rng.standard_normal(n)
+        for M, eo, t in ((a["S"], a["S_eo"], 0), (a["D"], a["D_eo"], 1)):
+            y, _ = O.apply_1d(n, t, True, False, eo, x)
+            assert rel(y, M @ x) < 1e-14
+            y, _ = O.apply_1d(n, t, False, False, eo, x)
+            assert rel(y, M.T @ x) < 1e-14
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_cell(golden, p):
+    g = golden("cell.npz")
+    n = p + 1
+    a = O.shape_arrays(p, O.BASIS_GLL)
+    W = np.einsum("k,j,i->kji", a["wq"], a["wq"], a["wq"]).ravel()
+    G6 = g["gll_G6_%d" % p]
+    G = np.concatenate([G6[e] * W for e in range(6)])
+    y = O.cell_apply(p, O.BASIS_GLL, G, g["gll_x_%d" % p], n ** 3)
+    assert rel(y, g["gll_y_%d" % p]) < 1e-14
+    if p != 2:  # the reference drops a nonzero term for the degree-2 Hermite basis
+        ij = np.array([4.0, 2.0, 4.0 / 3.0])
+        jxw = 1.0 / np.prod(ij)
+        G6 = np.array([jxw * ij[0] ** 2, jxw * ij[1] ** 2, jxw * ij[2] ** 2, 0, 0, 0])
+        G = np.concatenate([G6[e] * W for e in range(6)])
+        y = O.cell_apply(p, O.BASIS_HERMITE, G, g["herm_x_%d" % p], n ** 3)
+        assert rel(y, g["herm_y_%d" % p]) < 1e-14
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_continuous_affine(golden, p):
+    g = golden("cont.npz")
+    nc = tuple(int(v) for v in g["nc_%d" % p])
+    m = O.mesh(p, nc, length=tuple(g["len_%d" % p]))
+    G = O.cont_geometry(m)
+    y = O.cont_apply(m, G, g["x_%d" % p])
+    assert rel(y, g["y_%d" % p]) < 1e-13
+
+
+def test_continuous_q4_16(golden):
+    g = golden("cont.npz")
+    m = O.mesh(4, (16, 16, 16))
+    N = O.cont_n_dofs(m)
+    x = np.random.default_rng(20241203).uniform(-1.0, 1.0, N)
+    y = O.cont_apply(m, O.cont_geometry(m), x)
+    idx = g["q4_16_sample_idx"]
+    assert rel(y[idx], g["q4_16_sample_y"]) < 1e-13
+    assert abs(np.linalg.norm(y) - g["q4_16_norm2"][0]) < 1e-12 * g["q4_16_norm2"][0]
+
+
+@pytest.mark.parametrize("p", [1, 3, 4, 5, 6, 7, 8])
+def test_dg_sipg(golden, p):
+    g = golden("dg_sipg.npz")
+    d = O.dg(p, tuple(int(v) for v in g["nc_%d" % p]), tuple(g["h_%d" % p]))
+    y = O.dg_sipg_apply(d, g["x_%d" % p])
+    assert rel(y, g["y_%d" % p]) < 1e-14
+
+
+def test_dg_chebyshev_step(golden):
+    g = golden("dg_sipg.npz")
+    d = O.dg(5, tuple(int(v) for v in g["nc_5"]), tuple(g["h_5"]))
+    ax = O.dg_sipg_apply(d, g["x_5"])
+    xn, tn = O.chebyshev_update(ax, g["cheb_b"], g["cheb_dinv"], g["x_5"], g["cheb_t"], 0.7, 0.3)
+    assert rel(xn, g["cheb_xnew"]) < 1e-14
+    assert rel(tn, g["cheb_tnew"]) < 1e-14
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_dg_advect(golden, p):
+    g = golden("dg_advect.npz")
+    d = O.dg(p, tuple(int(v) for v in g["nc_%d" % p]), tuple(g["h_%d" % p]),
+             velocity=(1.0, 0.15, -0.05), inverse_mass=1)
+    y = O.dg_advect_apply(d, g["x_%d" % p])
+    assert rel(y, g["y_%d" % p]) < 1e-14
