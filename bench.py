@@ -1,0 +1,356 @@
+"""Benchmark: continuous FE Laplacian matvec on the deformed 64^3 mesh.
+
+Workload (the metric's configuration): 64x64x64 hexahedral cells on [0,1]^3
+mapped by x_i <- x_i + 0.05 sin(2 pi x_j) sin(2 pi x_k), Gauss quadrature
+with n = p+1 points, precomputed merged 6-entry geometry per quadrature point,
+homogeneous Dirichlet boundary, input uniform[-1,1].  Headline: degree 4,
+FP32 operator; the JSON line also carries the degree 2..8 sweep in FP32 and
+FP64 with the relative error of every FP32 apply against the FP64 apply.
+
+One step = one operator apply y = A x with x and the geometry resident in
+HBM (the working set, 0.9 GB at p=4 FP32, exceeds the 129 MB L2, so no
+explicit flush).  e2e = the same apply through the C ABI with the input
+copied from pinned host memory and the result copied back every step.
+
+``--impl reference`` times the reference's CPU algorithm for the same apply
+on the host cores (the FP64 oracle port, OpenMP over all host threads) on a
+bounded sample of cells and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Laplacian matvec GDoF/s + % HBM peak, FP32 vs FP64 at stated rel. error"
+UNIT = "GDoF/s"
+DEFORM = 0.05
+
+
+def algorithmic_bytes(p, n_dofs, n_cells, s):
+    """x read once, y written once, 6 geometry entries per quadrature point
+    (node indices are computed, not stored)"""
+    return 2 * s * n_dofs + 6 * s * (p + 1) ** 3 * n_cells
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """SM clock and throttle reasons sampled during the timed region through
+    NVML (libnvidia-ml, read-only queries) every 2 ms in a thread."""
+
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+               0x4: "sw_power_cap"}
+
+    def __init__(self, gpu_index=0):
+        import ctypes
+        import threading
+        self.samples, self.reasons, self.max_mhz = [], set(), None
+        self.stop_evt = threading.Event()
+        self.thread = None
+        self.nvml = None
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return
+            h = ctypes.c_void_p()
+            if nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(gpu_index), ctypes.byref(h)) != 0:
+                return
+            mx = ctypes.c_uint()
+            if nv.nvmlDeviceGetMaxClockInfo(h, ctypes.c_int(1), ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            fn = None
+            for name in ("nvmlDeviceGetCurrentClocksEventReasons",
+                         "nvmlDeviceGetCurrentClocksThrottleReasons"):
+                try:
+                    fn = getattr(nv, name)
+                    break
+                except AttributeError:
+                    continue
+            self.reason_fn = fn
+            self.nvml, self.h = nv, h
+        except OSError:
+            self.nvml = None
+
+    def _run(self):
+        import ctypes
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop_evt.is_set():
+            if self.nvml.nvmlDeviceGetClockInfo(self.h, ctypes.c_int(1), ctypes.byref(clk)) == 0:
+                self.samples.append(float(clk.value))
+            if self.reason_fn is not None and self.reason_fn(self.h, ctypes.byref(rs)) == 0:
+                for bit, name in self.REASONS.items():
+                    if rs.value & bit:
+                        self.reasons.add(name)
+            self.stop_evt.wait(0.002)
+
+    def start(self):
+        import threading
+        if self.nvml is not None:
+            self.thread = threading.Thread(target=self._run, daemon=True)
+            self.thread.start()
+
+    def stop(self):
+        if self.thread is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvml unavailable"]}
+        self.stop_evt.set()
+        self.thread.join()
+        return {"sm_mhz": statistics.median(self.samples) if self.samples else None,
+                "sm_max_mhz": self.max_mhz, "reasons": sorted(self.reasons),
+                "samples": len(self.samples)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference(p, seconds=12.0, n_threads=None):
+    """time the FP64 oracle port of the reference's cell algorithm (gather ->
+    even-odd sum factorisation -> scatter) on a bounded sample mesh"""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    threads = n_threads or os.cpu_count() or 1
+    nc = (16, 16, 16)
+    m = O.mesh(p, nc, deform=DEFORM)
+    G = O.cont_geometry(m)
+    x = np.random.default_rng(1).uniform(-1, 1, O.cont_n_dofs(m))
+    O.cont_apply(m, G, x, n_threads=threads)  # warm-up
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        O.cont_apply(m, G, x, n_threads=threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or reps >= 100000:
+            break
+    n_dofs = O.cont_n_dofs(m)
+    return {"value": n_dofs * reps / el / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "16^3 cells of the deformed mesh, p=%d, FP64, %d applies in %.1f s" % (p, reps, el)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    p = args.degree
+    per_step = []
+    base = None
+    for _ in range(args.warmup):
+        cpu_reference(p, seconds=1.0)
+    for _ in range(args.steps):
+        r = cpu_reference(p, seconds=args.ref_seconds)
+        per_step.append(r["value"])
+        base = r
+    value = statistics.median(per_step)
+    base["value"] = value
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "continuous Laplacian, deformed mesh, p=%d (CPU sample 16^3)" % p,
+                       "degree": p, "n_cells": [16, 16, 16], "deform": DEFORM},
+            "cpu_baseline": base,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def time_apply(op, x, y, steps, warmup, stream):
+    import torch
+    for _ in range(warmup):
+        op.vmult(x, y, stream=stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        op.vmult(x, y, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / steps
+
+
+def run_ours(args):
+    import torch
+
+    from sum_factorization_kernels_gb300 import sfgpu
+
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    peak, peak_kind = measured_peaks()
+    p = args.degree
+    NCELLS = (args.ncells,) * 3
+
+    # ---- headline: FP32, degree p, inputs resident ----
+    op = sfgpu.Operator(sfgpu.OP_LAPLACE, degree=p, n_cells=NCELLS, deform=DEFORM)
+    N, C = op.n_dofs, op.n_cells
+    gen = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    x64 = torch.rand(N, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1
+    x32 = x64.float()
+    y32 = torch.empty_like(x32)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            op.vmult(x32, y32, stream=stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        op.vmult(x32, y32, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    t_step = e0.elapsed_time(e1) / 1e3 / args.steps
+    clk = clocks.stop()
+    t_step = max_over_ranks(t_step, world)
+    value = N * world / t_step / 1e9
+    bytes_apply = algorithmic_bytes(p, N, C, 4)
+    achieved = bytes_apply / t_step / 1e9
+    launches_per_apply = 8 + 1  # 8 colour launches + boundary rows
+
+    # ---- e2e: pinned host input -> device -> apply -> host, every step ----
+    xh = torch.empty(N, dtype=torch.float32, pin_memory=True)
+    xh.copy_(x32.cpu())
+    yh = torch.empty(N, dtype=torch.float32, pin_memory=True)
+    xd = torch.empty_like(x32)
+    yd = torch.empty_like(x32)
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            xd.copy_(xh, non_blocking=True)
+            op.vmult(xd, yd, stream=stream)
+            yh.copy_(yd, non_blocking=True)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            xd.copy_(xh, non_blocking=True)
+            op.vmult(xd, yd, stream=stream)
+            yh.copy_(yd, non_blocking=True)
+        stream.synchronize()
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    e2e = {"value": N * world / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": 4 * N,
+           "d2h_bytes_per_step": 4 * N}
+
+    # ---- FP64 at the headline degree and the degree sweep ----
+    sweep = []
+    fp64_value = None
+    if not args.no_sweep:
+        y64 = torch.empty_like(x64)
+        del op, xh, yh, xd, yd
+        torch.cuda.empty_cache()
+        degrees = [int(d) for d in args.sweep.split(",")]
+        for q in degrees:
+            opq = sfgpu.Operator(sfgpu.OP_LAPLACE, degree=q, n_cells=NCELLS, deform=DEFORM)
+            Nq = opq.n_dofs
+            xq64 = torch.rand(Nq, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1
+            xq32 = xq64.float()
+            yq64 = torch.empty_like(xq64)
+            yq32 = torch.empty_like(xq32)
+            reps64 = max(2, min(args.steps, 6))
+            t64 = time_apply(opq, xq64, yq64, reps64, 2, stream)
+            t32 = time_apply(opq, xq32, yq32, max(3, args.steps), 2, stream)
+            err = float((yq32.double() - yq64).norm() / yq64.norm())
+            b32 = algorithmic_bytes(q, Nq, opq.n_cells, 4)
+            b64 = algorithmic_bytes(q, Nq, opq.n_cells, 8)
+            ent = {"degree": q, "n_dofs": Nq,
+                   "fp32_gdofs": round(Nq / t32 / 1e9, 3), "fp32_hbm_frac": round(b32 / t32 / 1e9 / peak, 4),
+                   "fp64_gdofs": round(Nq / t64 / 1e9, 3), "fp64_hbm_frac": round(b64 / t64 / 1e9 / peak, 4),
+                   "fp32_rel_err_vs_fp64": float("%.3g" % err)}
+            sweep.append(ent)
+            if q == p:
+                fp64_value = ent["fp64_gdofs"]
+            del opq, xq64, xq32, yq64, yq32
+            torch.cuda.empty_cache()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_reference(p, seconds=args.ref_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "continuous Laplacian matvec, deformed %d^3 hex mesh, p=%d, FP32"
+                                   % (args.ncells, p),
+                       "degree": p, "n_cells": list(NCELLS), "n_dofs": N, "deform": DEFORM,
+                       "geometry": "merged 6-entry JxW J^-1 J^-T per Gauss point, FP32",
+                       "dirichlet": True, "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "working set %.2f GB > 129 MB L2, no flush" % (bytes_apply / 1e9),
+                       "fp64_gdofs_same_degree": fp64_value},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "cont_vmult_kernel<5,float,deformed> (8 colour launches per apply)",
+                         "algorithmic_bytes_per_apply": bytes_apply},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk,
+            "gpu_launches": launches_per_apply * args.steps,
+            "sweep": sweep,
+        }
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--degree", type=int, default=4)
+    ap.add_argument("--ncells", type=int, default=64, help="cells per direction")
+    ap.add_argument("--sweep", default="2,3,4,5,6,7,8")
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,199 @@
+/*
+ * sfgpu.h -- C ABI of the GB300 (sm_103a) matrix-free sum-factorization
+ * operators.
+ *
+ * The reference (KKraljic/sum_factorization_kernels, directory legacy/) has
+ * no library interface: its operator "API" is a family of template member
+ * functions of evaluator classes that own their vectors.  Each entry point
+ * below names the member function whose job it takes over; the vectors that
+ * the reference keeps as private members are passed in here as caller-owned
+ * device buffers.
+ *
+ * Conventions
+ *  - Every function returns SF_OK (0) or a negative sf_status; no C++
+ *    exception crosses the ABI.  sf_last_error() describes the last failure
+ *    of the calling thread.
+ *  - Vector and array pointers are DEVICE pointers unless a parameter name
+ *    ends in _host.  They must be aligned to the element size; the library
+ *    never frees them.
+ *  - Work is ordered on the given stream (0 = legacy default stream) and is
+ *    asynchronous unless stated otherwise.  A handle is not re-entrant: calls
+ *    on one handle must not overlap; distinct handles are independent.
+ *  - Precision: SF_FP64 vectors are double, SF_FP32 vectors are float.
+ *
+ * Vector layouts
+ *  - continuous (SF_OP_LAPLACE): global lexicographic nodes of the
+ *    (p*nx+1) x (p*ny+1) x (p*nz+1) grid, x fastest; cell (i,j,k) local node
+ *    (a,b,c) is global ((k*p+c)*(p*ny+1) + (j*p+b))*(p*nx+1) + (i*p+a).
+ *    Restricted to one cell this is the reference's cell-local order
+ *    (evaluation_cell_laplacian.h:157-160).  With homogeneous Dirichlet
+ *    conditions the boundary nodes stay in the vector: the operator reads
+ *    them as zero and its boundary rows are the identity (y_b = x_b).
+ *  - DG (SF_OP_DG_SIPG, SF_OP_DG_ADVECT): cell-major, n^3 values per cell
+ *    in the cell-local order, cells x fastest.  This is the reference's
+ *    lane-interleaved layout (evaluation_dg_laplacian.h:162-166) with one
+ *    lane.
+ */
+#ifndef SFGPU_H
+#define SFGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  SF_OK = 0,
+  SF_ERR_INVALID = -1,      /* bad argument value                              */
+  SF_ERR_NULL = -2,         /* required pointer is NULL                        */
+  SF_ERR_UNSUPPORTED = -3,  /* degree / precision / operator combination       */
+  SF_ERR_CUDA = -4,         /* CUDA runtime error (see sf_last_error)          */
+  SF_ERR_OOM = -5,          /* device allocation failed                        */
+  SF_ERR_NOT_CONVERGED = -6,/* solver hit its iteration limit                  */
+  SF_ERR_BREAKDOWN = -7,    /* solver produced NaN/Inf or a non-positive curvature */
+  SF_ERR_ALIGN = -8,        /* pointer not aligned to its element size         */
+  SF_ERR_STATE = -9         /* call not valid for this handle's configuration  */
+} sf_status;
+
+typedef enum { SF_FP64 = 0, SF_FP32 = 1 } sf_prec;
+
+typedef enum {
+  SF_OP_LAPLACE = 0,   /* continuous FE Laplacian -div(kappa grad u)           */
+  SF_OP_DG_SIPG = 1,   /* DG symmetric interior penalty Laplacian, periodic     */
+  SF_OP_DG_ADVECT = 2  /* DG upwind advection, periodic                        */
+} sf_op_kind;
+
+typedef enum { SF_BASIS_GLL = 0, SF_BASIS_HERMITE = 1 } sf_basis;
+
+typedef struct {
+  int kind;            /* sf_op_kind                                            */
+  int degree;          /* 1..8                                                  */
+  int n_cells[3];      /* hexahedral cells per direction                        */
+  double length[3];    /* domain [0,Lx]x[0,Ly]x[0,Lz]                           */
+  int basis;           /* SF_OP_LAPLACE only (DG SIPG: Hermite-like, DG advect: GLL) */
+  double deform;       /* SF_OP_LAPLACE: amplitude a of the mapping
+                          x_i <- x_i + a sin(2 pi x_j) sin(2 pi x_k), (i,j,k)
+                          cyclic; 0 = affine (geometry not stored)            */
+  int dirichlet;       /* SF_OP_LAPLACE: 1 = homogeneous Dirichlet boundary    */
+  double penalty;      /* SF_OP_DG_SIPG: tau = penalty (p+1)^2 / h_d (ref: 1)  */
+  double velocity[3];  /* SF_OP_DG_ADVECT                                      */
+  int inverse_mass;    /* SF_OP_DG_ADVECT: 1 = apply M^-1 (reference do_matvec) */
+  int precisions;      /* bit 0: prepare FP64, bit 1: prepare FP32             */
+} sf_desc;
+
+typedef struct sf_op sf_op;
+
+const char *sf_last_error(void);
+const char *sf_version(void);
+
+/* Replaces initialize() of the evaluator classes
+ * (evaluation_cell_laplacian.h:34-101, evaluation_dg_laplacian.h:43-108,
+ * evaluation_dg_advect.h:107-180, benchmark_loops.cc:1163-1200): builds the
+ * shape tables and, for a deformed mesh, the per-quadrature-point geometry
+ * on the device (FP64, plus an FP32 copy).  Synchronous. */
+int sf_create(const sf_desc *desc, sf_op **op);
+int sf_destroy(sf_op *op);
+/* number of vector entries, number of cells */
+int sf_sizes(const sf_op *op, long long *n_dofs, long long *n_cells);
+
+/* Overrides the merged geometry of a SF_OP_LAPLACE handle with a deformed
+ * layout: G[cell][6][n^3] (xx,yy,zz,xy,xz,yz; JxW * J^-1 J^-T per Gauss
+ * point), FP64 device array.  Replaces the jacobian_data member
+ * (benchmark_loops.cc:1177-1197). */
+int sf_set_geometry(sf_op *op, const double *merged6);
+/* Per-quadrature-point coefficient kappa[cell][n^3] (FP64 device array),
+ * NULL to remove.  No reference counterpart (new in this library). */
+int sf_set_coefficient(sf_op *op, const double *kappa);
+
+/* y = A x.  Replaces matrix_vector_product() (evaluation_cell_laplacian.h:216,
+ * benchmark_loops.cc:1302) and do_matvec() (evaluation_dg_laplacian.h:121,
+ * evaluation_dg_advect.h:216). */
+int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream);
+/* y = A^T x.  The Laplacians are symmetric (A^T = A); for advection this is
+ * the transpose-upwind adjoint.  No reference counterpart. */
+int sf_vmult_transpose(sf_op *op, int prec, const void *x, void *y, void *stream);
+/* y[r] = A x[r] for r < nrhs; x and y hold nrhs vectors of n_dofs entries
+ * back to back.  One launch for all right-hand sides. */
+int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void *stream);
+int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, void *y,
+                               void *stream);
+
+/* Fused Chebyshev step, replaces do_cheby_iter<true>
+ * (evaluation_dg_laplacian.h:513-554, fused update :485-502):
+ *   t     <- c_tm * t + c_np * diag_inv .* (A x_old - b)
+ *   x_new <- x_old - t
+ * (the reference reads its member vector sol_rhs for b; this uses b). */
+int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv,
+                      const void *x_old, void *x_new, void *t, double c_np,
+                      double c_tm, void *stream);
+/* The same update without the operator, replaces
+ * emulate_cheby_vector_updates() (evaluation_dg_laplacian.h:556-601):
+ *   t <- c_tm * t + c_np * diag_inv .* (ax - b);  x_new <- x_old - t */
+int sf_vector_update(long long n, int prec, const void *ax, const void *b,
+                     const void *diag_inv, const void *x_old, void *x_new, void *t,
+                     double c_np, double c_tm, void *stream);
+
+/* Diagonal of A (for Jacobi / Chebyshev).  The reference uses a placeholder
+ * of ones (evaluation_dg_laplacian.h:88). */
+int sf_diagonal(sf_op *op, int prec, void *diag, void *stream);
+
+/* d(loss)/d(kappa_q) = grad(u)_q . G_q grad(lam)_q per Gauss point
+ * (FP64/FP32 u, lam; output [cell][n^3] of the same precision), gradients
+ * recomputed.  With lam = A x - b and u = x this is the kappa-gradient of
+ * 1/2 |A(kappa) x - b|^2.  No reference counterpart. */
+int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void *dkappa,
+                      void *stream);
+
+/* ---------------- conjugate gradients ---------------- */
+typedef enum {
+  SF_SOLVE_FP64 = 0,        /* plain CG, FP64 operator                          */
+  SF_SOLVE_MIXED = 1        /* FP64 outer iterative refinement around an FP32
+                               preconditioned CG inner solve                   */
+} sf_solve_mode;
+
+typedef enum { SF_PRECOND_NONE = 0, SF_PRECOND_JACOBI = 1, SF_PRECOND_CHEBYSHEV = 2 } sf_precond;
+
+typedef struct {
+  int mode;              /* sf_solve_mode                                        */
+  int precond;           /* sf_precond                                           */
+  int cheb_degree;       /* Chebyshev polynomial degree (default 5)              */
+  double cheb_range;     /* smoothing range lambda_max / lambda_min (default 15) */
+  int eig_iterations;    /* Lanczos steps for lambda_max (default 12)            */
+  double rtol;           /* relative residual target |b - A x| / |b|             */
+  int max_iter;          /* total inner iterations allowed                       */
+  double inner_rtol;     /* SF_SOLVE_MIXED: inner relative tolerance (1e-3)     */
+  int project_constant;  /* 1: remove the mean from b and x (periodic SIPG)      */
+} sf_solve_opts;
+
+typedef struct {
+  int iterations;        /* CG iterations (inner, for SF_SOLVE_MIXED)            */
+  int outer_iterations;  /* refinement steps (SF_SOLVE_MIXED)                    */
+  double rel_residual;   /* final |b - A x| / |b| in FP64                        */
+  double lambda_max;     /* estimate used by the Chebyshev preconditioner        */
+  double seconds;        /* wall time of the solve (device synchronised)         */
+  int operator_applies;  /* number of operator applications                      */
+} sf_solve_stats;
+
+void sf_solve_opts_default(sf_solve_opts *opts);
+/* Solves A x = b (FP64 device vectors, x holds the initial guess).  No
+ * reference counterpart: the reference has no solver.  Synchronous. */
+int sf_cg_solve(sf_op *op, const double *b, double *x, const sf_solve_opts *opts,
+                sf_solve_stats *stats, void *stream);
+
+/* ---------------- utilities ---------------- */
+/* FP64 <-> FP32 vector conversion */
+int sf_convert(long long n, int from_prec, const void *x, int to_prec, void *y, void *stream);
+/* deterministic FP64 dot product of two vectors of precision prec; the result
+ * is written to a device double (result_dev) -- no host synchronisation */
+int sf_dot(long long n, int prec, const void *x, const void *y, double *result_dev,
+           void *stream);
+/* shape tables used by the kernels (FP64, for inspection and tests):
+ * S[q*n+i], D[q*n+j], weights[n]; n = degree+1 */
+int sf_shape_tables(int degree, int basis, double *S_host, double *D_host,
+                    double *points_host, double *weights_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

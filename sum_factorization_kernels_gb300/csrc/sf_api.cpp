@@ -1,0 +1,377 @@
+// sf_api.cpp -- the C ABI (include/sfgpu.h): argument validation, handle
+// state, dispatch to the kernel launchers.  No exception leaves this file.
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "sf_internal.h"
+#include "sf_launch.h"
+
+namespace sf {
+
+static thread_local std::string g_error;
+
+void set_error(const std::string &msg) { g_error = msg; }
+
+int DevBuf::alloc(size_t b)
+{
+  release();
+  if (b == 0) return SF_OK;
+  cudaError_t e = cudaMalloc(&ptr, b);
+  if (e != cudaSuccess) {
+    ptr = nullptr;
+    (void)cudaGetLastError();
+    set_error(std::string("cudaMalloc(") + std::to_string(b) + " bytes): " + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? SF_ERR_OOM : SF_ERR_CUDA;
+  }
+  bytes = b;
+  return SF_OK;
+}
+
+void DevBuf::release()
+{
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+} // namespace sf
+
+using namespace sf;
+
+namespace {
+
+int fail(int code, const std::string &msg)
+{
+  set_error(msg);
+  return code;
+}
+
+size_t elem_size(int prec) { return prec == SF_FP64 ? sizeof(double) : sizeof(float); }
+
+int check_prec(const sf_op *op, int prec)
+{
+  if (prec != SF_FP64 && prec != SF_FP32) return fail(SF_ERR_INVALID, "precision must be SF_FP64 or SF_FP32");
+  const int bit = prec == SF_FP64 ? 1 : 2;
+  if (op && !(op->desc.precisions & bit))
+    return fail(SF_ERR_STATE, "precision not prepared by sf_create (desc.precisions)");
+  return SF_OK;
+}
+
+int check_ptr(const void *p, int prec, const char *name)
+{
+  if (!p) return fail(SF_ERR_NULL, std::string(name) + " is NULL");
+  if (reinterpret_cast<uintptr_t>(p) % elem_size(prec) != 0)
+    return fail(SF_ERR_ALIGN, std::string(name) + " is not aligned to its element size");
+  return SF_OK;
+}
+
+#define SF_RET(x)                                                              \
+  do {                                                                         \
+    int r_ = (x);                                                              \
+    if (r_ != SF_OK) return r_;                                                \
+  } while (0)
+
+int prepare_geometry(sf_op *op)
+{
+  const long long n3 = (long long)op->n * op->n * op->n;
+  op->geo_stride = (6 * n3 + 3) / 4 * 4; // 16-byte aligned cell blocks in FP32
+  const size_t entries = (size_t)op->n_cells * op->geo_stride;
+  if (op->desc.precisions & 1) SF_RET(op->geo64.alloc(entries * sizeof(double)));
+  // FP64 geometry is always computed; keep a temporary if FP64 is not prepared
+  DevBuf tmp;
+  double *G64 = (double *)op->geo64.ptr;
+  if (!G64) {
+    SF_RET(tmp.alloc(entries * sizeof(double)));
+    G64 = (double *)tmp.ptr;
+  }
+  SF_RET(launch_geometry(op, G64, 0));
+  if (op->desc.precisions & 2) {
+    SF_RET(op->geo32.alloc(entries * sizeof(float)));
+    SF_RET(launch_convert((long long)entries, SF_FP64, G64, SF_FP32, op->geo32.ptr, 0));
+  }
+  SF_CUDA_TRY(cudaDeviceSynchronize());
+  return SF_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *sf_last_error(void) { return g_error.c_str(); }
+
+const char *sf_version(void) { return "sfgpu 0.1 (sm_103a)"; }
+
+int sf_create(const sf_desc *desc, sf_op **out)
+{
+  if (!desc || !out) return fail(SF_ERR_NULL, "desc/op is NULL");
+  *out = nullptr;
+  const sf_desc &d = *desc;
+  if (d.kind < SF_OP_LAPLACE || d.kind > SF_OP_DG_ADVECT) return fail(SF_ERR_INVALID, "unknown operator kind");
+  if (d.degree < 1 || d.degree > kMaxDegree) return fail(SF_ERR_UNSUPPORTED, "degree must be 1..8");
+  for (int k = 0; k < 3; ++k) {
+    if (d.n_cells[k] < 1 || d.n_cells[k] > (1 << 20)) return fail(SF_ERR_INVALID, "n_cells out of range");
+    if (!(d.length[k] > 0.0)) return fail(SF_ERR_INVALID, "length must be positive");
+  }
+  if ((d.precisions & 3) == 0) return fail(SF_ERR_INVALID, "precisions must select FP64 and/or FP32");
+  if (d.kind == SF_OP_LAPLACE && d.basis != SF_BASIS_GLL && d.basis != SF_BASIS_HERMITE)
+    return fail(SF_ERR_INVALID, "unknown basis");
+  if (d.kind == SF_OP_DG_SIPG && !(d.penalty > 0.0)) return fail(SF_ERR_INVALID, "penalty must be positive");
+  if (d.kind == SF_OP_LAPLACE && !(d.deform >= 0.0 && d.deform < 0.15))
+    return fail(SF_ERR_INVALID, "deform amplitude must be in [0, 0.15) to keep the mapping invertible");
+  sf_op *op = new (std::nothrow) sf_op();
+  if (!op) return fail(SF_ERR_OOM, "host allocation failed");
+  op->desc = d;
+  const int basis = d.kind == SF_OP_LAPLACE ? d.basis : (d.kind == SF_OP_DG_SIPG ? SF_BASIS_HERMITE : SF_BASIS_GLL);
+  op->desc.basis = basis;
+  fill_shape(d.degree, basis, op->shape);
+  op->n = d.degree + 1;
+  for (int k = 0; k < 3; ++k) op->h[k] = d.length[k] / d.n_cells[k];
+  op->n_cells = (long long)d.n_cells[0] * d.n_cells[1] * d.n_cells[2];
+  const long long n3 = (long long)op->n * op->n * op->n;
+  if (d.kind == SF_OP_LAPLACE)
+    op->n_dofs = ((long long)d.degree * d.n_cells[0] + 1) * ((long long)d.degree * d.n_cells[1] + 1) *
+                 ((long long)d.degree * d.n_cells[2] + 1);
+  else
+    op->n_dofs = op->n_cells * n3;
+  if (op->n_dofs >= (1LL << 40)) {
+    delete op;
+    return fail(SF_ERR_INVALID, "problem too large");
+  }
+  if (d.kind == SF_OP_LAPLACE && d.deform > 0.0) {
+    op->deformed = true;
+    int r = prepare_geometry(op);
+    if (r != SF_OK) {
+      delete op;
+      return r;
+    }
+  }
+  *out = op;
+  return SF_OK;
+}
+
+int sf_destroy(sf_op *op)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  delete op;
+  return SF_OK;
+}
+
+int sf_sizes(const sf_op *op, long long *n_dofs, long long *n_cells)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (n_dofs) *n_dofs = op->n_dofs;
+  if (n_cells) *n_cells = op->n_cells;
+  return SF_OK;
+}
+
+int sf_set_geometry(sf_op *op, const double *G)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (op->desc.kind != SF_OP_LAPLACE) return fail(SF_ERR_STATE, "geometry only for SF_OP_LAPLACE");
+  SF_RET(check_ptr(G, SF_FP64, "merged6"));
+  const long long n3 = (long long)op->n * op->n * op->n;
+  op->geo_stride = (6 * n3 + 3) / 4 * 4;
+  const size_t entries = (size_t)op->n_cells * op->geo_stride;
+  DevBuf tmp;
+  double *G64;
+  if (op->desc.precisions & 1) {
+    if (op->geo64.bytes != entries * sizeof(double)) SF_RET(op->geo64.alloc(entries * sizeof(double)));
+    G64 = (double *)op->geo64.ptr;
+  } else {
+    SF_RET(tmp.alloc(entries * sizeof(double)));
+    G64 = (double *)tmp.ptr;
+  }
+  SF_CUDA_TRY(cudaMemcpy2D(G64, op->geo_stride * sizeof(double), G, 6 * n3 * sizeof(double),
+                           6 * n3 * sizeof(double), (size_t)op->n_cells, cudaMemcpyDeviceToDevice));
+  if (op->desc.precisions & 2) {
+    if (op->geo32.bytes != entries * sizeof(float)) SF_RET(op->geo32.alloc(entries * sizeof(float)));
+    SF_RET(launch_convert((long long)entries, SF_FP64, G64, SF_FP32, op->geo32.ptr, 0));
+  }
+  SF_CUDA_TRY(cudaDeviceSynchronize());
+  op->deformed = true;
+  return SF_OK;
+}
+
+int sf_set_coefficient(sf_op *op, const double *kappa)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (op->desc.kind != SF_OP_LAPLACE) return fail(SF_ERR_STATE, "coefficient only for SF_OP_LAPLACE");
+  if (!kappa) {
+    op->kap64.release();
+    op->kap32.release();
+    op->has_kappa = false;
+    return SF_OK;
+  }
+  SF_RET(check_ptr(kappa, SF_FP64, "kappa"));
+  const long long n3 = (long long)op->n * op->n * op->n;
+  const size_t entries = (size_t)op->n_cells * n3;
+  if (op->desc.precisions & 1) {
+    if (op->kap64.bytes != entries * sizeof(double)) SF_RET(op->kap64.alloc(entries * sizeof(double)));
+    SF_CUDA_TRY(cudaMemcpy(op->kap64.ptr, kappa, entries * sizeof(double), cudaMemcpyDeviceToDevice));
+  }
+  if (op->desc.precisions & 2) {
+    if (op->kap32.bytes != entries * sizeof(float)) SF_RET(op->kap32.alloc(entries * sizeof(float)));
+    SF_RET(launch_convert((long long)entries, SF_FP64, kappa, SF_FP32, op->kap32.ptr, 0));
+  }
+  SF_CUDA_TRY(cudaDeviceSynchronize());
+  op->has_kappa = true;
+  return SF_OK;
+}
+
+int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  SF_RET(check_prec(op, prec));
+  SF_RET(check_ptr(x, prec, "x"));
+  SF_RET(check_ptr(y, prec, "y"));
+  if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (op->desc.kind == SF_OP_LAPLACE) return launch_cont_vmult(op, prec, x, y, st);
+  return launch_dg_vmult(op, prec, 1, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
+}
+
+int sf_vmult_transpose(sf_op *op, int prec, const void *x, void *y, void *stream)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (op->desc.kind != SF_OP_DG_ADVECT) return sf_vmult(op, prec, x, y, stream);
+  return sf_vmult_transpose_batched(op, prec, 1, x, y, stream);
+}
+
+int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void *stream)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  SF_RET(check_prec(op, prec));
+  SF_RET(check_ptr(x, prec, "x"));
+  SF_RET(check_ptr(y, prec, "y"));
+  if (nrhs < 1 || nrhs > 64) return fail(SF_ERR_INVALID, "nrhs must be 1..64");
+  if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (op->desc.kind == SF_OP_LAPLACE) {
+    const size_t es = elem_size(prec);
+    for (int r = 0; r < nrhs; ++r)
+      SF_RET(launch_cont_vmult(op, prec, (const char *)x + r * op->n_dofs * es,
+                               (char *)y + r * op->n_dofs * es, st));
+    return SF_OK;
+  }
+  return launch_dg_vmult(op, prec, nrhs, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
+}
+
+int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void *stream)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (op->desc.kind != SF_OP_DG_ADVECT) return sf_vmult_batched(op, prec, nrhs, x, y, stream);
+  SF_RET(check_prec(op, prec));
+  SF_RET(check_ptr(x, prec, "x"));
+  SF_RET(check_ptr(y, prec, "y"));
+  if (nrhs < 1 || nrhs > 64) return fail(SF_ERR_INVALID, "nrhs must be 1..64");
+  if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
+  cudaStream_t st = (cudaStream_t)stream;
+  const void *src = x;
+  if (op->desc.inverse_mass) {
+    const size_t bytes = (size_t)nrhs * op->n_dofs * elem_size(prec);
+    if (op->scratch.bytes < bytes) SF_RET(op->scratch.alloc(bytes));
+    SF_RET(launch_dg_inverse_mass(op, prec, nrhs, x, op->scratch.ptr, st));
+    src = op->scratch.ptr;
+  }
+  return launch_dg_vmult(op, prec, nrhs, true, src, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
+}
+
+int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv, const void *x_old,
+                      void *x_new, void *t, double c_np, double c_tm, void *stream)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  SF_RET(check_prec(op, prec));
+  SF_RET(check_ptr(b, prec, "b"));
+  SF_RET(check_ptr(diag_inv, prec, "diag_inv"));
+  SF_RET(check_ptr(x_old, prec, "x_old"));
+  SF_RET(check_ptr(x_new, prec, "x_new"));
+  SF_RET(check_ptr(t, prec, "t"));
+  if (x_old == x_new) return fail(SF_ERR_INVALID, "x_old and x_new must not alias");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (op->desc.kind == SF_OP_DG_SIPG || op->desc.kind == SF_OP_DG_ADVECT)
+    return launch_dg_vmult(op, prec, 1, false, x_old, x_new, b, diag_inv, t, c_np, c_tm, st);
+  // continuous: operator into x_new, then the fused vector update in place
+  SF_RET(launch_cont_vmult(op, prec, x_old, x_new, st));
+  return launch_vector_update(op->n_dofs, prec, x_new, b, diag_inv, x_old, x_new, t, c_np, c_tm, st);
+}
+
+int sf_vector_update(long long n, int prec, const void *ax, const void *b, const void *diag_inv,
+                     const void *x_old, void *x_new, void *t, double c_np, double c_tm, void *stream)
+{
+  SF_RET(check_prec(nullptr, prec));
+  if (n < 0) return fail(SF_ERR_INVALID, "n < 0");
+  SF_RET(check_ptr(ax, prec, "ax"));
+  SF_RET(check_ptr(b, prec, "b"));
+  SF_RET(check_ptr(diag_inv, prec, "diag_inv"));
+  SF_RET(check_ptr(x_old, prec, "x_old"));
+  SF_RET(check_ptr(x_new, prec, "x_new"));
+  SF_RET(check_ptr(t, prec, "t"));
+  if (n == 0) return SF_OK;
+  return launch_vector_update(n, prec, ax, b, diag_inv, x_old, x_new, t, c_np, c_tm,
+                              (cudaStream_t)stream);
+}
+
+int sf_diagonal(sf_op *op, int prec, void *diag, void *stream)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  SF_RET(check_prec(op, prec));
+  SF_RET(check_ptr(diag, prec, "diag"));
+  if (op->desc.kind == SF_OP_LAPLACE) return launch_cont_diagonal(op, prec, diag, (cudaStream_t)stream);
+  return launch_dg_diagonal(op, prec, diag, (cudaStream_t)stream);
+}
+
+int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void *dkappa, void *stream)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (op->desc.kind != SF_OP_LAPLACE) return fail(SF_ERR_STATE, "kappa gradient only for SF_OP_LAPLACE");
+  SF_RET(check_prec(op, prec));
+  SF_RET(check_ptr(u, prec, "u"));
+  SF_RET(check_ptr(lam, prec, "lam"));
+  SF_RET(check_ptr(dkappa, prec, "dkappa"));
+  return launch_cont_kappa_grad(op, prec, u, lam, dkappa, (cudaStream_t)stream);
+}
+
+int sf_convert(long long n, int from_prec, const void *x, int to_prec, void *y, void *stream)
+{
+  SF_RET(check_prec(nullptr, from_prec));
+  SF_RET(check_prec(nullptr, to_prec));
+  SF_RET(check_ptr(x, from_prec, "x"));
+  SF_RET(check_ptr(y, to_prec, "y"));
+  if (n < 0) return fail(SF_ERR_INVALID, "n < 0");
+  if (n == 0) return SF_OK;
+  return launch_convert(n, from_prec, x, to_prec, y, (cudaStream_t)stream);
+}
+
+int sf_dot(long long n, int prec, const void *x, const void *y, double *result_dev, void *stream)
+{
+  SF_RET(check_prec(nullptr, prec));
+  SF_RET(check_ptr(x, prec, "x"));
+  SF_RET(check_ptr(y, prec, "y"));
+  SF_RET(check_ptr(result_dev, SF_FP64, "result_dev"));
+  if (n < 0) return fail(SF_ERR_INVALID, "n < 0");
+  // per-thread scratch for the partial sums (allocated once per thread)
+  static thread_local DevBuf scratch;
+  if (!scratch.ptr) SF_RET(scratch.alloc(sizeof(double) * kDotBlocks));
+  return launch_dot(n, prec, x, y, (double *)scratch.ptr, result_dev, (cudaStream_t)stream);
+}
+
+int sf_shape_tables(int degree, int basis, double *S, double *D, double *pts, double *w)
+{
+  Shape1D s;
+  if (fill_shape(degree, basis, s) != 0) return fail(SF_ERR_UNSUPPORTED, "degree must be 1..8");
+  const int n = s.n;
+  for (int q = 0; q < n; ++q)
+    for (int i = 0; i < n; ++i) {
+      if (S) S[q * n + i] = s.S[q][i];
+      if (D) D[q * n + i] = s.D[q][i];
+    }
+  for (int q = 0; q < n; ++q) {
+    if (pts) pts[q] = s.xq[q];
+    if (w) w[q] = s.wq[q];
+  }
+  return SF_OK;
+}
+
+} // extern "C"

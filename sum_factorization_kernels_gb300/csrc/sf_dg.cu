@@ -1,0 +1,588 @@
+// sf_dg.cu -- DG operators on periodic Cartesian meshes: symmetric interior
+// penalty Laplacian (Hermite-like basis) and upwind advection (GLL basis,
+// optional inverse mass matrix), forward and transpose, several right-hand
+// sides per launch, fused Chebyshev epilogue.
+//
+// Mathematics of evaluation_dg_laplacian.h:130-510 and
+// evaluation_dg_advect.h:286-676: values and collocation gradients at Gauss
+// points, face values/normal derivatives of the own cell extrapolated from
+// the Gauss-point values, those of the neighbour read from one node layer
+// (value) and two node layers (normal derivative, Hermite-like basis), SIPG
+// flux -{du/dn}[v] - [u]{dv/dn} + tau [u][v] with tau = penalty (p+1)^2 / h,
+// upwind flux (a.n) u_upwind, integration with the transposed matrices and
+// face injection.  Corrections relative to the reference: periodic x
+// neighbour index, transposed values in the last SIPG sweep.
+//
+// GPU mapping: a block holds CPB consecutive cells (n^2 threads each); the
+// block's cell data is one contiguous range of the vector, so it is loaded
+// and stored with coalesced vector accesses; each 1D sweep is line-local in
+// shared memory (see sf_laplace.cu); each thread also owns one point of each
+// face pair of its line, so the face fluxes are computed in the thread that
+// holds the matching line.
+#include "sf_device.cuh"
+#include "sf_internal.h"
+#include "sf_launch.h"
+#include "sf_tables.h"
+
+namespace sf {
+
+namespace {
+
+enum { K_SIPG = 0, K_ADVECT = 1 };
+
+template <int N, typename T>
+struct DGArgs {
+  EOMat<N, T> S, ST, D, DT, P;   // P = Sinv (Gauss values -> GLL nodes)
+  T fv0[N], fv1[N], fd0[N], fd1[N];
+  T w[N];
+  T ij[3];        // inverse cell sizes
+  T jxw;          // cell volume
+  T jface[3];     // face area elements jxw * ij_d
+  T tau[3];       // SIPG penalty per direction
+  T cdir[3];      // SIPG: ij_d^2 jxw ; advection: a_d ij_d jxw
+  T an[3];        // advection velocity a_d
+  T hd0;          // derivative of the first Hermite-like function at 0
+  const T *__restrict__ x;
+  T *__restrict__ y;
+  const T *__restrict__ cb;      // Chebyshev: rhs
+  const T *__restrict__ cdinv;   // Chebyshev: inverse diagonal
+  T *__restrict__ ct;            // Chebyshev: t
+  T c_np, c_tm;
+  int nc[3];
+  long long n_cells, n_dofs;
+};
+
+template <int N>
+struct DGCells {
+  // cells per block, about 128-256 threads
+  static constexpr int value = N == 2 ? 32 : N == 3 ? 14 : N == 4 ? 8 : N == 5 ? 5 : N == 6 ? 7
+                               : N == 7 ? 5 : N == 8 ? 2 : 3;
+};
+
+template <int N, typename T>
+__device__ __forceinline__ long long neighbour(const DGArgs<N, T> &A, long long cell, int dir, int side)
+{
+  long long ix = cell % A.nc[0];
+  long long iy = (cell / A.nc[0]) % A.nc[1];
+  long long iz = cell / ((long long)A.nc[0] * A.nc[1]);
+  const int d = side ? 1 : -1;
+  if (dir == 0) ix = (ix + d + A.nc[0]) % A.nc[0];
+  if (dir == 1) iy = (iy + d + A.nc[1]) % A.nc[1];
+  if (dir == 2) iz = (iz + d + A.nc[2]) % A.nc[2];
+  return (iz * A.nc[1] + iy) * A.nc[0] + ix;
+}
+
+// face flux at one face point.  side 0: face at coordinate 0 (outer normal
+// -e_d), side 1: at 1 (+e_d).  um/dm: own value and reference-coordinate
+// derivative, up/dp: neighbour's.  Returns the value-test coefficient in fv
+// and the derivative-test coefficient in fd (SIPG).
+template <int KIND, bool TRANSPOSE, int N, typename T>
+__device__ __forceinline__ void face_flux(const DGArgs<N, T> &A, int d, int side, T um, T dm, T up,
+                                          T dp, T wf, T &fv, T &fd)
+{
+  if (KIND == K_SIPG) {
+    const T sgn = side ? T(-1) : T(1);
+    const T jump = um - up;
+    const T avg = sgn * T(0.5) * A.ij[d] * (dm + dp);
+    fv = (avg + jump * A.tau[d]) * A.jface[d] * wf;
+    fd = sgn * (T(0.5) * A.ij[d] * A.jface[d]) * jump * wf;
+  } else {
+    const T an = side ? A.an[d] : -A.an[d];
+    const T aa = an < T(0) ? -an : an;
+    if (TRANSPOSE)
+      fv = T(-0.5) * (an + aa) * (um - up) * A.jface[d] * wf;
+    else
+      fv = T(-0.5) * ((um + up) * an + aa * (um - up)) * A.jface[d] * wf;
+    fd = T(0);
+  }
+}
+
+// Everything for one line of direction d held by this thread: values at Gauss
+// points u[], neighbour face data at index fi, produce the line residual r[]
+// (collocation space) = cell term + face injections.
+template <int KIND, bool TRANSPOSE, int N, typename T>
+__device__ __forceinline__ void line_residual(const DGArgs<N, T> &A, int d, const T (&u)[N], T wt,
+                                              const T *F, int fi, T (&r)[N])
+{
+  constexpr int N2 = N * N;
+  // own face values/derivatives (reference coordinates)
+  const T vm = dot_row<N, T>(A.fv0, u), vp = dot_row<N, T>(A.fv1, u);
+  T dm = T(0), dp = T(0);
+  if (KIND == K_SIPG) {
+    dm = dot_row<N, T>(A.fd0, u);
+    dp = dot_row<N, T>(A.fd1, u);
+  }
+  const T *Fm = F + (4 * d) * N2, *Fp = F + (4 * d + 2) * N2;
+  T fvm, fdm, fvp, fdp;
+  face_flux<KIND, TRANSPOSE, N, T>(A, d, 0, vm, dm, Fm[fi], KIND == K_SIPG ? Fm[N2 + fi] : T(0), wt,
+                                   fvm, fdm);
+  face_flux<KIND, TRANSPOSE, N, T>(A, d, 1, vp, dp, Fp[fi], KIND == K_SIPG ? Fp[N2 + fi] : T(0), wt,
+                                   fvp, fdp);
+  T g[N];
+  if (KIND == K_SIPG) {
+    eo_apply<N, -1>(A.D, u, g);
+#pragma unroll
+    for (int m = 0; m < N; ++m) g[m] *= A.cdir[d] * A.w[m] * wt;
+    eo_apply<N, -1>(A.DT, g, r);
+  } else if (!TRANSPOSE) {
+#pragma unroll
+    for (int m = 0; m < N; ++m) g[m] = A.cdir[d] * A.w[m] * wt * u[m];
+    eo_apply<N, -1>(A.DT, g, r);
+  } else {
+    eo_apply<N, -1>(A.D, u, g);
+#pragma unroll
+    for (int m = 0; m < N; ++m) r[m] = A.cdir[d] * A.w[m] * wt * g[m];
+  }
+#pragma unroll
+  for (int m = 0; m < N; ++m) {
+    r[m] = fma(A.fv0[m], fvm, r[m]);
+    r[m] = fma(A.fv1[m], fvp, r[m]);
+    if (KIND == K_SIPG) {
+      r[m] = fma(A.fd0[m], fdm, r[m]);
+      r[m] = fma(A.fd1[m], fdp, r[m]);
+    }
+  }
+}
+
+template <int N, typename T, int KIND, bool TRANSPOSE, bool INVMASS, bool CHEB>
+__global__ void __launch_bounds__(DGCells<N>::value *N *N)
+    dg_kernel(const __grid_constant__ DGArgs<N, T> A)
+{
+  constexpr int N2 = N * N, N3 = N * N * N;
+  constexpr int CPB = DGCells<N>::value;
+  constexpr int NF = KIND == K_SIPG ? 12 : 6; // face arrays per cell
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *smem = reinterpret_cast<T *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int cs = tid / N2;
+  const int t = tid - cs * N2;
+  const int a = t % N, b = t / N;
+  const long long cell0 = (long long)blockIdx.x * CPB;
+  const long long cell = cell0 + cs;
+  const bool valid = cell < A.n_cells;
+  const long long roff = (long long)blockIdx.y * A.n_dofs; // right-hand side offset
+  const T *__restrict__ x = A.x + roff;
+  T *Bblk = smem;                       // CPB cells x n^3: input / results
+  T *B0 = Bblk + cs * N3;
+  T *B1 = smem + CPB * N3 + cs * N3;    // Gauss-point values
+  T *B2 = smem + 2 * CPB * N3 + cs * N3;
+  // face arrays: [dir][side][value, derivative][n^2]  (SIPG), values only (advection)
+  T *F = smem + 3 * CPB * N3 + cs * (12 * N2);
+
+  // ---- coalesced load of the block's cells ----
+  const long long ncell_blk = min((long long)CPB, A.n_cells - cell0);
+  const long long nval = ncell_blk * N3;
+  const T *src = x + cell0 * N3;
+  for (long long e = tid; e < nval; e += blockDim.x) Bblk[e] = __ldg(src + e);
+  // ---- neighbour face layers ----
+  if (valid) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      // face-local index t: x faces (b,c) = (t%N, t/N), y faces (a,c), z faces (a,b)
+      const int f0 = t % N, f1 = t / N;
+      long long base_in[2];
+      int stride_n;
+      // offset of the face point inside a cell, without the normal coordinate
+      int off;
+      if (d == 0) { off = N * f0 + N2 * f1; stride_n = 1; }
+      else if (d == 1) { off = f0 + N2 * f1; stride_n = N; }
+      else { off = f0 + N * f1; stride_n = N2; }
+      base_in[0] = neighbour(A, cell, d, 0) * N3 + off;
+      base_in[1] = neighbour(A, cell, d, 1) * N3 + off;
+      // side 0 (face at 0): neighbour's layer p (value) and p-1; side 1: layers 0 and 1
+      const T v0 = __ldg(x + base_in[0] + (N - 1) * stride_n);
+      const T v1 = __ldg(x + base_in[1]);
+      F[(4 * d + 0) * N2 + t] = v0;
+      F[(4 * d + 2) * N2 + t] = v1;
+      if (KIND == K_SIPG) {
+        const T u0 = __ldg(x + base_in[0] + (N - 2) * stride_n);
+        const T u1 = __ldg(x + base_in[1] + stride_n);
+        F[(4 * d + 1) * N2 + t] = A.hd0 * (u0 - v0);
+        F[(4 * d + 3) * N2 + t] = -A.hd0 * (u1 - v1);
+      }
+    }
+  }
+  __syncthreads();
+  T v[N], r[N];
+  // ---- z sweep of the cell, first tangential direction of the faces ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B0[t + N2 * m];
+  eo_apply<N, 1>(A.S, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B0[t + N2 * m] = v[m];
+  for (int task = t; task < NF * N; task += N2) {
+    const int arr = task / N, line = task % N;
+    const int k = KIND == K_SIPG ? arr : 2 * arr; // advection uses the value arrays only
+    T *Fa = F + k * N2 + line * N;
+#pragma unroll
+    for (int m = 0; m < N; ++m) v[m] = Fa[m];
+    eo_apply<N, 1>(A.S, v, v);
+#pragma unroll
+    for (int m = 0; m < N; ++m) Fa[m] = v[m];
+  }
+  __syncthreads();
+  // ---- x sweep, second tangential direction of the faces ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B0[N * t + m];
+  eo_apply<N, 1>(A.S, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B0[N * t + m] = v[m];
+  for (int task = t; task < NF * N; task += N2) {
+    const int arr = task / N, line = task % N;
+    const int k = KIND == K_SIPG ? arr : 2 * arr;
+    T *Fa = F + k * N2 + line;
+#pragma unroll
+    for (int m = 0; m < N; ++m) v[m] = Fa[N * m];
+    eo_apply<N, 1>(A.S, v, v);
+#pragma unroll
+    for (int m = 0; m < N; ++m) Fa[N * m] = v[m];
+  }
+  __syncthreads();
+  // ---- y lines: Gauss-point values, y residual ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B0[a + N * m + N2 * b];
+  eo_apply<N, 1>(A.S, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B1[a + N * m + N2 * b] = v[m];
+  // y line t = (a, c=b): face point (a, c) has weight w_a w_c
+  line_residual<KIND, TRANSPOSE, N, T>(A, 1, v, A.w[a] * A.w[b], F, t, r);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B2[a + N * m + N2 * b] = r[m];
+  __syncthreads();
+  // ---- x lines and z lines ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B1[N * t + m];
+  // x line t = (b, c) = (t%N, t/N)
+  line_residual<KIND, TRANSPOSE, N, T>(A, 0, v, A.w[a] * A.w[b], F, t, r);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B0[N * t + m] = r[m];
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B1[t + N2 * m];
+  T rz[N];
+  line_residual<KIND, TRANSPOSE, N, T>(A, 2, v, A.w[a] * A.w[b], F, t, rz);
+  __syncthreads();
+  // ---- sum, then integrate / apply the inverse mass along z ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = rz[m] + B0[t + N2 * m] + B2[t + N2 * m];
+  if (INVMASS) {
+    const T wab = A.w[a] * A.w[b];
+#pragma unroll
+    for (int m = 0; m < N; ++m) v[m] = v[m] / (A.jxw * wab * A.w[m]);
+    eo_apply<N, 1>(A.P, v, v);
+  } else {
+    eo_apply<N, 1>(A.ST, v, v);
+  }
+#pragma unroll
+  for (int m = 0; m < N; ++m) B1[t + N2 * m] = v[m];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B1[N * t + m];
+  if (INVMASS) eo_apply<N, 1>(A.P, v, v);
+  else eo_apply<N, 1>(A.ST, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B1[N * t + m] = v[m];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B1[a + N * m + N2 * b];
+  if (INVMASS) eo_apply<N, 1>(A.P, v, v);
+  else eo_apply<N, 1>(A.ST, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B1[a + N * m + N2 * b] = v[m];
+  __syncthreads();
+  // ---- coalesced store (plain or fused Chebyshev update) ----
+  T *Rblk = smem + CPB * N3;
+  T *dst = A.y + roff + cell0 * N3;
+  if (CHEB) {
+    const long long o = cell0 * N3;
+    for (long long e = tid; e < nval; e += blockDim.x) {
+      const T res = Rblk[e] - A.cb[o + e];
+      const T tn = A.c_tm * A.ct[o + e] + A.c_np * A.cdinv[o + e] * res;
+      A.ct[o + e] = tn;
+      dst[e] = __ldg(x + o + e) - tn;
+    }
+  } else {
+    for (long long e = tid; e < nval; e += blockDim.x) dst[e] = Rblk[e];
+  }
+}
+
+// cell-local inverse mass matrix M^-1 = P W^-1 P^T (GLL basis, Gauss points)
+template <int N, typename T>
+__global__ void __launch_bounds__(DGCells<N>::value *N *N)
+    dg_inverse_mass_kernel(const __grid_constant__ DGArgs<N, T> A)
+{
+  constexpr int N2 = N * N, N3 = N * N * N;
+  constexpr int CPB = DGCells<N>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *smem = reinterpret_cast<T *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int cs = tid / N2;
+  const int t = tid - cs * N2;
+  const int a = t % N, b = t / N;
+  const long long cell0 = (long long)blockIdx.x * CPB;
+  const long long roff = (long long)blockIdx.y * A.n_dofs;
+  T *B = smem + cs * N3;
+  const long long nval = min((long long)CPB, A.n_cells - cell0) * N3;
+  const T *src = A.x + roff + cell0 * N3;
+  for (long long e = tid; e < nval; e += blockDim.x) smem[e] = __ldg(src + e);
+  __syncthreads();
+  // P^T in z, x, y; scale; P in z, x, y  (P^T = transposed Sinv)
+  EOMat<N, T> PT; // built on the fly from P: transposed tables passed in ST slot
+  T v[N];
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B[t + N2 * m];
+  eo_apply<N, 1>(A.ST, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B[t + N2 * m] = v[m];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B[N * t + m];
+  eo_apply<N, 1>(A.ST, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B[N * t + m] = v[m];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B[a + N * m + N2 * b];
+  eo_apply<N, 1>(A.ST, v, v);
+  // now at Gauss point (a, m, c=b): divide by JxW w
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = v[m] / (A.jxw * A.w[a] * A.w[m] * A.w[b]);
+  eo_apply<N, 1>(A.P, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B[a + N * m + N2 * b] = v[m];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B[N * t + m];
+  eo_apply<N, 1>(A.P, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B[N * t + m] = v[m];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B[t + N2 * m];
+  eo_apply<N, 1>(A.P, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B[t + N2 * m] = v[m];
+  __syncthreads();
+  (void)PT;
+  T *dst = A.y + roff + cell0 * N3;
+  for (long long e = tid; e < nval; e += blockDim.x) dst[e] = smem[e];
+}
+
+// fill a vector with a per-cell pattern of n^3 values (uniform Cartesian mesh)
+template <typename T>
+__global__ void pattern_kernel(long long n, int n3, const T *__restrict__ pat, T *__restrict__ y)
+{
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = pat[i % n3];
+}
+
+template <int N, typename T>
+DGArgs<N, T> make_dg_args(const sf_op *op)
+{
+  DGArgs<N, T> A{};
+  const Shape1D &s = op->shape;
+  A.S = eo_of<N, T>(s.S, false);
+  A.ST = eo_of<N, T>(s.S, true);
+  A.D = eo_of<N, T>(s.D, false);
+  A.DT = eo_of<N, T>(s.D, true);
+  A.P = eo_of<N, T>(s.Sinv, false);
+  for (int i = 0; i < N; ++i) {
+    A.fv0[i] = T(s.fv[0][i]);
+    A.fv1[i] = T(s.fv[1][i]);
+    A.fd0[i] = T(s.fd[0][i]);
+    A.fd1[i] = T(s.fd[1][i]);
+    A.w[i] = T(s.wq[i]);
+  }
+  const double jxw = op->h[0] * op->h[1] * op->h[2];
+  A.jxw = T(jxw);
+  for (int d = 0; d < 3; ++d) {
+    const double ij = 1.0 / op->h[d];
+    A.ij[d] = T(ij);
+    A.jface[d] = T(jxw * ij);
+    A.tau[d] = T((N) * (N) * op->desc.penalty * ij);
+    A.an[d] = T(op->desc.velocity[d]);
+    A.cdir[d] = op->desc.kind == SF_OP_DG_SIPG ? T(ij * ij * jxw) : T(op->desc.velocity[d] * ij * jxw);
+    A.nc[d] = op->desc.n_cells[d];
+  }
+  A.hd0 = T(s.hermite_d0);
+  A.n_cells = op->n_cells;
+  A.n_dofs = op->n_dofs;
+  return A;
+}
+
+template <int N, typename T>
+int dg_vmult_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T *y, const T *cb,
+                  const T *cdinv, T *ct, double c_np, double c_tm, cudaStream_t st)
+{
+  constexpr int CPB = DGCells<N>::value;
+  constexpr int N3 = N * N * N;
+  DGArgs<N, T> A = make_dg_args<N, T>(op);
+  A.x = x;
+  A.y = y;
+  A.cb = cb;
+  A.cdinv = cdinv;
+  A.ct = ct;
+  A.c_np = T(c_np);
+  A.c_tm = T(c_tm);
+  const bool sipg = op->desc.kind == SF_OP_DG_SIPG;
+  const bool cheb = cb != nullptr;
+  const bool invm = !sipg && !transpose && op->desc.inverse_mass;
+  void (*kern)(const DGArgs<N, T>);
+  if (sipg)
+    kern = cheb ? dg_kernel<N, T, K_SIPG, false, false, true> : dg_kernel<N, T, K_SIPG, false, false, false>;
+  else if (transpose)
+    kern = dg_kernel<N, T, K_ADVECT, true, false, false>;
+  else if (invm)
+    kern = cheb ? dg_kernel<N, T, K_ADVECT, false, true, true> : dg_kernel<N, T, K_ADVECT, false, true, false>;
+  else
+    kern = cheb ? dg_kernel<N, T, K_ADVECT, false, false, true> : dg_kernel<N, T, K_ADVECT, false, false, false>;
+  const size_t smem = (size_t(3) * CPB * N3 + size_t(CPB) * 12 * N * N) * sizeof(T);
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long long blocks = (op->n_cells + CPB - 1) / CPB;
+  kern<<<dim3((unsigned)blocks, (unsigned)nrhs), dim3(CPB * N * N), smem, st>>>(A);
+  SF_CUDA_TRY(cudaGetLastError());
+  return SF_OK;
+}
+
+template <int N, typename T>
+int dg_invmass_impl(const sf_op *op, int nrhs, const T *x, T *y, cudaStream_t st)
+{
+  constexpr int CPB = DGCells<N>::value;
+  constexpr int N3 = N * N * N;
+  DGArgs<N, T> A = make_dg_args<N, T>(op);
+  // the transposed tables of P go into the ST slot
+  A.ST = eo_of<N, T>(op->shape.Sinv, true);
+  A.x = x;
+  A.y = y;
+  const size_t smem = size_t(CPB) * N3 * sizeof(T);
+  SF_CUDA_TRY(cudaFuncSetAttribute(dg_inverse_mass_kernel<N, T>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long long blocks = (op->n_cells + CPB - 1) / CPB;
+  dg_inverse_mass_kernel<N, T><<<dim3((unsigned)blocks, (unsigned)nrhs), dim3(CPB * N * N), smem, st>>>(A);
+  SF_CUDA_TRY(cudaGetLastError());
+  return SF_OK;
+}
+
+template <int N>
+int dg_vmult_n(const sf_op *op, int prec, int nrhs, bool tr, const void *x, void *y, const void *cb,
+               const void *cd, void *ct, double c_np, double c_tm, cudaStream_t st)
+{
+  if (prec == SF_FP64)
+    return dg_vmult_impl<N, double>(op, nrhs, tr, (const double *)x, (double *)y, (const double *)cb,
+                                    (const double *)cd, (double *)ct, c_np, c_tm, st);
+  return dg_vmult_impl<N, float>(op, nrhs, tr, (const float *)x, (float *)y, (const float *)cb,
+                                 (const float *)cd, (float *)ct, c_np, c_tm, st);
+}
+
+template <int N>
+int dg_invmass_n(const sf_op *op, int prec, int nrhs, const void *x, void *y, cudaStream_t st)
+{
+  if (prec == SF_FP64) return dg_invmass_impl<N, double>(op, nrhs, (const double *)x, (double *)y, st);
+  return dg_invmass_impl<N, float>(op, nrhs, (const float *)x, (float *)y, st);
+}
+
+} // namespace
+
+#define SF_DEG_DISPATCH(DEG, FN, ...)                                          \
+  switch (DEG) {                                                               \
+  case 1: return FN<2>(__VA_ARGS__);                                           \
+  case 2: return FN<3>(__VA_ARGS__);                                           \
+  case 3: return FN<4>(__VA_ARGS__);                                           \
+  case 4: return FN<5>(__VA_ARGS__);                                           \
+  case 5: return FN<6>(__VA_ARGS__);                                           \
+  case 6: return FN<7>(__VA_ARGS__);                                           \
+  case 7: return FN<8>(__VA_ARGS__);                                           \
+  case 8: return FN<9>(__VA_ARGS__);                                           \
+  default: set_error("unsupported degree"); return SF_ERR_UNSUPPORTED;         \
+  }
+
+int launch_dg_vmult(const sf_op *op, int prec, int nrhs, bool transpose, const void *x, void *y,
+                    const void *cb, const void *cdinv, void *ct, double c_np, double c_tm,
+                    cudaStream_t st)
+{
+  if (op->desc.n_cells[0] < 1) return SF_ERR_INVALID;
+  SF_DEG_DISPATCH(op->desc.degree, dg_vmult_n, op, prec, nrhs, transpose, x, y, cb, cdinv, ct, c_np,
+                  c_tm, st)
+}
+
+int launch_dg_inverse_mass(const sf_op *op, int prec, int nrhs, const void *x, void *y,
+                           cudaStream_t st)
+{
+  SF_DEG_DISPATCH(op->desc.degree, dg_invmass_n, op, prec, nrhs, x, y, st)
+}
+
+// Diagonal of the SIPG operator on a uniform periodic Cartesian mesh.  The
+// operator is sum_d (1D SIPG along d) x (1D mass) x (1D mass); its diagonal
+// entry for local node (a,b,c) is
+//   sum_d K_d[i_d] prod_{e != d} M[i_e]
+// with M[i] = sum_q w_q phi_i(x_q)^2 and, for direction d with inverse size
+// ij, volume jxw, face area jf = jxw ij and tau = pen (p+1)^2 ij,
+//   K_d[i] = ij^2 jxw sum_q w_q phi_i'(x_q)^2
+//          + jf (ij phi_i'(0) phi_i(0) + tau phi_i(0)^2
+//                - ij phi_i'(1) phi_i(1) + tau phi_i(1)^2)
+// (the own-cell part of the face terms; neighbour couplings are off the
+// diagonal).  Computed on the host in FP64 and broadcast to all cells.
+// Advection has no diagonal preconditioner use; it gets the same formula's
+// analogue: sum_d of the cell-diagonal of M^-1 K along d is not provided.
+int launch_dg_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st)
+{
+  if (op->desc.kind != SF_OP_DG_SIPG) {
+    set_error("diagonal only for SF_OP_DG_SIPG and SF_OP_LAPLACE");
+    return SF_ERR_STATE;
+  }
+  const Shape1D &s = op->shape;
+  const int n = s.n, n3 = n * n * n;
+  // 1D basis values / derivatives at Gauss points and faces, through the
+  // Gauss-Lagrange interpolant of the Gauss-point values (exact)
+  double M[kMaxN], K[3][kMaxN];
+  const double jxw = op->h[0] * op->h[1] * op->h[2];
+  for (int i = 0; i < n; ++i) {
+    double m = 0, k = 0, v0 = 0, v1 = 0, d0 = 0, d1 = 0;
+    double dq[kMaxN];
+    for (int q = 0; q < n; ++q) {
+      double dd = 0;
+      for (int j = 0; j < n; ++j) dd += s.D[q][j] * s.S[j][i];
+      dq[q] = dd;
+    }
+    for (int q = 0; q < n; ++q) {
+      m += s.wq[q] * s.S[q][i] * s.S[q][i];
+      k += s.wq[q] * dq[q] * dq[q];
+      v0 += s.fv[0][q] * s.S[q][i];
+      v1 += s.fv[1][q] * s.S[q][i];
+      d0 += s.fd[0][q] * s.S[q][i];
+      d1 += s.fd[1][q] * s.S[q][i];
+    }
+    M[i] = m;
+    for (int d = 0; d < 3; ++d) {
+      const double ij = 1.0 / op->h[d], jf = jxw * ij;
+      const double tau = op->desc.penalty * n * n * ij;
+      K[d][i] = ij * ij * jxw * k + jf * (ij * d0 * v0 + tau * v0 * v0 - ij * d1 * v1 + tau * v1 * v1);
+    }
+  }
+  double pat[kMaxN * kMaxN * kMaxN];
+  for (int c = 0; c < n; ++c)
+    for (int b = 0; b < n; ++b)
+      for (int a = 0; a < n; ++a)
+        pat[(c * n + b) * n + a] = K[0][a] * M[b] * M[c] + M[a] * K[1][b] * M[c] + M[a] * M[b] * K[2][c];
+  DevBuf buf;
+  if (prec == SF_FP64) {
+    int r = buf.alloc(n3 * sizeof(double));
+    if (r) return r;
+    SF_CUDA_TRY(cudaMemcpyAsync(buf.ptr, pat, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+    pattern_kernel<double><<<152 * 8, 256, 0, st>>>(op->n_dofs, n3, (const double *)buf.ptr, (double *)diag);
+  } else {
+    float pf[kMaxN * kMaxN * kMaxN];
+    for (int i = 0; i < n3; ++i) pf[i] = float(pat[i]);
+    int r = buf.alloc(n3 * sizeof(float));
+    if (r) return r;
+    SF_CUDA_TRY(cudaMemcpyAsync(buf.ptr, pf, n3 * sizeof(float), cudaMemcpyHostToDevice, st));
+    pattern_kernel<float><<<152 * 8, 256, 0, st>>>(op->n_dofs, n3, (const float *)buf.ptr, (float *)diag);
+  }
+  SF_CUDA_TRY(cudaGetLastError());
+  // the staging buffer is released when buf goes out of scope; wait for the
+  // kernel that reads it
+  SF_CUDA_TRY(cudaStreamSynchronize(st));
+  return SF_OK;
+}
+
+} // namespace sf

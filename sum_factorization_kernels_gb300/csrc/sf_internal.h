@@ -1,0 +1,69 @@
+// sf_internal.h -- shared declarations of the sfgpu library (host side).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sfgpu.h"
+
+namespace sf {
+
+constexpr int kMaxDegree = 8;
+constexpr int kMaxN = kMaxDegree + 1;
+
+// FP64 1D tables of one degree and basis (see sf_basis.cpp)
+struct Shape1D {
+  int degree, n, basis;
+  double xq[kMaxN], wq[kMaxN], xgll[kMaxN];
+  double S[kMaxN][kMaxN];    // S[q][i]    = phi_i(xq_q)
+  double D[kMaxN][kMaxN];    // D[q][j]    = l_j'(xq_q)   (Gauss-Lagrange)
+  double Sinv[kMaxN][kMaxN]; // Sinv[i][q] = l_q(xgll_i)
+  double fv[2][kMaxN];       // l_j(0), l_j(1)
+  double fd[2][kMaxN];       // l_j'(0), l_j'(1)
+  double hermite_d0;         // phi_0'(0) of the Hermite-like basis
+};
+
+void gauss_points(int n, double *x, double *w);
+void gll_points(int n, double *x);
+int fill_shape(int degree, int basis, Shape1D &s);
+
+// thread-local error text for sf_last_error()
+void set_error(const std::string &msg);
+
+// device buffer owned by a handle
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  int alloc(size_t b);
+  void release();
+  ~DevBuf() { release(); }
+};
+
+} // namespace sf
+
+// the opaque handle
+struct sf_op {
+  sf_desc desc;
+  sf::Shape1D shape;
+  long long n_dofs = 0, n_cells = 0;
+  int n = 0;                    // degree + 1
+  long long geo_stride = 0;     // entries per cell in the geometry arrays
+  bool deformed = false;
+  sf::DevBuf geo64, geo32;      // [cell][6][n^3] (+pad) merged tensors
+  sf::DevBuf kap64, kap32;      // [cell][n^3] coefficient
+  bool has_kappa = false;
+  sf::DevBuf scratch;           // operator-private scratch (transpose, M^-1)
+  double h[3];
+};
+
+#define SF_CUDA_TRY(call)                                                     \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      sf::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));      \
+      return SF_ERR_CUDA;                                                     \
+    }                                                                         \
+  } while (0)

@@ -1,0 +1,543 @@
+// sf_laplace.cu -- continuous FE Laplacian -div(kappa grad u) on hexahedral
+// meshes of degree 1..8: operator apply, geometry, kappa-gradient, diagonal.
+//
+// Per cell the operator is y_e = S^T (sum_d D_d^T t_d), t = kappa_q G_q D S x_e
+// (S: basis -> Gauss values, D: collocation derivative, G: merged
+// JxW J^-1 J^-T), the sweep order of the reference's GLL cell Laplacian
+// (benchmark_loops.cc:1316-1384) with the quadrature-point operation of
+// evaluation_cell_laplacian.h:392-415 extended to one tensor per point.
+//
+// GPU mapping: a thread block holds CPB cells; each cell owns n^2 threads and
+// four n^3 shared-memory slabs.  Every 1D sweep is done "line-locally": in a
+// sweep along direction d thread t owns line t of direction d, loads its n
+// values, applies the even-odd kernel with constant-bank coefficients and
+// stores the n results, so each sweep reads and writes each value once.  The
+// z sweeps run on the register column a thread gathered.
+//
+// Summation over shared nodes is atomic-free: cells are split into 8 colour
+// classes by the parity of (i,j,k); cells of one colour share no node, so
+// one launch per colour adds its cell contributions with plain
+// read-modify-write stores into a zeroed output.
+#include "sf_device.cuh"
+#include "sf_internal.h"
+#include "sf_tables.h"
+#include "sf_launch.h"
+
+namespace sf {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+template <int N, typename T>
+struct ContArgs {
+  EOMat<N, T> S, ST, D, DT;
+  T w[N];
+  const T *__restrict__ x;
+  T *__restrict__ y;
+  const T *__restrict__ x2;   // second field (kappa gradient)
+  const T *__restrict__ geo;
+  const T *__restrict__ kappa;
+  long long geo_stride;
+  int nc[3];
+  long long Nx, Ny, Nz;
+  T aff[3];                   // affine: JxW / h_d^2 (without quadrature weight)
+  int dirichlet;
+  int cx, cy, cz, mx, my;
+  int step;                   // 2: one colour class, 1: all cells
+  long long count;            // cells in this launch
+};
+
+template <int N, typename T>
+struct CellPos {
+  long long cell;
+  long long gbase;            // global index of local node (a, b, 0)
+  int X, Y, Z0;               // global node coordinates of (a, b, 0)
+  bool valid;
+};
+
+// gather the z column (a,b,.) of a cell, Dirichlet nodes read as zero
+template <int N, typename T>
+__device__ __forceinline__ void gather_column(const ContArgs<N, T> &A, const T *__restrict__ x,
+                                              const CellPos<N, T> &p, T (&v)[N])
+{
+  const bool side = A.dirichlet && (p.X == 0 || p.X == A.Nx - 1 || p.Y == 0 || p.Y == A.Ny - 1);
+  const long long plane = A.Nx * A.Ny;
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const int Z = p.Z0 + c;
+    const bool bnd = side || (A.dirichlet && (Z == 0 || Z == A.Nz - 1));
+    v[c] = (p.valid && !bnd) ? __ldg(x + p.gbase + (long long)c * plane) : T(0);
+  }
+}
+
+// values and gradients at the Gauss points of one cell.  On return (after a
+// block barrier) B0 = d/dx, B2 = d/dy, B3 = d/dz of u in slab layout; B1 is
+// free.  v holds the gathered z column on entry.
+template <int N, typename T>
+__device__ __forceinline__ void cell_gradients(const ContArgs<N, T> &A, T (&v)[N], T *B0, T *B1,
+                                               T *B2, T *B3, int t, int a, int b)
+{
+  constexpr int N2 = N * N;
+  T g[N];
+  eo_apply<N, 1>(A.S, v, v);
+#pragma unroll
+  for (int c = 0; c < N; ++c) B0[t + N2 * c] = v[c];
+  __syncthreads();
+  // x sweep: line (b, c) = t
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B0[N * t + m];
+  eo_apply<N, 1>(A.S, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B0[N * t + m] = v[m];
+  __syncthreads();
+  // y sweep: line (a, c=b) -> values at Gauss points, y derivative
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B0[a + N * m + N2 * b];
+  eo_apply<N, 1>(A.S, v, v);
+  eo_apply<N, -1>(A.D, v, g);
+#pragma unroll
+  for (int m = 0; m < N; ++m) {
+    B1[a + N * m + N2 * b] = v[m];
+    B2[a + N * m + N2 * b] = g[m];
+  }
+  __syncthreads();
+  // x derivative on line t, z derivative on column t
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B1[N * t + m];
+  eo_apply<N, -1>(A.D, v, g);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B0[N * t + m] = g[m];
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B1[t + N2 * m];
+  eo_apply<N, -1>(A.D, v, g);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B3[t + N2 * m] = g[m];
+  __syncthreads();
+}
+
+// integrate t_x (B0), t_y (B2) and the register column tz against the test
+// functions; returns the z column of the cell result in v (after barriers)
+template <int N, typename T>
+__device__ __forceinline__ void cell_integrate(const ContArgs<N, T> &A, T (&tz)[N], T (&v)[N],
+                                               T *B0, T *B1, T *B2, int t, int a, int b)
+{
+  constexpr int N2 = N * N;
+  T g[N];
+  eo_apply<N, -1>(A.DT, tz, g);
+#pragma unroll
+  for (int c = 0; c < N; ++c) B1[t + N2 * c] = g[c];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B0[N * t + m];
+  eo_apply<N, -1>(A.DT, v, g);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B1[N * t + m] += g[m];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B2[a + N * m + N2 * b];
+  eo_apply<N, -1>(A.DT, v, g);
+#pragma unroll
+  for (int m = 0; m < N; ++m) g[m] += B1[a + N * m + N2 * b];
+  eo_apply<N, 1>(A.ST, g, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B1[a + N * m + N2 * b] = v[m];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B1[N * t + m];
+  eo_apply<N, 1>(A.ST, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B1[N * t + m] = v[m];
+  __syncthreads();
+#pragma unroll
+  for (int c = 0; c < N; ++c) v[c] = B1[t + N2 * c];
+  eo_apply<N, 1>(A.ST, v, v);
+}
+
+template <int N, typename T>
+__device__ __forceinline__ CellPos<N, T> cell_position(const ContArgs<N, T> &A, long long ordinal,
+                                                       int a, int b)
+{
+  CellPos<N, T> p;
+  p.valid = ordinal < A.count;
+  const long long o = p.valid ? ordinal : 0;
+  const int mi = int(o % A.mx);
+  const int mj = int((o / A.mx) % A.my);
+  const int mk = int(o / ((long long)A.mx * A.my));
+  const int i = A.step * mi + A.cx, j = A.step * mj + A.cy, k = A.step * mk + A.cz;
+  p.cell = ((long long)k * A.nc[1] + j) * A.nc[0] + i;
+  p.X = i * (N - 1) + a;
+  p.Y = j * (N - 1) + b;
+  p.Z0 = k * (N - 1);
+  p.gbase = ((long long)p.Z0 * A.Ny + p.Y) * A.Nx + p.X;
+  return p;
+}
+
+template <int N, typename T, bool DEFORMED, bool KAPPA>
+__global__ void __launch_bounds__(CellsPerBlock<N>::value *N *N)
+    cont_vmult_kernel(const __grid_constant__ ContArgs<N, T> A)
+{
+  constexpr int N2 = N * N, N3 = N * N * N;
+  constexpr int CPB = CellsPerBlock<N>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *smem = reinterpret_cast<T *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int cs = tid / N2;
+  const int t = tid - cs * N2;
+  const int a = t % N, b = t / N;
+  T *B0 = smem + cs * 4 * N3, *B1 = B0 + N3, *B2 = B1 + N3, *B3 = B2 + N3;
+
+  const CellPos<N, T> p = cell_position<N, T>(A, (long long)blockIdx.x * CPB + cs, a, b);
+  T v[N];
+  gather_column<N, T>(A, A.x, p, v);
+  cell_gradients<N, T>(A, v, B0, B1, B2, B3, t, a, b);
+
+  // quadrature-point operation on column t
+  const T wab = A.w[a] * A.w[b];
+  T tz[N];
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const int q = t + N2 * c;
+    const T gx = B0[q], gy = B2[q], gz = B3[q];
+    T tx, ty, tzc;
+    if (DEFORMED) {
+      const T *G = A.geo + p.cell * A.geo_stride + q;
+      T g0 = T(0), g1 = T(0), g2 = T(0), g3 = T(0), g4 = T(0), g5 = T(0);
+      if (p.valid) {
+        g0 = __ldg(G);
+        g1 = __ldg(G + N3);
+        g2 = __ldg(G + 2 * N3);
+        g3 = __ldg(G + 3 * N3);
+        g4 = __ldg(G + 4 * N3);
+        g5 = __ldg(G + 5 * N3);
+      }
+      tx = gx * g0 + gy * g3 + gz * g4;
+      ty = gx * g3 + gy * g1 + gz * g5;
+      tzc = gx * g4 + gy * g5 + gz * g2;
+    } else {
+      const T wq = wab * A.w[c];
+      tx = gx * (A.aff[0] * wq);
+      ty = gy * (A.aff[1] * wq);
+      tzc = gz * (A.aff[2] * wq);
+    }
+    if (KAPPA) {
+      const T k = p.valid ? __ldg(A.kappa + p.cell * N3 + q) : T(0);
+      tx *= k;
+      ty *= k;
+      tzc *= k;
+    }
+    B0[q] = tx;
+    B2[q] = ty;
+    tz[c] = tzc;
+  }
+  cell_integrate<N, T>(A, tz, v, B0, B1, B2, t, a, b);
+
+  // colour-exclusive accumulation; Dirichlet rows are written afterwards
+  if (p.valid) {
+    const bool side = A.dirichlet && (p.X == 0 || p.X == A.Nx - 1 || p.Y == 0 || p.Y == A.Ny - 1);
+    const long long plane = A.Nx * A.Ny;
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      const int Z = p.Z0 + c;
+      const bool bnd = side || (A.dirichlet && (Z == 0 || Z == A.Nz - 1));
+      if (!bnd) {
+        T *dst = A.y + p.gbase + (long long)c * plane;
+        *dst += v[c];
+      }
+    }
+  }
+}
+
+// dk_q = grad(u)_q . G_q grad(lam)_q  (G without kappa)
+template <int N, typename T, bool DEFORMED>
+__global__ void __launch_bounds__(CellsPerBlock<N>::value *N *N)
+    cont_kappa_grad_kernel(const __grid_constant__ ContArgs<N, T> A)
+{
+  constexpr int N2 = N * N, N3 = N * N * N;
+  constexpr int CPB = CellsPerBlock<N>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *smem = reinterpret_cast<T *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int cs = tid / N2;
+  const int t = tid - cs * N2;
+  const int a = t % N, b = t / N;
+  T *B0 = smem + cs * 4 * N3, *B1 = B0 + N3, *B2 = B1 + N3, *B3 = B2 + N3;
+  const CellPos<N, T> p = cell_position<N, T>(A, (long long)blockIdx.x * CPB + cs, a, b);
+  T v[N], gx[N], gy[N], gz[N];
+  gather_column<N, T>(A, A.x2, p, v);
+  cell_gradients<N, T>(A, v, B0, B1, B2, B3, t, a, b);
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    gx[c] = B0[t + N2 * c];
+    gy[c] = B2[t + N2 * c];
+    gz[c] = B3[t + N2 * c];
+  }
+  __syncthreads();
+  gather_column<N, T>(A, A.x, p, v);
+  cell_gradients<N, T>(A, v, B0, B1, B2, B3, t, a, b);
+  const T wab = A.w[a] * A.w[b];
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const int q = t + N2 * c;
+    const T ux = B0[q], uy = B2[q], uz = B3[q];
+    T r;
+    if (DEFORMED) {
+      const T *G = A.geo + p.cell * A.geo_stride + q;
+      if (p.valid) {
+        const T g0 = __ldg(G), g1 = __ldg(G + N3), g2 = __ldg(G + 2 * N3), g3 = __ldg(G + 3 * N3),
+                g4 = __ldg(G + 4 * N3), g5 = __ldg(G + 5 * N3);
+        r = ux * (g0 * gx[c] + g3 * gy[c] + g4 * gz[c]) + uy * (g3 * gx[c] + g1 * gy[c] + g5 * gz[c]) +
+            uz * (g4 * gx[c] + g5 * gy[c] + g2 * gz[c]);
+      } else {
+        r = T(0);
+      }
+    } else {
+      const T wq = wab * A.w[c];
+      r = wq * (A.aff[0] * ux * gx[c] + A.aff[1] * uy * gy[c] + A.aff[2] * uz * gz[c]);
+    }
+    if (p.valid) A.y[p.cell * N3 + q] = r;
+  }
+}
+
+// boundary rows: y_b = x_b on all boundary nodes of the node grid
+template <typename T>
+__global__ void dirichlet_rows_kernel(const T *__restrict__ x, T *__restrict__ y, long long Nx,
+                                      long long Ny, long long Nz)
+{
+  const long long nzf = Nx * Ny, nyf = Nx * (Nz - 2), nxf = (Ny - 2) * (Nz - 2);
+  const long long total = 2 * (nzf + nyf + nxf);
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < total;
+       s += (long long)gridDim.x * blockDim.x) {
+    long long X, Y, Z, r = s;
+    if (r < 2 * nzf) {
+      Z = r < nzf ? 0 : Nz - 1;
+      r %= nzf;
+      X = r % Nx;
+      Y = r / Nx;
+    } else if ((r -= 2 * nzf) < 2 * nyf) {
+      Y = r < nyf ? 0 : Ny - 1;
+      r %= nyf;
+      X = r % Nx;
+      Z = 1 + r / Nx;
+    } else {
+      r -= 2 * nyf;
+      X = r < nxf ? 0 : Nx - 1;
+      r %= nxf;
+      Y = 1 + r % (Ny - 2);
+      Z = 1 + r / (Ny - 2);
+    }
+    const long long g = (Z * Ny + Y) * Nx + X;
+    y[g] = x[g];
+  }
+}
+
+// deformed-mesh geometry in FP64: G[cell][6][n^3] = JxW J^-1 J^-T
+struct GeoArgs {
+  double xq[kMaxN], wq[kMaxN];
+  int n, nc[3];
+  double h[3], deform;
+  long long stride;
+  double *G;
+};
+
+__global__ void geometry_kernel(const __grid_constant__ GeoArgs A)
+{
+  const int n = A.n, n3 = n * n * n;
+  const long long total = (long long)A.nc[0] * A.nc[1] * A.nc[2] * n3;
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < total;
+       s += (long long)gridDim.x * blockDim.x) {
+    const long long cell = s / n3;
+    const int q = int(s - cell * n3);
+    const int qx = q % n, qy = (q / n) % n, qz = q / (n * n);
+    const int i = int(cell % A.nc[0]);
+    const int j = int((cell / A.nc[0]) % A.nc[1]);
+    const int k = int(cell / ((long long)A.nc[0] * A.nc[1]));
+    const double X0 = (i + A.xq[qx]) * A.h[0], X1 = (j + A.xq[qy]) * A.h[1],
+                 X2 = (k + A.xq[qz]) * A.h[2];
+    const double tp = 2.0 * kPi, a = A.deform;
+    double s0, c0, s1, c1, s2, c2;
+    sincos(tp * X0, &s0, &c0);
+    sincos(tp * X1, &s1, &c1);
+    sincos(tp * X2, &s2, &c2);
+    double J[3][3];
+    J[0][0] = A.h[0];
+    J[0][1] = A.h[1] * a * tp * c1 * s2;
+    J[0][2] = A.h[2] * a * tp * s1 * c2;
+    J[1][0] = A.h[0] * a * tp * s2 * c0;
+    J[1][1] = A.h[1];
+    J[1][2] = A.h[2] * a * tp * c2 * s0;
+    J[2][0] = A.h[0] * a * tp * c0 * s1;
+    J[2][1] = A.h[1] * a * tp * s0 * c1;
+    J[2][2] = A.h[2];
+    const double C00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const double C01 = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    const double C02 = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    const double C10 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    const double C11 = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    const double C12 = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    const double C20 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    const double C21 = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    const double C22 = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    const double det = J[0][0] * C00 + J[0][1] * C10 + J[0][2] * C20;
+    // J^-1 = C / det; G = det w J^-1 J^-T = (w / det) C C^T
+    const double f = (A.wq[qz] * A.wq[qy]) * A.wq[qx] / det;
+    double *G = A.G + cell * A.stride + q;
+    G[0 * n3] = f * (C00 * C00 + C01 * C01 + C02 * C02);
+    G[1 * n3] = f * (C10 * C10 + C11 * C11 + C12 * C12);
+    G[2 * n3] = f * (C20 * C20 + C21 * C21 + C22 * C22);
+    G[3 * n3] = f * (C00 * C10 + C01 * C11 + C02 * C12);
+    G[4 * n3] = f * (C00 * C20 + C01 * C21 + C02 * C22);
+    G[5 * n3] = f * (C10 * C20 + C11 * C21 + C12 * C22);
+  }
+}
+
+template <int N, typename T>
+ContArgs<N, T> make_args(const sf_op *op)
+{
+  ContArgs<N, T> A{};
+  const Shape1D &s = op->shape;
+  A.S = eo_of<N, T>(s.S, false);
+  A.ST = eo_of<N, T>(s.S, true);
+  A.D = eo_of<N, T>(s.D, false);
+  A.DT = eo_of<N, T>(s.D, true);
+  for (int i = 0; i < N; ++i) A.w[i] = T(s.wq[i]);
+  for (int d = 0; d < 3; ++d) A.nc[d] = op->desc.n_cells[d];
+  A.Nx = (long long)(N - 1) * A.nc[0] + 1;
+  A.Ny = (long long)(N - 1) * A.nc[1] + 1;
+  A.Nz = (long long)(N - 1) * A.nc[2] + 1;
+  const double jxw = op->h[0] * op->h[1] * op->h[2];
+  for (int d = 0; d < 3; ++d) A.aff[d] = T(jxw / (op->h[d] * op->h[d]));
+  A.dirichlet = op->desc.dirichlet;
+  A.geo_stride = op->geo_stride;
+  return A;
+}
+
+template <int N, typename T>
+int cont_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
+{
+  constexpr int CPB = CellsPerBlock<N>::value;
+  constexpr int N3 = N * N * N;
+  ContArgs<N, T> A = make_args<N, T>(op);
+  A.x = x;
+  A.y = y;
+  const bool deformed = op->deformed;
+  const bool kap = op->has_kappa;
+  A.geo = (const T *)(sizeof(T) == 8 ? op->geo64.ptr : op->geo32.ptr);
+  A.kappa = (const T *)(sizeof(T) == 8 ? op->kap64.ptr : op->kap32.ptr);
+  const size_t smem = size_t(CPB) * 4 * N3 * sizeof(T);
+  auto kern = deformed ? (kap ? cont_vmult_kernel<N, T, true, true> : cont_vmult_kernel<N, T, true, false>)
+                       : (kap ? cont_vmult_kernel<N, T, false, true> : cont_vmult_kernel<N, T, false, false>);
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SF_CUDA_TRY(cudaMemsetAsync(y, 0, sizeof(T) * op->n_dofs, st));
+  A.step = 2;
+  for (int color = 0; color < 8; ++color) {
+    A.cx = color & 1;
+    A.cy = (color >> 1) & 1;
+    A.cz = (color >> 2) & 1;
+    A.mx = (A.nc[0] - A.cx + 1) / 2;
+    A.my = (A.nc[1] - A.cy + 1) / 2;
+    const int mz = (A.nc[2] - A.cz + 1) / 2;
+    A.count = (long long)A.mx * A.my * mz;
+    if (A.count == 0) continue;
+    const long long blocks = (A.count + CPB - 1) / CPB;
+    kern<<<dim3((unsigned)blocks), dim3(CPB * N * N), smem, st>>>(A);
+    SF_CUDA_TRY(cudaGetLastError());
+  }
+  if (A.dirichlet) {
+    dirichlet_rows_kernel<T><<<1024, 256, 0, st>>>(x, y, A.Nx, A.Ny, A.Nz);
+    SF_CUDA_TRY(cudaGetLastError());
+  }
+  return SF_OK;
+}
+
+template <int N, typename T>
+int cont_kappa_grad_impl(const sf_op *op, const T *u, const T *lam, T *dk, cudaStream_t st)
+{
+  constexpr int CPB = CellsPerBlock<N>::value;
+  constexpr int N3 = N * N * N;
+  ContArgs<N, T> A = make_args<N, T>(op);
+  A.x = u;
+  A.x2 = lam;
+  A.y = dk;
+  A.geo = (const T *)(sizeof(T) == 8 ? op->geo64.ptr : op->geo32.ptr);
+  const size_t smem = size_t(CPB) * 4 * N3 * sizeof(T);
+  auto kern = op->deformed ? cont_kappa_grad_kernel<N, T, true> : cont_kappa_grad_kernel<N, T, false>;
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // all cells in one launch: every cell writes only its own quadrature points
+  A.cx = A.cy = A.cz = 0;
+  A.step = 1;
+  A.mx = A.nc[0];
+  A.my = A.nc[1];
+  A.count = op->n_cells;
+  const long long blocks = (A.count + CPB - 1) / CPB;
+  kern<<<dim3((unsigned)blocks), dim3(CPB * N * N), smem, st>>>(A);
+  SF_CUDA_TRY(cudaGetLastError());
+  return SF_OK;
+}
+
+} // namespace
+} // namespace sf
+
+namespace sf {
+
+#define SF_DEG_DISPATCH(DEG, FN, ...)                                          \
+  switch (DEG) {                                                               \
+  case 1: return FN<2>(__VA_ARGS__);                                           \
+  case 2: return FN<3>(__VA_ARGS__);                                           \
+  case 3: return FN<4>(__VA_ARGS__);                                           \
+  case 4: return FN<5>(__VA_ARGS__);                                           \
+  case 5: return FN<6>(__VA_ARGS__);                                           \
+  case 6: return FN<7>(__VA_ARGS__);                                           \
+  case 7: return FN<8>(__VA_ARGS__);                                           \
+  case 8: return FN<9>(__VA_ARGS__);                                           \
+  default: set_error("unsupported degree"); return SF_ERR_UNSUPPORTED;         \
+  }
+
+namespace {
+template <int N>
+int cont_vmult_n(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
+{
+  if (prec == SF_FP64) return cont_vmult_impl<N, double>(op, (const double *)x, (double *)y, st);
+  return cont_vmult_impl<N, float>(op, (const float *)x, (float *)y, st);
+}
+template <int N>
+int cont_kgrad_n(const sf_op *op, int prec, const void *u, const void *l, void *dk, cudaStream_t st)
+{
+  if (prec == SF_FP64)
+    return cont_kappa_grad_impl<N, double>(op, (const double *)u, (const double *)l, (double *)dk, st);
+  return cont_kappa_grad_impl<N, float>(op, (const float *)u, (const float *)l, (float *)dk, st);
+}
+} // namespace
+
+int launch_cont_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
+{
+  SF_DEG_DISPATCH(op->desc.degree, cont_vmult_n, op, prec, x, y, st)
+}
+
+int launch_cont_kappa_grad(const sf_op *op, int prec, const void *u, const void *lam, void *dk,
+                           cudaStream_t st)
+{
+  SF_DEG_DISPATCH(op->desc.degree, cont_kgrad_n, op, prec, u, lam, dk, st)
+}
+
+int launch_geometry(const sf_op *op, double *G, cudaStream_t st)
+{
+  GeoArgs A{};
+  for (int i = 0; i < op->n; ++i) {
+    A.xq[i] = op->shape.xq[i];
+    A.wq[i] = op->shape.wq[i];
+  }
+  A.n = op->n;
+  for (int d = 0; d < 3; ++d) {
+    A.nc[d] = op->desc.n_cells[d];
+    A.h[d] = op->h[d];
+  }
+  A.deform = op->desc.deform;
+  A.stride = op->geo_stride;
+  A.G = G;
+  geometry_kernel<<<152 * 16, 256, 0, st>>>(A);
+  SF_CUDA_TRY(cudaGetLastError());
+  return SF_OK;
+}
+
+} // namespace sf

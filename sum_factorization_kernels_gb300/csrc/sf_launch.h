@@ -1,0 +1,35 @@
+// sf_launch.h -- host launchers of the device kernels (one per .cu file).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sf_internal.h"
+
+namespace sf {
+
+// sf_laplace.cu
+int launch_cont_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st);
+int launch_cont_kappa_grad(const sf_op *op, int prec, const void *u, const void *lam, void *dk,
+                           cudaStream_t st);
+int launch_geometry(const sf_op *op, double *G, cudaStream_t st);
+int launch_cont_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
+
+// sf_dg.cu
+int launch_dg_vmult(const sf_op *op, int prec, int nrhs, bool transpose, const void *x, void *y,
+                    const void *cheb_b, const void *cheb_dinv, void *cheb_t, double c_np,
+                    double c_tm, cudaStream_t st);
+int launch_dg_inverse_mass(const sf_op *op, int prec, int nrhs, const void *x, void *y,
+                           cudaStream_t st);
+int launch_dg_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
+
+// sf_vector.cu
+int launch_convert(long long n, int from, const void *x, int to, void *y, cudaStream_t st);
+int launch_vector_update(long long n, int prec, const void *ax, const void *b, const void *dinv,
+                         const void *x_old, void *x_new, void *t, double c_np, double c_tm,
+                         cudaStream_t st);
+// partial sums for a deterministic dot product: needs dot_scratch_doubles()
+int launch_dot(long long n, int prec, const void *x, const void *y, double *scratch,
+               double *result, cudaStream_t st);
+constexpr int kDotBlocks = 1024;
+
+} // namespace sf

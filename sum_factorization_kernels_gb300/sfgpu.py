@@ -1,0 +1,240 @@
+"""ctypes binding of the sfgpu C ABI (include/sfgpu.h).
+
+Loads the in-tree ``libsfgpu.so`` built for sm_103a and fails loudly when it
+is missing: there is no CPU fallback.  Arrays are passed as device pointers;
+anything with ``data_ptr()`` (a CUDA ``torch.Tensor``) or an integer address
+works.  PyTorch is only the allocator here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsfgpu.so")
+
+SF_OK = 0
+STATUS = {0: "SF_OK", -1: "SF_ERR_INVALID", -2: "SF_ERR_NULL", -3: "SF_ERR_UNSUPPORTED",
+          -4: "SF_ERR_CUDA", -5: "SF_ERR_OOM", -6: "SF_ERR_NOT_CONVERGED",
+          -7: "SF_ERR_BREAKDOWN", -8: "SF_ERR_ALIGN", -9: "SF_ERR_STATE"}
+FP64, FP32 = 0, 1
+OP_LAPLACE, OP_DG_SIPG, OP_DG_ADVECT = 0, 1, 2
+BASIS_GLL, BASIS_HERMITE = 0, 1
+SOLVE_FP64, SOLVE_MIXED = 0, 1
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2
+
+EXPORTS = [
+    "sf_last_error", "sf_version", "sf_create", "sf_destroy", "sf_sizes", "sf_set_geometry",
+    "sf_set_coefficient", "sf_vmult", "sf_vmult_transpose", "sf_vmult_batched",
+    "sf_vmult_transpose_batched", "sf_chebyshev_step", "sf_vector_update", "sf_diagonal",
+    "sf_kappa_gradient", "sf_solve_opts_default", "sf_cg_solve", "sf_convert", "sf_dot",
+    "sf_shape_tables",
+]
+
+
+class SFError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (STATUS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Desc(C.Structure):
+    _fields_ = [("kind", C.c_int), ("degree", C.c_int), ("n_cells", C.c_int * 3),
+                ("length", C.c_double * 3), ("basis", C.c_int), ("deform", C.c_double),
+                ("dirichlet", C.c_int), ("penalty", C.c_double), ("velocity", C.c_double * 3),
+                ("inverse_mass", C.c_int), ("precisions", C.c_int)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("mode", C.c_int), ("precond", C.c_int), ("cheb_degree", C.c_int),
+                ("cheb_range", C.c_double), ("eig_iterations", C.c_int), ("rtol", C.c_double),
+                ("max_iter", C.c_int), ("inner_rtol", C.c_double), ("project_constant", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("outer_iterations", C.c_int),
+                ("rel_residual", C.c_double), ("lambda_max", C.c_double),
+                ("seconds", C.c_double), ("operator_applies", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libsfgpu.so not built (run __graft_entry__.build()); "
+                              "there is no CPU fallback")
+        L = C.CDLL(LIB_PATH)
+        vp, i, d, ll = C.c_void_p, C.c_int, C.c_double, C.c_longlong
+        L.sf_last_error.restype = C.c_char_p
+        L.sf_version.restype = C.c_char_p
+        L.sf_create.argtypes = [C.POINTER(Desc), C.POINTER(vp)]
+        L.sf_destroy.argtypes = [vp]
+        L.sf_sizes.argtypes = [vp, C.POINTER(ll), C.POINTER(ll)]
+        L.sf_set_geometry.argtypes = [vp, vp]
+        L.sf_set_coefficient.argtypes = [vp, vp]
+        L.sf_vmult.argtypes = [vp, i, vp, vp, vp]
+        L.sf_vmult_transpose.argtypes = [vp, i, vp, vp, vp]
+        L.sf_vmult_batched.argtypes = [vp, i, i, vp, vp, vp]
+        L.sf_vmult_transpose_batched.argtypes = [vp, i, i, vp, vp, vp]
+        L.sf_chebyshev_step.argtypes = [vp, i, vp, vp, vp, vp, vp, d, d, vp]
+        L.sf_vector_update.argtypes = [ll, i, vp, vp, vp, vp, vp, vp, d, d, vp]
+        L.sf_diagonal.argtypes = [vp, i, vp, vp]
+        L.sf_kappa_gradient.argtypes = [vp, i, vp, vp, vp, vp]
+        L.sf_solve_opts_default.argtypes = [C.POINTER(SolveOpts)]
+        L.sf_solve_opts_default.restype = None
+        L.sf_cg_solve.argtypes = [vp, vp, vp, C.POINTER(SolveOpts), C.POINTER(SolveStats), vp]
+        L.sf_convert.argtypes = [ll, i, vp, i, vp, vp]
+        L.sf_dot.argtypes = [ll, i, vp, vp, vp, vp]
+        L.sf_shape_tables.argtypes = [i, i, vp, vp, vp, vp]
+        _lib = L
+    return _lib
+
+
+def check(code):
+    if code != SF_OK:
+        raise SFError(code, lib().sf_last_error().decode())
+    return code
+
+
+def ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    return a.data_ptr()
+
+
+def prec_of(t):
+    import torch
+    if t.dtype == torch.float64:
+        return FP64
+    if t.dtype == torch.float32:
+        return FP32
+    raise TypeError("vectors must be float32 or float64, got %s" % t.dtype)
+
+
+def stream_ptr(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class Operator:
+    """One operator handle (sf_op).  Mirrors the evaluator classes of the
+    reference: construction = initialize(), vmult = matrix_vector_product()
+    / do_matvec(), chebyshev_step = do_cheby_iter<true>()."""
+
+    def __init__(self, kind=OP_LAPLACE, degree=4, n_cells=(16, 16, 16), length=(1.0, 1.0, 1.0),
+                 basis=BASIS_GLL, deform=0.0, dirichlet=1, penalty=1.0,
+                 velocity=(1.0, 0.5, 0.25), inverse_mass=1, precisions=3):
+        d = Desc()
+        d.kind, d.degree = kind, degree
+        for k in range(3):
+            d.n_cells[k] = int(n_cells[k])
+            d.length[k] = float(length[k])
+            d.velocity[k] = float(velocity[k])
+        d.basis, d.deform, d.dirichlet = basis, float(deform), int(dirichlet)
+        d.penalty, d.inverse_mass, d.precisions = float(penalty), int(inverse_mass), int(precisions)
+        self.desc = d
+        h = C.c_void_p()
+        check(lib().sf_create(C.byref(d), C.byref(h)))
+        self._h = h
+        nd, nc = C.c_longlong(), C.c_longlong()
+        check(lib().sf_sizes(self._h, C.byref(nd), C.byref(nc)))
+        self.n_dofs, self.n_cells = nd.value, nc.value
+        self.degree = degree
+        self.kind = kind
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().sf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def vmult(self, x, y, stream=None):
+        check(lib().sf_vmult(self._h, prec_of(x), ptr(x), ptr(y), stream_ptr(stream)))
+        return y
+
+    def vmult_transpose(self, x, y, stream=None):
+        check(lib().sf_vmult_transpose(self._h, prec_of(x), ptr(x), ptr(y), stream_ptr(stream)))
+        return y
+
+    def vmult_batched(self, x, y, nrhs, stream=None):
+        check(lib().sf_vmult_batched(self._h, prec_of(x), nrhs, ptr(x), ptr(y), stream_ptr(stream)))
+        return y
+
+    def vmult_transpose_batched(self, x, y, nrhs, stream=None):
+        check(lib().sf_vmult_transpose_batched(self._h, prec_of(x), nrhs, ptr(x), ptr(y),
+                                               stream_ptr(stream)))
+        return y
+
+    def chebyshev_step(self, b, diag_inv, x_old, x_new, t, c_np, c_tm, stream=None):
+        check(lib().sf_chebyshev_step(self._h, prec_of(x_old), ptr(b), ptr(diag_inv), ptr(x_old),
+                                      ptr(x_new), ptr(t), float(c_np), float(c_tm),
+                                      stream_ptr(stream)))
+
+    def diagonal(self, out, stream=None):
+        check(lib().sf_diagonal(self._h, prec_of(out), ptr(out), stream_ptr(stream)))
+        return out
+
+    def kappa_gradient(self, u, lam, out, stream=None):
+        check(lib().sf_kappa_gradient(self._h, prec_of(u), ptr(u), ptr(lam), ptr(out),
+                                      stream_ptr(stream)))
+        return out
+
+    def set_geometry(self, G):
+        check(lib().sf_set_geometry(self._h, ptr(G)))
+
+    def set_coefficient(self, kappa):
+        check(lib().sf_set_coefficient(self._h, ptr(kappa)))
+
+    def cg_solve(self, b, x, opts=None, stream=None):
+        o = default_solve_opts() if opts is None else opts
+        st = SolveStats()
+        code = lib().sf_cg_solve(self._h, ptr(b), ptr(x), C.byref(o), C.byref(st), stream_ptr(stream))
+        return code, st
+
+
+def default_solve_opts(**kw):
+    o = SolveOpts()
+    lib().sf_solve_opts_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def dot(x, y, out, stream=None):
+    check(lib().sf_dot(x.numel(), prec_of(x), ptr(x), ptr(y), ptr(out), stream_ptr(stream)))
+    return out
+
+
+def convert(x, y, stream=None):
+    check(lib().sf_convert(x.numel(), prec_of(x), ptr(x), prec_of(y), ptr(y), stream_ptr(stream)))
+    return y
+
+
+def vector_update(ax, b, dinv, x_old, x_new, t, c_np, c_tm, stream=None):
+    check(lib().sf_vector_update(x_old.numel(), prec_of(x_old), ptr(ax), ptr(b), ptr(dinv),
+                                 ptr(x_old), ptr(x_new), ptr(t), float(c_np), float(c_tm),
+                                 stream_ptr(stream)))
+
+
+def shape_tables(degree, basis=BASIS_GLL):
+    import numpy as np
+    n = degree + 1
+    S, D, x, w = (np.zeros(n * n), np.zeros(n * n), np.zeros(n), np.zeros(n))
+    check(lib().sf_shape_tables(degree, basis, S.ctypes.data, D.ctypes.data, x.ctypes.data,
+                                w.ctypes.data))
+    return S.reshape(n, n), D.reshape(n, n), x, w

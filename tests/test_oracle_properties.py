@@ -1,0 +1,110 @@
+"""Mathematical identities of the oracle itself (size-independent checks that
+complement the golden vectors): symmetry, explicit transposes and diagonals,
+the analytic advection derivative of the reference's self-check, and central
+finite differences for the kappa gradient."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def dense(apply, n):
+    A = np.zeros((n, n))
+    e = np.zeros(n)
+    for j in range(n):
+        e[j] = 1.0
+        A[:, j] = apply(e)
+        e[j] = 0.0
+    return A
+
+
+@pytest.mark.parametrize("p,basis", [(1, 0), (2, 0), (3, 1), (4, 0)])
+def test_continuous_matrix_symmetric_and_diagonal(p, basis):
+    m = O.mesh(p, (2, 2, 2), basis=basis, deform=0.06)
+    G = O.cont_geometry(m)
+    kappa = np.exp(0.3 * np.random.default_rng(1).standard_normal(8 * (p + 1) ** 3))
+    A = dense(lambda v: O.cont_apply(m, G, v, kappa=kappa), O.cont_n_dofs(m))
+    assert np.abs(A - A.T).max() < 1e-13 * np.abs(A).max()
+    assert np.allclose(np.diag(A), O.cont_diagonal(m, G, kappa=kappa), rtol=1e-13, atol=1e-15)
+    w = np.linalg.eigvalsh(A)
+    assert w.min() > 0  # SPD with identity Dirichlet rows
+
+
+@pytest.mark.parametrize("p", [1, 3, 4])
+def test_sipg_matrix_symmetric_positive(p):
+    d = O.dg(p, (3, 2, 2), (0.3, 0.5, 0.2))
+    A = dense(lambda v: O.dg_sipg_apply(d, v), O.dg_n_dofs(d))
+    assert np.abs(A - A.T).max() < 1e-12 * np.abs(A).max()
+    w = np.linalg.eigvalsh(0.5 * (A + A.T))
+    assert w[0] > -1e-9 * w[-1]  # periodic: constant null space, PSD
+    assert np.allclose(np.diag(A), O.dg_sipg_diagonal(d), rtol=1e-13, atol=1e-14)
+
+
+@pytest.mark.parametrize("p,invm", [(1, 1), (2, 0), (3, 1), (4, 0)])
+def test_advect_transpose_is_matrix_transpose(p, invm):
+    d = O.dg(p, (2, 3, 2), (0.25, 0.2, 0.4), velocity=(1.0, 0.5, 0.25), inverse_mass=invm)
+    n = O.dg_n_dofs(d)
+    A = dense(lambda v: O.dg_advect_apply(d, v), n)
+    At = dense(lambda v: O.dg_advect_apply_transpose(d, v), n)
+    assert np.abs(At - A.T).max() < 1e-12 * np.abs(A).max()
+
+
+def _wave(points, t, a):
+    k = 4.0 * np.pi
+    xs = [points[i] - t * a[i] for i in range(3)]
+    u = np.sin(k * xs[0]) * np.cos(k * xs[1]) * np.cos(k * xs[2])
+    dudt = -(a[0] * k * np.cos(k * xs[0]) * np.cos(k * xs[1]) * np.cos(k * xs[2])
+             - a[1] * k * np.sin(k * xs[0]) * np.sin(k * xs[1]) * np.cos(k * xs[2])
+             - a[2] * k * np.sin(k * xs[0]) * np.cos(k * xs[1]) * np.sin(k * xs[2]))
+    return u, dudt
+
+
+def test_advect_analytic_time_derivative_converges():
+    """the reference's verify_derivative (evaluation_dg_advect.h:221-251):
+    M^-1 A u at the GLL nodes approximates du/dt of the advected wave"""
+    a = (1.0, 0.15, -0.05)
+    errs = []
+    nc = (4, 4, 4)
+    for p in (3, 5, 7):
+        n = p + 1
+        h = 2.0 / nc[0]
+        xg = O.shape_arrays(p, O.BASIS_GLL)["xgll"]
+        pts = []
+        for k in range(nc[2]):
+            for j in range(nc[1]):
+                for i in range(nc[0]):
+                    c, b, aa = np.meshgrid(xg, xg, xg, indexing="ij")
+                    pts.append([(i + aa) * h, (j + b) * h, (k + c) * h])
+        P = [np.concatenate([q[dd].ravel() for q in pts]) for dd in range(3)]
+        u, dudt = _wave(P, 0.0, a)
+        d = O.dg(p, nc, (h, h, h), velocity=a, inverse_mass=1)
+        errs.append(np.abs(O.dg_advect_apply(d, u) - dudt).max() / np.abs(dudt).max())
+    assert errs[0] > errs[1] > errs[2]
+    assert errs[2] < 2e-2
+
+
+def test_kappa_gradient_central_differences():
+    """dL/dkappa of L = 1/2 |A(kappa) x - b|^2 against central differences
+    with step 1e-6 (relative), FP64"""
+    p, nc = 2, (2, 2, 2)
+    m = O.mesh(p, nc, deform=0.05)
+    G = O.cont_geometry(m)
+    rng = np.random.default_rng(4)
+    nq = 8 * (p + 1) ** 3
+    kappa = np.exp(0.5 * rng.standard_normal(nq))
+    x = rng.uniform(-1, 1, O.cont_n_dofs(m))
+    b = rng.uniform(-1, 1, O.cont_n_dofs(m))
+
+    def L(k):
+        r = O.cont_apply(m, G, x, kappa=k) - b
+        return 0.5 * r @ r
+
+    r = O.cont_apply(m, G, x, kappa=kappa) - b
+    g = O.cont_kappa_grad(m, G, x, r)
+    for q in rng.choice(nq, 12, replace=False):
+        hstep = 1e-6 * kappa[q]
+        kp, km = kappa.copy(), kappa.copy()
+        kp[q] += hstep
+        km[q] -= hstep
+        fd = (L(kp) - L(km)) / (2 * hstep)
+        assert abs(fd - g[q]) <= 1e-6 * max(abs(fd), 1e-3 * np.abs(g).max()), (q, fd, g[q])
