@@ -145,6 +145,17 @@ int sf_diagonal(sf_op *op, int prec, void *diag, void *stream);
 int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void *dkappa,
                       void *stream);
 
+/* Kernel selection for the continuous Laplacian: SF_KERNEL_AUTO uses the
+ * FP32 plane-ownership kernel for degrees 1..4 and the generic
+ * line-ownership kernel otherwise; SF_KERNEL_GENERIC forces the latter
+ * (for comparisons).  No reference counterpart. */
+typedef enum { SF_KERNEL_AUTO = 0, SF_KERNEL_GENERIC = 1 } sf_kernel_variant;
+int sf_set_kernel_variant(sf_op *op, int variant);
+/* Device-side error flags of the handle's kernels (bit 0: a bounded wait
+ * for an asynchronous copy timed out; the result of that apply is invalid).
+ * Synchronous.  No reference counterpart. */
+int sf_device_status(sf_op *op, int *flags);
+
 /* ---------------- conjugate gradients ---------------- */
 typedef enum {
   SF_SOLVE_FP64 = 0,        /* plain CG, FP64 operator                          */

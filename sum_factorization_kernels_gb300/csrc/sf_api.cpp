@@ -73,26 +73,32 @@ int check_ptr(const void *p, int prec, const char *name)
     if (r_ != SF_OK) return r_;                                                \
   } while (0)
 
+// derived FP32 copies of the FP64 geometry (and coefficient): the natural
+// layout for the generic kernels, the colour-major plane layout for the
+// FP32 degree 1..4 kernel
+int derive_fp32_geometry(sf_op *op)
+{
+  if (!(op->desc.precisions & 2) || !op->deformed) return SF_OK;
+  const size_t entries = (size_t)op->n_cells * op->geo_stride;
+  if (op->geo32.bytes != entries * sizeof(float)) SF_RET(op->geo32.alloc(entries * sizeof(float)));
+  SF_RET(launch_convert((long long)entries, SF_FP64, op->geo64.ptr, SF_FP32, op->geo32.ptr, 0));
+  if (op->n <= 5)
+    SF_RET(repack_plane_geometry(op, (const double *)op->geo64.ptr, op->geo_stride,
+                                 op->has_kappa ? (const double *)op->kap64.ptr : nullptr, 0));
+  SF_CUDA_TRY(cudaDeviceSynchronize());
+  return SF_OK;
+}
+
+// the FP64 geometry is always kept (it is the source of the FP32 copies)
 int prepare_geometry(sf_op *op)
 {
   const long long n3 = (long long)op->n * op->n * op->n;
   op->geo_stride = (6 * n3 + 3) / 4 * 4; // 16-byte aligned cell blocks in FP32
   const size_t entries = (size_t)op->n_cells * op->geo_stride;
-  if (op->desc.precisions & 1) SF_RET(op->geo64.alloc(entries * sizeof(double)));
-  // FP64 geometry is always computed; keep a temporary if FP64 is not prepared
-  DevBuf tmp;
-  double *G64 = (double *)op->geo64.ptr;
-  if (!G64) {
-    SF_RET(tmp.alloc(entries * sizeof(double)));
-    G64 = (double *)tmp.ptr;
-  }
-  SF_RET(launch_geometry(op, G64, 0));
-  if (op->desc.precisions & 2) {
-    SF_RET(op->geo32.alloc(entries * sizeof(float)));
-    SF_RET(launch_convert((long long)entries, SF_FP64, G64, SF_FP32, op->geo32.ptr, 0));
-  }
+  SF_RET(op->geo64.alloc(entries * sizeof(double)));
+  SF_RET(launch_geometry(op, (double *)op->geo64.ptr, 0));
   SF_CUDA_TRY(cudaDeviceSynchronize());
-  return SF_OK;
+  return derive_fp32_geometry(op);
 }
 
 } // namespace
@@ -139,6 +145,14 @@ int sf_create(const sf_desc *desc, sf_op **out)
     delete op;
     return fail(SF_ERR_INVALID, "problem too large");
   }
+  {
+    int r = op->dev_err.alloc(sizeof(int));
+    if (r == SF_OK && cudaMemset(op->dev_err.ptr, 0, sizeof(int)) != cudaSuccess) r = SF_ERR_CUDA;
+    if (r != SF_OK) {
+      delete op;
+      return r;
+    }
+  }
   if (d.kind == SF_OP_LAPLACE && d.deform > 0.0) {
     op->deformed = true;
     int r = prepare_geometry(op);
@@ -154,6 +168,7 @@ int sf_create(const sf_desc *desc, sf_op **out)
 int sf_destroy(sf_op *op)
 {
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  release_solver_cache(op);
   delete op;
   return SF_OK;
 }
@@ -174,24 +189,11 @@ int sf_set_geometry(sf_op *op, const double *G)
   const long long n3 = (long long)op->n * op->n * op->n;
   op->geo_stride = (6 * n3 + 3) / 4 * 4;
   const size_t entries = (size_t)op->n_cells * op->geo_stride;
-  DevBuf tmp;
-  double *G64;
-  if (op->desc.precisions & 1) {
-    if (op->geo64.bytes != entries * sizeof(double)) SF_RET(op->geo64.alloc(entries * sizeof(double)));
-    G64 = (double *)op->geo64.ptr;
-  } else {
-    SF_RET(tmp.alloc(entries * sizeof(double)));
-    G64 = (double *)tmp.ptr;
-  }
-  SF_CUDA_TRY(cudaMemcpy2D(G64, op->geo_stride * sizeof(double), G, 6 * n3 * sizeof(double),
+  if (op->geo64.bytes != entries * sizeof(double)) SF_RET(op->geo64.alloc(entries * sizeof(double)));
+  SF_CUDA_TRY(cudaMemcpy2D(op->geo64.ptr, op->geo_stride * sizeof(double), G, 6 * n3 * sizeof(double),
                            6 * n3 * sizeof(double), (size_t)op->n_cells, cudaMemcpyDeviceToDevice));
-  if (op->desc.precisions & 2) {
-    if (op->geo32.bytes != entries * sizeof(float)) SF_RET(op->geo32.alloc(entries * sizeof(float)));
-    SF_RET(launch_convert((long long)entries, SF_FP64, G64, SF_FP32, op->geo32.ptr, 0));
-  }
-  SF_CUDA_TRY(cudaDeviceSynchronize());
   op->deformed = true;
-  return SF_OK;
+  return derive_fp32_geometry(op);
 }
 
 int sf_set_coefficient(sf_op *op, const double *kappa)
@@ -202,21 +204,36 @@ int sf_set_coefficient(sf_op *op, const double *kappa)
     op->kap64.release();
     op->kap32.release();
     op->has_kappa = false;
-    return SF_OK;
+    return derive_fp32_geometry(op);
   }
   SF_RET(check_ptr(kappa, SF_FP64, "kappa"));
   const long long n3 = (long long)op->n * op->n * op->n;
   const size_t entries = (size_t)op->n_cells * n3;
-  if (op->desc.precisions & 1) {
-    if (op->kap64.bytes != entries * sizeof(double)) SF_RET(op->kap64.alloc(entries * sizeof(double)));
-    SF_CUDA_TRY(cudaMemcpy(op->kap64.ptr, kappa, entries * sizeof(double), cudaMemcpyDeviceToDevice));
-  }
+  if (op->kap64.bytes != entries * sizeof(double)) SF_RET(op->kap64.alloc(entries * sizeof(double)));
+  SF_CUDA_TRY(cudaMemcpy(op->kap64.ptr, kappa, entries * sizeof(double), cudaMemcpyDeviceToDevice));
   if (op->desc.precisions & 2) {
     if (op->kap32.bytes != entries * sizeof(float)) SF_RET(op->kap32.alloc(entries * sizeof(float)));
     SF_RET(launch_convert((long long)entries, SF_FP64, kappa, SF_FP32, op->kap32.ptr, 0));
   }
-  SF_CUDA_TRY(cudaDeviceSynchronize());
   op->has_kappa = true;
+  SF_RET(derive_fp32_geometry(op));
+  SF_CUDA_TRY(cudaDeviceSynchronize());
+  return SF_OK;
+}
+
+int sf_set_kernel_variant(sf_op *op, int variant)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (variant != SF_KERNEL_AUTO && variant != SF_KERNEL_GENERIC)
+    return fail(SF_ERR_INVALID, "unknown kernel variant");
+  op->force_line_kernel = variant == SF_KERNEL_GENERIC;
+  return SF_OK;
+}
+
+int sf_device_status(sf_op *op, int *flags)
+{
+  if (!op || !flags) return fail(SF_ERR_NULL, "op/flags is NULL");
+  SF_CUDA_TRY(cudaMemcpy(flags, op->dev_err.ptr, sizeof(int), cudaMemcpyDeviceToHost));
   return SF_OK;
 }
 

@@ -9,6 +9,8 @@
 
 #include "../../include/sfgpu.h"
 
+struct sf_op;
+
 namespace sf {
 
 constexpr int kMaxDegree = 8;
@@ -33,6 +35,9 @@ int fill_shape(int degree, int basis, Shape1D &s);
 // thread-local error text for sf_last_error()
 void set_error(const std::string &msg);
 
+// drops the cached preconditioner state of a handle (sf_solver.cu)
+void release_solver_cache(sf_op *op);
+
 // device buffer owned by a handle
 struct DevBuf {
   void *ptr = nullptr;
@@ -56,6 +61,10 @@ struct sf_op {
   sf::DevBuf kap64, kap32;      // [cell][n^3] coefficient
   bool has_kappa = false;
   sf::DevBuf scratch;           // operator-private scratch (transpose, M^-1)
+  sf::DevBuf geoP;              // FP32 geometry for the plane kernel (colour-major)
+  long long geoP_stride = 0;
+  sf::DevBuf dev_err;           // device error flags (bounded waits)
+  bool force_line_kernel = false;
   double h[3];
 };
 

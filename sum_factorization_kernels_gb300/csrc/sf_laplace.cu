@@ -391,6 +391,132 @@ __global__ void geometry_kernel(const __grid_constant__ GeoArgs A)
   }
 }
 
+// Diagonal of the cell operator by sum factorisation.  With Dt = D S (the
+// derivative of the basis at the Gauss points), Z = S.S, Q = Dt.Dt and
+// P = Dt.S (entrywise products), the diagonal entry of local node (a,b,c) is
+//   sum_q [ G0 Q_a Z_b Z_c + G1 Z_a Q_b Z_c + G2 Z_a Z_b Q_c
+//         + 2 G3 P_a P_b Z_c + 2 G4 P_a Z_b P_c + 2 G5 Z_a P_b P_c ](q)
+// (M_a meaning M[q_x][a] etc.); each term is three transposed 1D
+// contractions of one geometry component.  Terms are grouped by their z
+// factor so that the z contraction runs three times, not six.
+template <int N, typename T>
+struct DiagTables {
+  EOMat<N, T> ZT, QT, PT;
+};
+
+template <int N, typename T, bool DEFORMED, bool KAPPA>
+__global__ void __launch_bounds__(CellsPerBlock<N>::value *N *N)
+    cont_diag_kernel(const __grid_constant__ ContArgs<N, T> A, const __grid_constant__ DiagTables<N, T> M)
+{
+  constexpr int N2 = N * N, N3 = N * N * N;
+  constexpr int CPB = CellsPerBlock<N>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *smem = reinterpret_cast<T *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int cs = tid / N2;
+  const int t = tid - cs * N2;
+  const int a = t % N, b = t / N;
+  T *B0 = smem + cs * 4 * N3, *GZ = B0 + N3, *GQ = GZ + N3, *GP = GQ + N3;
+  const CellPos<N, T> p = cell_position<N, T>(A, (long long)blockIdx.x * CPB + cs, a, b);
+  const T wab = A.w[a] * A.w[b];
+  T v[N];
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    GZ[t + N2 * c] = T(0);
+    GQ[t + N2 * c] = T(0);
+    GP[t + N2 * c] = T(0);
+  }
+#pragma unroll 1
+  for (int e = 0; e < 6; ++e) {
+    // component e on the column t, times kappa; factor 2 for off-diagonals
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      const int q = t + N2 * c;
+      T g;
+      if (DEFORMED) {
+        g = p.valid ? __ldg(A.geo + p.cell * A.geo_stride + e * N3 + q) : T(0);
+      } else {
+        g = e < 3 ? A.aff[e] * wab * A.w[c] : T(0);
+      }
+      if (KAPPA) g *= p.valid ? __ldg(A.kappa + p.cell * N3 + q) : T(0);
+      B0[q] = e >= 3 ? T(2) * g : g;
+    }
+    __syncthreads();
+    // x contraction on line t
+#pragma unroll
+    for (int m = 0; m < N; ++m) v[m] = B0[N * t + m];
+    if (e == 0) eo_apply<N, 1>(M.QT, v, v);
+    else if (e == 1 || e == 2 || e == 5) eo_apply<N, 1>(M.ZT, v, v);
+    else eo_apply<N, -1>(M.PT, v, v);
+#pragma unroll
+    for (int m = 0; m < N; ++m) B0[N * t + m] = v[m];
+    __syncthreads();
+    // y contraction on line (a, c=b), accumulate into the z-factor group
+#pragma unroll
+    for (int m = 0; m < N; ++m) v[m] = B0[a + N * m + N2 * b];
+    if (e == 1) eo_apply<N, 1>(M.QT, v, v);
+    else if (e == 0 || e == 2 || e == 4) eo_apply<N, 1>(M.ZT, v, v);
+    else eo_apply<N, -1>(M.PT, v, v);
+    T *grp = (e == 0 || e == 1 || e == 3) ? GZ : (e == 2 ? GQ : GP);
+#pragma unroll
+    for (int m = 0; m < N; ++m) grp[a + N * m + N2 * b] += v[m];
+    __syncthreads();
+  }
+  T r[N];
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = GZ[t + N2 * m];
+  eo_apply<N, 1>(M.ZT, v, r);
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = GQ[t + N2 * m];
+  eo_apply<N, 1>(M.QT, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) r[m] += v[m];
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = GP[t + N2 * m];
+  eo_apply<N, -1>(M.PT, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) r[m] += v[m];
+  if (p.valid) {
+    const bool side = A.dirichlet && (p.X == 0 || p.X == A.Nx - 1 || p.Y == 0 || p.Y == A.Ny - 1);
+    const long long plane = A.Nx * A.Ny;
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      const int Z = p.Z0 + c;
+      const bool bnd = side || (A.dirichlet && (Z == 0 || Z == A.Nz - 1));
+      if (!bnd) A.y[p.gbase + (long long)c * plane] += r[c];
+    }
+  }
+}
+
+template <typename T>
+__global__ void fill_boundary_kernel(T *__restrict__ y, T val, long long Nx, long long Ny, long long Nz)
+{
+  const long long nzf = Nx * Ny, nyf = Nx * (Nz - 2), nxf = (Ny - 2) * (Nz - 2);
+  const long long total = 2 * (nzf + nyf + nxf);
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < total;
+       s += (long long)gridDim.x * blockDim.x) {
+    long long X, Y, Z, r = s;
+    if (r < 2 * nzf) {
+      Z = r < nzf ? 0 : Nz - 1;
+      r %= nzf;
+      X = r % Nx;
+      Y = r / Nx;
+    } else if ((r -= 2 * nzf) < 2 * nyf) {
+      Y = r < nyf ? 0 : Ny - 1;
+      r %= nyf;
+      X = r % Nx;
+      Z = 1 + r / Nx;
+    } else {
+      r -= 2 * nyf;
+      X = r < nxf ? 0 : Nx - 1;
+      r %= nxf;
+      Y = 1 + r % (Ny - 2);
+      Z = 1 + r / (Ny - 2);
+    }
+    y[(Z * Ny + Y) * Nx + X] = val;
+  }
+}
+
 template <int N, typename T>
 ContArgs<N, T> make_args(const sf_op *op)
 {
@@ -475,6 +601,59 @@ int cont_kappa_grad_impl(const sf_op *op, const T *u, const T *lam, T *dk, cudaS
   return SF_OK;
 }
 
+template <int N, typename T>
+int cont_diag_impl(const sf_op *op, T *diag, cudaStream_t st)
+{
+  constexpr int CPB = CellsPerBlock<N>::value;
+  constexpr int N3 = N * N * N;
+  ContArgs<N, T> A = make_args<N, T>(op);
+  A.y = diag;
+  A.geo = (const T *)(sizeof(T) == 8 ? op->geo64.ptr : op->geo32.ptr);
+  A.kappa = (const T *)(sizeof(T) == 8 ? op->kap64.ptr : op->kap32.ptr);
+  const Shape1D &s = op->shape;
+  double Dt[kMaxN][kMaxN], Z[kMaxN][kMaxN], Q[kMaxN][kMaxN], P[kMaxN][kMaxN];
+  for (int q = 0; q < N; ++q)
+    for (int i = 0; i < N; ++i) {
+      double d = 0;
+      for (int j = 0; j < N; ++j) d += s.D[q][j] * s.S[j][i];
+      Dt[q][i] = d;
+    }
+  for (int q = 0; q < N; ++q)
+    for (int i = 0; i < N; ++i) {
+      Z[q][i] = s.S[q][i] * s.S[q][i];
+      Q[q][i] = Dt[q][i] * Dt[q][i];
+      P[q][i] = Dt[q][i] * s.S[q][i];
+    }
+  DiagTables<N, T> M;
+  M.ZT = eo_of<N, T>(Z, true);
+  M.QT = eo_of<N, T>(Q, true);
+  M.PT = eo_of<N, T>(P, true);
+  const size_t smem = size_t(CPB) * 4 * N3 * sizeof(T);
+  const bool kap = op->has_kappa;
+  auto kern = op->deformed ? (kap ? cont_diag_kernel<N, T, true, true> : cont_diag_kernel<N, T, true, false>)
+                           : (kap ? cont_diag_kernel<N, T, false, true> : cont_diag_kernel<N, T, false, false>);
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SF_CUDA_TRY(cudaMemsetAsync(diag, 0, sizeof(T) * op->n_dofs, st));
+  A.step = 2;
+  for (int color = 0; color < 8; ++color) {
+    A.cx = color & 1;
+    A.cy = (color >> 1) & 1;
+    A.cz = (color >> 2) & 1;
+    A.mx = (A.nc[0] - A.cx + 1) / 2;
+    A.my = (A.nc[1] - A.cy + 1) / 2;
+    const int mz = (A.nc[2] - A.cz + 1) / 2;
+    A.count = (long long)A.mx * A.my * mz;
+    if (A.count == 0) continue;
+    kern<<<dim3((unsigned)((A.count + CPB - 1) / CPB)), dim3(CPB * N * N), smem, st>>>(A, M);
+    SF_CUDA_TRY(cudaGetLastError());
+  }
+  if (A.dirichlet) {
+    fill_boundary_kernel<T><<<1024, 256, 0, st>>>(diag, T(1), A.Nx, A.Ny, A.Nz);
+    SF_CUDA_TRY(cudaGetLastError());
+  }
+  return SF_OK;
+}
+
 } // namespace
 } // namespace sf
 
@@ -511,6 +690,7 @@ int cont_kgrad_n(const sf_op *op, int prec, const void *u, const void *l, void *
 
 int launch_cont_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
 {
+  if (plane_path(op, prec)) return launch_cont_vmult_plane(op, (const float *)x, (float *)y, st);
   SF_DEG_DISPATCH(op->desc.degree, cont_vmult_n, op, prec, x, y, st)
 }
 
@@ -518,6 +698,20 @@ int launch_cont_kappa_grad(const sf_op *op, int prec, const void *u, const void 
                            cudaStream_t st)
 {
   SF_DEG_DISPATCH(op->desc.degree, cont_kgrad_n, op, prec, u, lam, dk, st)
+}
+
+namespace {
+template <int N>
+int cont_diag_n(const sf_op *op, int prec, void *d, cudaStream_t st)
+{
+  if (prec == SF_FP64) return cont_diag_impl<N, double>(op, (double *)d, st);
+  return cont_diag_impl<N, float>(op, (float *)d, st);
+}
+} // namespace
+
+int launch_cont_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st)
+{
+  SF_DEG_DISPATCH(op->desc.degree, cont_diag_n, op, prec, diag, st)
 }
 
 int launch_geometry(const sf_op *op, double *G, cudaStream_t st)

@@ -14,6 +14,12 @@ int launch_cont_kappa_grad(const sf_op *op, int prec, const void *u, const void 
 int launch_geometry(const sf_op *op, double *G, cudaStream_t st);
 int launch_cont_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
 
+// sf_laplace_plane.cu (FP32, degrees 1..4)
+bool plane_path(const sf_op *op, int prec);
+int launch_cont_vmult_plane(const sf_op *op, const float *x, float *y, cudaStream_t st);
+int repack_plane_geometry(sf_op *op, const double *G64, long long s64, const double *kap64,
+                          cudaStream_t st);
+
 // sf_dg.cu
 int launch_dg_vmult(const sf_op *op, int prec, int nrhs, bool transpose, const void *x, void *y,
                     const void *cheb_b, const void *cheb_dinv, void *cheb_t, double c_np,

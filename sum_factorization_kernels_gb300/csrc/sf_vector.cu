@@ -31,9 +31,9 @@ __global__ void convert_kernel(long long n, const S *__restrict__ x, D *__restri
 }
 
 template <typename T>
-__global__ void vector_update_kernel(long long n, const T *__restrict__ ax, const T *__restrict__ b,
+__global__ void vector_update_kernel(long long n, const T *ax, const T *__restrict__ b,
                                      const T *__restrict__ dinv, const T *__restrict__ xo,
-                                     T *__restrict__ xn, T *__restrict__ t, T c_np, T c_tm)
+                                     T *xn, T *__restrict__ t, T c_np, T c_tm)
 {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {

@@ -22,13 +22,14 @@ OP_LAPLACE, OP_DG_SIPG, OP_DG_ADVECT = 0, 1, 2
 BASIS_GLL, BASIS_HERMITE = 0, 1
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2
+KERNEL_AUTO, KERNEL_GENERIC = 0, 1
 
 EXPORTS = [
     "sf_last_error", "sf_version", "sf_create", "sf_destroy", "sf_sizes", "sf_set_geometry",
     "sf_set_coefficient", "sf_vmult", "sf_vmult_transpose", "sf_vmult_batched",
     "sf_vmult_transpose_batched", "sf_chebyshev_step", "sf_vector_update", "sf_diagonal",
     "sf_kappa_gradient", "sf_solve_opts_default", "sf_cg_solve", "sf_convert", "sf_dot",
-    "sf_shape_tables",
+    "sf_shape_tables", "sf_set_kernel_variant", "sf_device_status",
 ]
 
 
@@ -90,6 +91,8 @@ def lib():
         L.sf_convert.argtypes = [ll, i, vp, i, vp, vp]
         L.sf_dot.argtypes = [ll, i, vp, vp, vp, vp]
         L.sf_shape_tables.argtypes = [i, i, vp, vp, vp, vp]
+        L.sf_set_kernel_variant.argtypes = [vp, i]
+        L.sf_device_status.argtypes = [vp, C.POINTER(i)]
         _lib = L
     return _lib
 
@@ -199,6 +202,14 @@ class Operator:
 
     def set_coefficient(self, kappa):
         check(lib().sf_set_coefficient(self._h, ptr(kappa)))
+
+    def set_kernel_variant(self, variant):
+        check(lib().sf_set_kernel_variant(self._h, int(variant)))
+
+    def device_status(self):
+        f = C.c_int()
+        check(lib().sf_device_status(self._h, C.byref(f)))
+        return f.value
 
     def cg_solve(self, b, x, opts=None, stream=None):
         o = default_solve_opts() if opts is None else opts

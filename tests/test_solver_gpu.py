@@ -1,0 +1,98 @@
+"""Conjugate gradients on the GPU: all-FP64 and FP32-inner / FP64-refined
+solves reach the same 1e-10 relative residual; Chebyshev eigenvalue
+estimate checked against a dense eigen-decomposition."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.gpu_util import rel, to_dev, to_np, torch_cuda
+
+pytestmark = pytest.mark.gpu
+
+
+def _sf():
+    from sum_factorization_kernels_gb300 import sfgpu
+    return sfgpu
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("precond", [0, 1, 2])
+def test_cg_continuous_deformed(mode, precond):
+    torch = torch_cuda()
+    sf = _sf()
+    op = sf.Operator(sf.OP_LAPLACE, degree=4, n_cells=(12, 10, 8), deform=0.05)
+    b = torch.tensor(np.random.default_rng(1).uniform(-1, 1, op.n_dofs), device="cuda:0")
+    x = torch.zeros_like(b)
+    opts = sf.default_solve_opts(mode=mode, precond=precond, rtol=1e-10, max_iter=3000)
+    code, st = op.cg_solve(b, x, opts)
+    assert code == 0, (code, sf.lib().sf_last_error())
+    assert st.rel_residual <= 1e-10
+    # residual recomputed independently
+    ax = torch.empty_like(x)
+    op.vmult(x, ax)
+    assert float((b - ax).norm() / b.norm()) < 1.01e-10
+
+
+def test_cg_mixed_equals_fp64_solution():
+    torch = torch_cuda()
+    sf = _sf()
+    op = sf.Operator(sf.OP_LAPLACE, degree=5, n_cells=(8, 8, 8), deform=0.05)
+    b = torch.tensor(np.random.default_rng(2).uniform(-1, 1, op.n_dofs), device="cuda:0")
+    xs = []
+    for mode in (0, 1):
+        x = torch.zeros_like(b)
+        code, st = op.cg_solve(b, x, sf.default_solve_opts(mode=mode, rtol=1e-10))
+        assert code == 0
+        xs.append(x)
+    assert float((xs[0] - xs[1]).norm() / xs[0].norm()) < 1e-8
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_cg_dg_sipg_periodic(mode):
+    torch = torch_cuda()
+    sf = _sf()
+    op = sf.Operator(sf.OP_DG_SIPG, degree=5, n_cells=(8, 8, 8), length=(1.0, 1.0, 1.0))
+    b = torch.tensor(np.random.default_rng(3).standard_normal(op.n_dofs), device="cuda:0")
+    x = torch.zeros_like(b)
+    opts = sf.default_solve_opts(mode=mode, precond=2, rtol=1e-10, project_constant=1)
+    code, st = op.cg_solve(b, x, opts)
+    assert code == 0, sf.lib().sf_last_error()
+    assert st.rel_residual <= 1e-10
+    assert st.iterations < 400
+
+
+def test_lambda_max_estimate_vs_dense():
+    torch = torch_cuda()
+    sf = _sf()
+    p, nc = 2, (3, 3, 2)
+    op = sf.Operator(sf.OP_LAPLACE, degree=p, n_cells=nc, deform=0.05)
+    m = O.mesh(p, nc, deform=0.05)
+    G = O.cont_geometry(m)
+    n = O.cont_n_dofs(m)
+    A = np.zeros((n, n))
+    e = np.zeros(n)
+    for j in range(n):
+        e[j] = 1.0
+        A[:, j] = O.cont_apply(m, G, e)
+        e[j] = 0.0
+    d = np.diag(A)
+    lam = np.linalg.eigvals(A / d[:, None]).real.max()
+    b = torch.ones(op.n_dofs, dtype=torch.float64, device="cuda:0")
+    x = torch.zeros_like(b)
+    code, st = op.cg_solve(b, x, sf.default_solve_opts(precond=2, eig_iterations=30))
+    assert code == 0
+    assert 0.9 * lam < st.lambda_max <= lam * (1 + 1e-8)
+
+
+def test_invalid_options_and_advection_rejected():
+    torch = torch_cuda()
+    sf = _sf()
+    op = sf.Operator(sf.OP_DG_ADVECT, degree=2, n_cells=(2, 2, 2))
+    b = torch.ones(op.n_dofs, dtype=torch.float64, device="cuda:0")
+    x = torch.zeros_like(b)
+    code, _ = op.cg_solve(b, x)
+    assert code == -9
+    op2 = sf.Operator(sf.OP_LAPLACE, degree=2, n_cells=(2, 2, 2))
+    code, _ = op2.cg_solve(b[: op2.n_dofs].contiguous(), x[: op2.n_dofs].contiguous(),
+                           sf.default_solve_opts(cheb_range=0.5))
+    assert code == -1
