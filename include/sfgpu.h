@@ -119,6 +119,22 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
 int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, void *y,
                                void *stream);
 
+/* The transposed advection apply of sf_vmult_transpose_batched() for callers
+ * that cannot allocate device memory while they run -- for example code
+ * inside a stream capture, where cudaMalloc is not allowed, or code with its
+ * own memory pool.  No counterpart in the reference.  The intermediate
+ * vector of the inverse-mass form comes from a 4 MiB array compiled into the
+ * library (reserved on every GPU that loads it, until process exit) instead
+ * of a cudaMalloc'd buffer; this function allocates nothing.  Only for
+ * SF_OP_DG_ADVECT handles; nrhs * n_dofs * element size must not exceed
+ * 4 MiB (SF_ERR_INVALID otherwise).  The first call on a device looks up the
+ * array's device address once; make that first call before any stream
+ * capture.  All calls share the array (nothing in it needs to start at
+ * zero), so calls whose work overlaps on the GPU race: keep them on one
+ * stream or synchronise between them. */
+int sf_vmult_transpose_static(sf_op *op, int prec, int nrhs, const void *x, void *y,
+                              void *stream);
+
 /* Fused Chebyshev step, replaces do_cheby_iter<true>
  * (evaluation_dg_laplacian.h:513-554, fused update :485-502):
  *   t     <- c_tm * t + c_np * diag_inv .* (A x_old - b)

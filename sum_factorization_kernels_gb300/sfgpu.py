@@ -29,7 +29,7 @@ EXPORTS = [
     "sf_set_coefficient", "sf_vmult", "sf_vmult_transpose", "sf_vmult_batched",
     "sf_vmult_transpose_batched", "sf_chebyshev_step", "sf_vector_update", "sf_diagonal",
     "sf_kappa_gradient", "sf_solve_opts_default", "sf_cg_solve", "sf_convert", "sf_dot",
-    "sf_shape_tables", "sf_set_kernel_variant", "sf_device_status",
+    "sf_shape_tables", "sf_set_kernel_variant", "sf_device_status", "sf_vmult_transpose_static",
 ]
 
 
@@ -92,6 +92,7 @@ def lib():
         L.sf_dot.argtypes = [ll, i, vp, vp, vp, vp]
         L.sf_shape_tables.argtypes = [i, i, vp, vp, vp, vp]
         L.sf_set_kernel_variant.argtypes = [vp, i]
+        L.sf_vmult_transpose_static.argtypes = [vp, i, i, vp, vp, vp]
         L.sf_device_status.argtypes = [vp, C.POINTER(i)]
         _lib = L
     return _lib
@@ -181,6 +182,12 @@ class Operator:
     def vmult_transpose_batched(self, x, y, nrhs, stream=None):
         check(lib().sf_vmult_transpose_batched(self._h, prec_of(x), nrhs, ptr(x), ptr(y),
                                                stream_ptr(stream)))
+        return y
+
+    def vmult_transpose_static(self, x, y, nrhs=1, stream=None):
+        """transposed advection apply that allocates nothing (see sfgpu.h)"""
+        check(lib().sf_vmult_transpose_static(self._h, prec_of(x), nrhs, ptr(x), ptr(y),
+                                              stream_ptr(stream)))
         return y
 
     def chebyshev_step(self, b, diag_inv, x_old, x_new, t, c_np, c_tm, stream=None):
