@@ -204,6 +204,127 @@ def time_apply(op, x, y, steps, warmup, stream):
     return e0.elapsed_time(e1) / 1e3 / steps
 
 
+def secondary_configs(stream, peak):
+    """the other configurations of the metric, measured once each: config 1
+    (Q4 16^3 affine FP64, error vs the reference's golden vector), config 3
+    (DG SIPG p=5 48^3 CG to 1e-10: FP32-inner/FP64-refined vs all-FP64),
+    config 4 (variable kappa p=4 32^3: forward and adjoint), config 5 (DG
+    advection p=4 48^3, 8 right-hand sides: forward / transpose, dot test)"""
+    import numpy as np
+    import torch
+
+    from sum_factorization_kernels_gb300 import sfgpu
+
+    out = {}
+    # ---- config 1 ----
+    op = sfgpu.Operator(sfgpu.OP_LAPLACE, degree=4, n_cells=(16, 16, 16))
+    x = torch.tensor(np.random.default_rng(20241203).uniform(-1.0, 1.0, op.n_dofs), device="cuda")
+    y = torch.empty_like(x)
+    t = time_apply(op, x, y, 50, 5, stream)
+    g = np.load(os.path.join(ROOT, "tests", "golden", "cont.npz"))
+    idx = g["q4_16_sample_idx"]
+    yh = y.cpu().numpy()
+    err = float(np.linalg.norm(yh[idx] - g["q4_16_sample_y"]) / np.linalg.norm(g["q4_16_sample_y"]))
+    out["q4_affine_16c_fp64"] = {"n_dofs": op.n_dofs, "gdofs": round(op.n_dofs / t / 1e9, 3),
+                                 "rel_err_vs_reference_golden": float("%.3g" % err)}
+    del op, x, y
+    # ---- config 3 ----
+    op = sfgpu.Operator(sfgpu.OP_DG_SIPG, degree=5, n_cells=(48, 48, 48))
+    N = op.n_dofs
+    b = torch.tensor(np.random.default_rng(3).standard_normal(N), device="cuda")
+    xd32 = torch.randn(N, device="cuda", dtype=torch.float32)
+    yd32 = torch.empty_like(xd32)
+    t32 = time_apply(op, xd32, yd32, 20, 3, stream)
+    xd64 = xd32.double()
+    yd64 = torch.empty_like(xd64)
+    t64 = time_apply(op, xd64, yd64, 5, 2, stream)
+    res = {"n_dofs": N, "apply_fp32_gdofs": round(N / t32 / 1e9, 3),
+           "apply_fp32_hbm_frac": round(2 * 4 * N / t32 / 1e9 / peak, 4),
+           "apply_fp64_gdofs": round(N / t64 / 1e9, 3)}
+    for name, mode in (("mixed_fp32_inner", sfgpu.SOLVE_MIXED), ("all_fp64", sfgpu.SOLVE_FP64)):
+        xs = torch.zeros_like(b)
+        opts = sfgpu.default_solve_opts(mode=mode, precond=sfgpu.PRECOND_CHEBYSHEV, cheb_degree=5,
+                                        rtol=1e-10, project_constant=1, max_iter=4000)
+        op.cg_solve(b, torch.zeros_like(b), opts)  # preconditioner setup (cached per handle)
+        code, st = op.cg_solve(b, xs, opts)
+        res[name] = {"status": code, "iterations": st.iterations, "outer": st.outer_iterations,
+                     "rel_residual": float("%.3g" % st.rel_residual), "seconds": round(st.seconds, 3),
+                     "operator_applies": st.operator_applies}
+    if res["mixed_fp32_inner"]["seconds"] > 0:
+        res["fp64_over_mixed_wall_time"] = round(res["all_fp64"]["seconds"] / res["mixed_fp32_inner"]["seconds"], 2)
+    out["dg_sipg_p5_48c_cg"] = res
+    del op, b
+    torch.cuda.empty_cache()
+    # ---- config 4 ----
+    op = sfgpu.Operator(sfgpu.OP_LAPLACE, degree=4, n_cells=(32, 32, 32), deform=0.05)
+    nq = op.n_cells * 125
+    kap = torch.exp(0.5 * torch.randn(nq, dtype=torch.float64, device="cuda"))
+    op.set_coefficient(kap)
+    res = {"n_dofs": op.n_dofs}
+    for prec, dt in (("fp32", torch.float32), ("fp64", torch.float64)):
+        xx = (torch.rand(op.n_dofs, device="cuda", dtype=torch.float64) * 2 - 1).to(dt)
+        yy = torch.empty_like(xx)
+        tf = time_apply(op, xx, yy, 20, 3, stream)
+        dk = torch.empty(nq, dtype=dt, device="cuda")
+        for _ in range(3):
+            op.kappa_gradient(xx, yy, dk)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            op.kappa_gradient(xx, yy, dk)
+        e1.record()
+        torch.cuda.synchronize()
+        tg = e0.elapsed_time(e1) / 1e3 / 10
+        res[prec] = {"forward_gdofs": round(op.n_dofs / tf / 1e9, 3),
+                     "dkappa_gdofs": round(op.n_dofs / tg / 1e9, 3)}
+    out["kappa_p4_32c"] = res
+    del op
+    torch.cuda.empty_cache()
+    # ---- config 5 ----
+    op = sfgpu.Operator(sfgpu.OP_DG_ADVECT, degree=4, n_cells=(48, 48, 48), velocity=(1.0, 0.5, 0.25),
+                        inverse_mass=1)
+    N = op.n_dofs
+    res = {"n_dofs_per_rhs": N, "nrhs": 8}
+    for prec, dt in (("fp32", torch.float32), ("fp64", torch.float64)):
+        xx = (torch.rand(8 * N, device="cuda", dtype=torch.float64) * 2 - 1).to(dt)
+        yy = torch.empty_like(xx)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        for _ in range(3):
+            op.vmult_batched(xx, yy, 8, stream=stream)
+            op.vmult_transpose_batched(xx, yy, 8, stream=stream)
+        torch.cuda.synchronize()
+        reps = 10 if prec == "fp32" else 3
+        ev[0].record(stream)
+        for _ in range(reps):
+            op.vmult_batched(xx, yy, 8, stream=stream)
+        ev[1].record(stream)
+        for _ in range(reps):
+            op.vmult_transpose_batched(xx, yy, 8, stream=stream)
+        ev[2].record(stream)
+        torch.cuda.synchronize()
+        tf = ev[0].elapsed_time(ev[1]) / 1e3 / reps
+        tt = ev[1].elapsed_time(ev[2]) / 1e3 / reps
+        res[prec] = {"forward_gdofs_per_rhs": round(N / tf / 1e9, 3),
+                     "forward_hbm_frac": round(2 * dt.itemsize * 8 * N / tf / 1e9 / peak, 4),
+                     "transpose_gdofs_per_rhs": round(N / tt / 1e9, 3)}
+    x64 = torch.rand(8 * N, device="cuda", dtype=torch.float64) * 2 - 1
+    y64 = torch.rand(8 * N, device="cuda", dtype=torch.float64) * 2 - 1
+    ax, aty = torch.empty_like(x64), torch.empty_like(y64)
+    op.vmult_batched(x64, ax, 8)
+    op.vmult_transpose_batched(y64, aty, 8)
+    worst = 0.0
+    for r in range(8):
+        s_ = slice(r * N, (r + 1) * N)
+        lhs, rhs = float(torch.dot(ax[s_], y64[s_])), float(torch.dot(x64[s_], aty[s_]))
+        worst = max(worst, abs(lhs - rhs) / float(ax[s_].norm() * y64[s_].norm()))
+    res["adjoint_dot_test_rel"] = float("%.3g" % worst)
+    out["dg_advect_p4_48c_8rhs"] = res
+    del op
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -245,7 +366,17 @@ def run_ours(args):
     value = N * world / t_step / 1e9
     bytes_apply = algorithmic_bytes(p, N, C, 4)
     achieved = bytes_apply / t_step / 1e9
-    launches_per_apply = 8 + 1  # 8 colour launches + boundary rows
+    launches_per_apply = 8  # one launch per colour class
+
+    # ---- the other kernel variant at the headline degree (plane ownership) ----
+    variants = {"line_gdofs": round(value / world, 3)}
+    for name, var in (("pair_fp32x2_gdofs", sfgpu.KERNEL_PAIR), ("plane_gdofs", sfgpu.KERNEL_PLANE)):
+        if var == sfgpu.KERNEL_PLANE and p > 4:
+            continue
+        op.set_kernel_variant(var)
+        tv = time_apply(op, x32, y32, max(10, args.steps // 2), 3, stream)
+        variants[name] = round(N / tv / 1e9, 3)
+    op.set_kernel_variant(sfgpu.KERNEL_AUTO)
 
     # ---- e2e: pinned host input -> device -> apply -> host, every step ----
     xh = torch.empty(N, dtype=torch.float32, pin_memory=True)
@@ -302,6 +433,10 @@ def run_ours(args):
             del opq, xq64, xq32, yq64, yq32
             torch.cuda.empty_cache()
 
+    configs = None
+    if not args.no_configs and world == 1:
+        configs = secondary_configs(stream, peak)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_reference(p, seconds=args.ref_seconds)
@@ -318,17 +453,18 @@ def run_ours(args):
                        "geometry": "merged 6-entry JxW J^-1 J^-T per Gauss point, FP32",
                        "dirichlet": True, "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "working set %.2f GB > 129 MB L2, no flush" % (bytes_apply / 1e9),
-                       "fp64_gdofs_same_degree": fp64_value},
+                       "fp64_gdofs_same_degree": fp64_value, "kernel_variants": variants},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": None, "peak_kind": peak_kind,
-                         "kernel": "cont_vmult_kernel<5,float,deformed> (8 colour launches per apply)",
+                         "kernel": "line_vmult_kernel<%d,float,deformed> (8 colour launches per apply)" % (p + 1),
                          "algorithmic_bytes_per_apply": bytes_apply},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,
             "gpu_launches": launches_per_apply * args.steps,
             "sweep": sweep,
+            "configs": configs,
         }
         print(json.dumps(line))
 
@@ -344,6 +480,7 @@ def main():
     ap.add_argument("--sweep", default="2,3,4,5,6,7,8")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip configs 1, 3, 4, 5")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -372,9 +372,11 @@ int sfo_shape_init(int degree, int basis, sfo_shape *s)
 /* ------------------------------------------------------------------------ */
 /* 1D even-odd contraction: matrix_vector_kernel.h:30-185                    */
 /* ------------------------------------------------------------------------ */
-void sfo_apply_1d(int nn, int stride, int type, int cor, int add_into,
-                  const double *c, const double *in, double *out,
-                  const double *add, int do_dg, const double *dg, double *face)
+#define SFO_INLINE static inline __attribute__((always_inline))
+
+SFO_INLINE void apply_1d_impl(int nn, int stride, int type, int cor, int add_into,
+                              const double *c, const double *in, double *out,
+                              const double *add, int do_dg, const double *dg, double *face)
 {
   const int mid = nn / 2, offset = (nn + 1) / 2;
   double xp[SFO_MAX_N], xm[SFO_MAX_N];
@@ -474,6 +476,13 @@ void sfo_apply_1d(int nn, int stride, int type, int cor, int add_into,
   }
 }
 
+void sfo_apply_1d(int nn, int stride, int type, int cor, int add_into,
+                  const double *c, const double *in, double *out,
+                  const double *add, int do_dg, const double *dg, double *face)
+{
+  apply_1d_impl(nn, stride, type, cor, add_into, c, in, out, add, do_dg, dg, face);
+}
+
 /* test_multiplication.cc:18-60 style plain contraction (no even-odd) */
 void sfo_apply_1d_plain(int n, int stride, const double *M, int transpose,
                         const double *in, double *out)
@@ -489,16 +498,16 @@ void sfo_apply_1d_plain(int n, int stride, const double *M, int transpose,
 }
 
 /* one tensor direction over all n^2 lines of a cell-local array */
-static void sweep(int n, int dir, int type, int cor, int add, const double *eo,
-                  const double *in, double *out)
+SFO_INLINE void sweep(int n, int dir, int type, int cor, int add, const double *eo,
+                      const double *in, double *out)
 {
   const int stride = dir == 0 ? 1 : (dir == 1 ? n : n * n);
   for (int i2 = 0; i2 < n; ++i2)
     for (int i1 = 0; i1 < n; ++i1) {
       const int base = dir == 0 ? (i1 * n + i2 * n * n)
                                 : (dir == 1 ? (i1 + i2 * n * n) : (i1 + i2 * n));
-      sfo_apply_1d(n, stride, type, cor, add, eo, in + base, out + base,
-                   add ? out + base : NULL, 0, NULL, NULL);
+      apply_1d_impl(n, stride, type, cor, add, eo, in + base, out + base,
+                    add ? out + base : NULL, 0, NULL, NULL);
     }
 }
 
@@ -507,11 +516,13 @@ static void sweep(int n, int dir, int type, int cor, int add, const double *eo,
 /* quadrature-point tensor of evaluation_cell_laplacian.h:392-415 generalised */
 /* to one 6-entry tensor per quadrature point (including JxW and kappa)      */
 /* ------------------------------------------------------------------------ */
-static void cell_grad(const sfo_shape *s, const double *in, double *uq,
-                      double *gx, double *gy, double *gz)
+#define SFO_MAX_NQ (SFO_MAX_N * SFO_MAX_N * SFO_MAX_N)
+
+SFO_INLINE void cell_grad_n(int n, const sfo_shape *s, const double *in, double *uq,
+                            double *gx, double *gy, double *gz)
 {
-  const int n = s->n, nq = n * n * n;
-  double *t = (double *)malloc(sizeof(double) * nq);
+  const int nq = n * n * n;
+  double t[SFO_MAX_NQ];
   sweep(n, 0, 0, 1, 0, s->S_eo, in, t);
   sweep(n, 1, 0, 1, 0, s->S_eo, t, uq);
   sweep(n, 2, 0, 1, 0, s->S_eo, uq, t);
@@ -519,34 +530,35 @@ static void cell_grad(const sfo_shape *s, const double *in, double *uq,
   sweep(n, 2, 1, 1, 0, s->D_eo, uq, gz);
   sweep(n, 1, 1, 1, 0, s->D_eo, uq, gy);
   sweep(n, 0, 1, 1, 0, s->D_eo, uq, gx);
-  free(t);
 }
 
-static void cell_integrate(const sfo_shape *s, const double *tx, const double *ty,
-                           const double *tz, double *out)
+static void cell_grad(const sfo_shape *s, const double *in, double *uq,
+                      double *gx, double *gy, double *gz)
 {
-  const int n = s->n, nq = n * n * n;
-  double *a = (double *)malloc(sizeof(double) * nq);
-  double *b = (double *)malloc(sizeof(double) * nq);
+  cell_grad_n(s->n, s, in, uq, gx, gy, gz);
+}
+
+SFO_INLINE void cell_integrate_n(int n, const sfo_shape *s, const double *tx, const double *ty,
+                                 const double *tz, double *out)
+{
+  double a[SFO_MAX_NQ], b[SFO_MAX_NQ];
   sweep(n, 0, 1, 0, 0, s->D_eo, tx, a);
   sweep(n, 1, 1, 0, 1, s->D_eo, ty, a);
   sweep(n, 2, 1, 0, 1, s->D_eo, tz, a);
   sweep(n, 2, 0, 0, 0, s->S_eo, a, b);
   sweep(n, 1, 0, 0, 0, s->S_eo, b, a);
   sweep(n, 0, 0, 0, 0, s->S_eo, a, out);
-  free(a);
-  free(b);
 }
 
 /* geometry pointer Gcell has 6 blocks of geo_stride entries (0 => one
  * constant tensor for the whole cell, reference Cartesian form) */
-static void cell_apply_k(const sfo_shape *s, const double *G, int gs,
-                         const double *kappa, const double *in, double *out)
+SFO_INLINE void cell_apply_n(int n, const sfo_shape *s, const double *G, int gs,
+                             const double *kappa, const double *in, double *out)
 {
-  const int n = s->n, nq = n * n * n;
-  double *buf = (double *)malloc(sizeof(double) * nq * 4);
+  const int nq = n * n * n;
+  double buf[4 * SFO_MAX_NQ];
   double *uq = buf, *gx = buf + nq, *gy = buf + 2 * nq, *gz = buf + 3 * nq;
-  cell_grad(s, in, uq, gx, gy, gz);
+  cell_grad_n(n, s, in, uq, gx, gy, gz);
   for (int q = 0; q < nq; ++q) {
     const int o = gs ? q : 0;
     const double *g = G + o;
@@ -559,8 +571,24 @@ static void cell_apply_k(const sfo_shape *s, const double *G, int gs,
     gy[q] = t1 * k;
     gz[q] = t2 * k;
   }
-  cell_integrate(s, gx, gy, gz, out);
-  free(buf);
+  cell_integrate_n(n, s, gx, gy, gz, out);
+}
+
+/* one specialised copy of the cell operator per degree */
+static void cell_apply_k(const sfo_shape *s, const double *G, int gs,
+                         const double *kappa, const double *in, double *out)
+{
+  switch (s->n) {
+  case 2: cell_apply_n(2, s, G, gs, kappa, in, out); break;
+  case 3: cell_apply_n(3, s, G, gs, kappa, in, out); break;
+  case 4: cell_apply_n(4, s, G, gs, kappa, in, out); break;
+  case 5: cell_apply_n(5, s, G, gs, kappa, in, out); break;
+  case 6: cell_apply_n(6, s, G, gs, kappa, in, out); break;
+  case 7: cell_apply_n(7, s, G, gs, kappa, in, out); break;
+  case 8: cell_apply_n(8, s, G, gs, kappa, in, out); break;
+  case 9: cell_apply_n(9, s, G, gs, kappa, in, out); break;
+  default: cell_apply_n(s->n, s, G, gs, kappa, in, out); break;
+  }
 }
 
 void sfo_cell_apply(const sfo_shape *s, const double *Gcell, int geo_stride,

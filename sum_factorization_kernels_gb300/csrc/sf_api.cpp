@@ -76,15 +76,30 @@ int check_ptr(const void *p, int prec, const char *name)
 // derived FP32 copies of the FP64 geometry (and coefficient): the natural
 // layout for the generic kernels, the colour-major plane layout for the
 // FP32 degree 1..4 kernel
+// The plane and pair kernels read their own FP32 geometry layouts; these
+// copies exist only while the kernel variant that reads them is selected.
+int derive_variant_geometry(sf_op *op)
+{
+  const bool fp32 = (op->desc.precisions & 2) && op->deformed && op->desc.kind == SF_OP_LAPLACE;
+  const double *k64 = op->has_kappa ? (const double *)op->kap64.ptr : nullptr;
+  if (fp32 && op->kernel_variant == SF_KERNEL_PLANE && op->n <= 5)
+    SF_RET(repack_plane_geometry(op, (const double *)op->geo64.ptr, op->geo_stride, k64, 0));
+  else
+    op->geoP.release();
+  if (fp32 && op->kernel_variant == SF_KERNEL_PAIR)
+    SF_RET(repack_pair_geometry(op, (const double *)op->geo64.ptr, op->geo_stride, k64, 0));
+  else
+    op->geoPair.release();
+  return SF_OK;
+}
+
 int derive_fp32_geometry(sf_op *op)
 {
   if (!(op->desc.precisions & 2) || !op->deformed) return SF_OK;
   const size_t entries = (size_t)op->n_cells * op->geo_stride;
   if (op->geo32.bytes != entries * sizeof(float)) SF_RET(op->geo32.alloc(entries * sizeof(float)));
   SF_RET(launch_convert((long long)entries, SF_FP64, op->geo64.ptr, SF_FP32, op->geo32.ptr, 0));
-  if (op->n <= 5)
-    SF_RET(repack_plane_geometry(op, (const double *)op->geo64.ptr, op->geo_stride,
-                                 op->has_kappa ? (const double *)op->kap64.ptr : nullptr, 0));
+  SF_RET(derive_variant_geometry(op));
   SF_CUDA_TRY(cudaDeviceSynchronize());
   return SF_OK;
 }
@@ -135,6 +150,10 @@ int sf_create(const sf_desc *desc, sf_op **out)
   op->n = d.degree + 1;
   for (int k = 0; k < 3; ++k) op->h[k] = d.length[k] / d.n_cells[k];
   op->n_cells = (long long)d.n_cells[0] * d.n_cells[1] * d.n_cells[2];
+  if (op->n_cells >= (1LL << 31)) {
+    delete op;
+    return fail(SF_ERR_INVALID, "more than 2^31 - 1 cells");
+  }
   const long long n3 = (long long)op->n * op->n * op->n;
   if (d.kind == SF_OP_LAPLACE)
     op->n_dofs = ((long long)d.degree * d.n_cells[0] + 1) * ((long long)d.degree * d.n_cells[1] + 1) *
@@ -224,9 +243,11 @@ int sf_set_coefficient(sf_op *op, const double *kappa)
 int sf_set_kernel_variant(sf_op *op, int variant)
 {
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
-  if (variant != SF_KERNEL_AUTO && variant != SF_KERNEL_GENERIC)
+  if (variant < SF_KERNEL_AUTO || variant > SF_KERNEL_PAIR)
     return fail(SF_ERR_INVALID, "unknown kernel variant");
-  op->force_line_kernel = variant == SF_KERNEL_GENERIC;
+  op->kernel_variant = variant;
+  SF_RET(derive_variant_geometry(op));
+  SF_CUDA_TRY(cudaDeviceSynchronize());
   return SF_OK;
 }
 

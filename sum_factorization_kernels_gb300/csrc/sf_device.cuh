@@ -79,6 +79,24 @@ __device__ __forceinline__ T dot_row(const T (&row)[N], const T (&v)[N])
   return s;
 }
 
+// Synchronise the threads of one cell group.  A one-warp group uses
+// __syncwarp (no hardware barrier); larger groups use named barriers 1..3
+// with compile-time ids, so a block reserves only GROUPS + 1 of the SM's
+// barriers (a register id would reserve all 16 and cap residency).
+template <int G>
+__device__ __forceinline__ void cell_group_sync(int grp)
+{
+  if (G == 1) {
+    __syncwarp();
+  } else {
+    constexpr int NT = 32 * G;
+    if (grp == 0) asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
+    else if (grp == 1) asm volatile("bar.sync 2, %0;" ::"n"(NT) : "memory");
+    else if (grp == 2) asm volatile("bar.sync 3, %0;" ::"n"(NT) : "memory");
+    else asm volatile("bar.sync 4, %0;" ::"n"(NT) : "memory");
+  }
+}
+
 // cells per thread block for n^2 threads per cell (about 128-256 threads)
 template <int N>
 struct CellsPerBlock {

@@ -59,17 +59,15 @@ struct DGCells {
                                : N == 7 ? 5 : N == 8 ? 2 : 3;
 };
 
+// periodic neighbour of the cell (ix, iy, iz) across face `side` of
+// direction `dir` (no division: a +-1 step with wrap-around)
 template <int N, typename T>
-__device__ __forceinline__ long long neighbour(const DGArgs<N, T> &A, long long cell, int dir, int side)
+__device__ __forceinline__ long long neighbour(const DGArgs<N, T> &A, int ix, int iy, int iz, int dir, int side)
 {
-  long long ix = cell % A.nc[0];
-  long long iy = (cell / A.nc[0]) % A.nc[1];
-  long long iz = cell / ((long long)A.nc[0] * A.nc[1]);
-  const int d = side ? 1 : -1;
-  if (dir == 0) ix = (ix + d + A.nc[0]) % A.nc[0];
-  if (dir == 1) iy = (iy + d + A.nc[1]) % A.nc[1];
-  if (dir == 2) iz = (iz + d + A.nc[2]) % A.nc[2];
-  return (iz * A.nc[1] + iy) * A.nc[0] + ix;
+  if (dir == 0) ix = side ? (ix + 1 == A.nc[0] ? 0 : ix + 1) : (ix == 0 ? A.nc[0] - 1 : ix - 1);
+  if (dir == 1) iy = side ? (iy + 1 == A.nc[1] ? 0 : iy + 1) : (iy == 0 ? A.nc[1] - 1 : iy - 1);
+  if (dir == 2) iz = side ? (iz + 1 == A.nc[2] ? 0 : iz + 1) : (iz == 0 ? A.nc[2] - 1 : iz - 1);
+  return ((long long)iz * A.nc[1] + iy) * A.nc[0] + ix;
 }
 
 // face flux at one face point.  side 0: face at coordinate 0 (outer normal
@@ -176,6 +174,9 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   for (long long e = tid; e < nval; e += blockDim.x) Bblk[e] = __ldg(src + e);
   // ---- neighbour face layers ----
   if (valid) {
+    const unsigned uc = (unsigned)cell, unx = (unsigned)A.nc[0], uny = (unsigned)A.nc[1];
+    const unsigned q = uc / unx;
+    const int ix = int(uc - q * unx), iz = int(q / uny), iy = int(q - unsigned(iz) * uny);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       // face-local index t: x faces (b,c) = (t%N, t/N), y faces (a,c), z faces (a,b)
@@ -187,8 +188,8 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
       if (d == 0) { off = N * f0 + N2 * f1; stride_n = 1; }
       else if (d == 1) { off = f0 + N2 * f1; stride_n = N; }
       else { off = f0 + N * f1; stride_n = N2; }
-      base_in[0] = neighbour(A, cell, d, 0) * N3 + off;
-      base_in[1] = neighbour(A, cell, d, 1) * N3 + off;
+      base_in[0] = neighbour(A, ix, iy, iz, d, 0) * N3 + off;
+      base_in[1] = neighbour(A, ix, iy, iz, d, 1) * N3 + off;
       // side 0 (face at 0): neighbour's layer p (value) and p-1; side 1: layers 0 and 1
       const T v0 = __ldg(x + base_in[0] + (N - 1) * stride_n);
       const T v1 = __ldg(x + base_in[1]);
@@ -438,6 +439,8 @@ int dg_vmult_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T *y, c
     kern = cheb ? dg_kernel<N, T, K_ADVECT, false, false, true> : dg_kernel<N, T, K_ADVECT, false, false, false>;
   const size_t smem = (size_t(3) * CPB * N3 + size_t(CPB) * 12 * N * N) * sizeof(T);
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   cudaSharedmemCarveoutMaxShared));
   const long long blocks = (op->n_cells + CPB - 1) / CPB;
   kern<<<dim3((unsigned)blocks, (unsigned)nrhs), dim3(CPB * N * N), smem, st>>>(A);
   SF_CUDA_TRY(cudaGetLastError());

@@ -63,8 +63,10 @@ struct sf_op {
   sf::DevBuf scratch;           // operator-private scratch (transpose, M^-1)
   sf::DevBuf geoP;              // FP32 geometry for the plane kernel (colour-major)
   long long geoP_stride = 0;
+  sf::DevBuf geoPair;           // FP32 geometry for the pair kernel (pair-interleaved)
+  long long geoPair_stride = 0;
   sf::DevBuf dev_err;           // device error flags (bounded waits)
-  bool force_line_kernel = false;
+  int kernel_variant = 0;       // sf_kernel_variant
   double h[3];
 };
 

@@ -1,6 +1,12 @@
 // sf_laplace.cu -- continuous FE Laplacian -div(kappa grad u) on hexahedral
 // meshes of degree 1..8: operator apply, geometry, kappa-gradient, diagonal.
 //
+// The operator apply itself lives in sf_laplace_pair.cu (FP32, default),
+// sf_laplace_line.cu (FP64; FP32 on request) and sf_laplace_plane.cu (FP32,
+// degrees 1..4, on request); this file holds the
+// setup (geometry), diagonal and kappa-gradient kernels, which use the same
+// cell pipeline with one block of CPB cells and block barriers.
+//
 // Per cell the operator is y_e = S^T (sum_d D_d^T t_d), t = kappa_q G_q D S x_e
 // (S: basis -> Gauss values, D: collocation derivative, G: merged
 // JxW J^-1 J^-T), the sweep order of the reference's GLL cell Laplacian
@@ -173,81 +179,6 @@ __device__ __forceinline__ CellPos<N, T> cell_position(const ContArgs<N, T> &A, 
   return p;
 }
 
-template <int N, typename T, bool DEFORMED, bool KAPPA>
-__global__ void __launch_bounds__(CellsPerBlock<N>::value *N *N)
-    cont_vmult_kernel(const __grid_constant__ ContArgs<N, T> A)
-{
-  constexpr int N2 = N * N, N3 = N * N * N;
-  constexpr int CPB = CellsPerBlock<N>::value;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *smem = reinterpret_cast<T *>(smem_raw);
-  const int tid = threadIdx.x;
-  const int cs = tid / N2;
-  const int t = tid - cs * N2;
-  const int a = t % N, b = t / N;
-  T *B0 = smem + cs * 4 * N3, *B1 = B0 + N3, *B2 = B1 + N3, *B3 = B2 + N3;
-
-  const CellPos<N, T> p = cell_position<N, T>(A, (long long)blockIdx.x * CPB + cs, a, b);
-  T v[N];
-  gather_column<N, T>(A, A.x, p, v);
-  cell_gradients<N, T>(A, v, B0, B1, B2, B3, t, a, b);
-
-  // quadrature-point operation on column t
-  const T wab = A.w[a] * A.w[b];
-  T tz[N];
-#pragma unroll
-  for (int c = 0; c < N; ++c) {
-    const int q = t + N2 * c;
-    const T gx = B0[q], gy = B2[q], gz = B3[q];
-    T tx, ty, tzc;
-    if (DEFORMED) {
-      const T *G = A.geo + p.cell * A.geo_stride + q;
-      T g0 = T(0), g1 = T(0), g2 = T(0), g3 = T(0), g4 = T(0), g5 = T(0);
-      if (p.valid) {
-        g0 = __ldg(G);
-        g1 = __ldg(G + N3);
-        g2 = __ldg(G + 2 * N3);
-        g3 = __ldg(G + 3 * N3);
-        g4 = __ldg(G + 4 * N3);
-        g5 = __ldg(G + 5 * N3);
-      }
-      tx = gx * g0 + gy * g3 + gz * g4;
-      ty = gx * g3 + gy * g1 + gz * g5;
-      tzc = gx * g4 + gy * g5 + gz * g2;
-    } else {
-      const T wq = wab * A.w[c];
-      tx = gx * (A.aff[0] * wq);
-      ty = gy * (A.aff[1] * wq);
-      tzc = gz * (A.aff[2] * wq);
-    }
-    if (KAPPA) {
-      const T k = p.valid ? __ldg(A.kappa + p.cell * N3 + q) : T(0);
-      tx *= k;
-      ty *= k;
-      tzc *= k;
-    }
-    B0[q] = tx;
-    B2[q] = ty;
-    tz[c] = tzc;
-  }
-  cell_integrate<N, T>(A, tz, v, B0, B1, B2, t, a, b);
-
-  // colour-exclusive accumulation; Dirichlet rows are written afterwards
-  if (p.valid) {
-    const bool side = A.dirichlet && (p.X == 0 || p.X == A.Nx - 1 || p.Y == 0 || p.Y == A.Ny - 1);
-    const long long plane = A.Nx * A.Ny;
-#pragma unroll
-    for (int c = 0; c < N; ++c) {
-      const int Z = p.Z0 + c;
-      const bool bnd = side || (A.dirichlet && (Z == 0 || Z == A.Nz - 1));
-      if (!bnd) {
-        T *dst = A.y + p.gbase + (long long)c * plane;
-        *dst += v[c];
-      }
-    }
-  }
-}
-
 // dk_q = grad(u)_q . G_q grad(lam)_q  (G without kappa)
 template <int N, typename T, bool DEFORMED>
 __global__ void __launch_bounds__(CellsPerBlock<N>::value *N *N)
@@ -296,38 +227,6 @@ __global__ void __launch_bounds__(CellsPerBlock<N>::value *N *N)
       r = wq * (A.aff[0] * ux * gx[c] + A.aff[1] * uy * gy[c] + A.aff[2] * uz * gz[c]);
     }
     if (p.valid) A.y[p.cell * N3 + q] = r;
-  }
-}
-
-// boundary rows: y_b = x_b on all boundary nodes of the node grid
-template <typename T>
-__global__ void dirichlet_rows_kernel(const T *__restrict__ x, T *__restrict__ y, long long Nx,
-                                      long long Ny, long long Nz)
-{
-  const long long nzf = Nx * Ny, nyf = Nx * (Nz - 2), nxf = (Ny - 2) * (Nz - 2);
-  const long long total = 2 * (nzf + nyf + nxf);
-  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < total;
-       s += (long long)gridDim.x * blockDim.x) {
-    long long X, Y, Z, r = s;
-    if (r < 2 * nzf) {
-      Z = r < nzf ? 0 : Nz - 1;
-      r %= nzf;
-      X = r % Nx;
-      Y = r / Nx;
-    } else if ((r -= 2 * nzf) < 2 * nyf) {
-      Y = r < nyf ? 0 : Ny - 1;
-      r %= nyf;
-      X = r % Nx;
-      Z = 1 + r / Nx;
-    } else {
-      r -= 2 * nyf;
-      X = r < nxf ? 0 : Nx - 1;
-      r %= nxf;
-      Y = 1 + r % (Ny - 2);
-      Z = 1 + r / (Ny - 2);
-    }
-    const long long g = (Z * Ny + Y) * Nx + X;
-    y[g] = x[g];
   }
 }
 
@@ -539,44 +438,6 @@ ContArgs<N, T> make_args(const sf_op *op)
 }
 
 template <int N, typename T>
-int cont_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
-{
-  constexpr int CPB = CellsPerBlock<N>::value;
-  constexpr int N3 = N * N * N;
-  ContArgs<N, T> A = make_args<N, T>(op);
-  A.x = x;
-  A.y = y;
-  const bool deformed = op->deformed;
-  const bool kap = op->has_kappa;
-  A.geo = (const T *)(sizeof(T) == 8 ? op->geo64.ptr : op->geo32.ptr);
-  A.kappa = (const T *)(sizeof(T) == 8 ? op->kap64.ptr : op->kap32.ptr);
-  const size_t smem = size_t(CPB) * 4 * N3 * sizeof(T);
-  auto kern = deformed ? (kap ? cont_vmult_kernel<N, T, true, true> : cont_vmult_kernel<N, T, true, false>)
-                       : (kap ? cont_vmult_kernel<N, T, false, true> : cont_vmult_kernel<N, T, false, false>);
-  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  SF_CUDA_TRY(cudaMemsetAsync(y, 0, sizeof(T) * op->n_dofs, st));
-  A.step = 2;
-  for (int color = 0; color < 8; ++color) {
-    A.cx = color & 1;
-    A.cy = (color >> 1) & 1;
-    A.cz = (color >> 2) & 1;
-    A.mx = (A.nc[0] - A.cx + 1) / 2;
-    A.my = (A.nc[1] - A.cy + 1) / 2;
-    const int mz = (A.nc[2] - A.cz + 1) / 2;
-    A.count = (long long)A.mx * A.my * mz;
-    if (A.count == 0) continue;
-    const long long blocks = (A.count + CPB - 1) / CPB;
-    kern<<<dim3((unsigned)blocks), dim3(CPB * N * N), smem, st>>>(A);
-    SF_CUDA_TRY(cudaGetLastError());
-  }
-  if (A.dirichlet) {
-    dirichlet_rows_kernel<T><<<1024, 256, 0, st>>>(x, y, A.Nx, A.Ny, A.Nz);
-    SF_CUDA_TRY(cudaGetLastError());
-  }
-  return SF_OK;
-}
-
-template <int N, typename T>
 int cont_kappa_grad_impl(const sf_op *op, const T *u, const T *lam, T *dk, cudaStream_t st)
 {
   constexpr int CPB = CellsPerBlock<N>::value;
@@ -674,12 +535,6 @@ namespace sf {
 
 namespace {
 template <int N>
-int cont_vmult_n(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
-{
-  if (prec == SF_FP64) return cont_vmult_impl<N, double>(op, (const double *)x, (double *)y, st);
-  return cont_vmult_impl<N, float>(op, (const float *)x, (float *)y, st);
-}
-template <int N>
 int cont_kgrad_n(const sf_op *op, int prec, const void *u, const void *l, void *dk, cudaStream_t st)
 {
   if (prec == SF_FP64)
@@ -690,8 +545,9 @@ int cont_kgrad_n(const sf_op *op, int prec, const void *u, const void *l, void *
 
 int launch_cont_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
 {
+  if (pair_path(op, prec)) return launch_cont_vmult_pair(op, (const float *)x, (float *)y, st);
   if (plane_path(op, prec)) return launch_cont_vmult_plane(op, (const float *)x, (float *)y, st);
-  SF_DEG_DISPATCH(op->desc.degree, cont_vmult_n, op, prec, x, y, st)
+  return launch_cont_vmult_line(op, prec, x, y, st);
 }
 
 int launch_cont_kappa_grad(const sf_op *op, int prec, const void *u, const void *lam, void *dk,

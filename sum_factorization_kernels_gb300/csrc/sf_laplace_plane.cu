@@ -70,6 +70,9 @@ struct PlaneArgs {
   int color, cx, cy, cz, mx, my;
   long long count;
   int *err;
+  // ordinal stride of a warp's walk (warps x cells per warp), decomposed
+  // in the colour's (mi, mj, mk) index space
+  int step_i, step_j, step_k;
 };
 
 template <int N, int SIGN>
@@ -144,15 +147,21 @@ __global__ void __launch_bounds__(32 * PlaneCfg<N>::WARPS)
   pdl_trigger();
   uint32_t parity = 0;
   bool y_ready = false;
+  // (mi, mj, mk) of this lane's cell; advanced by the walk stride each batch
+  int mi, mj, mk;
+  {
+    const unsigned uo = (unsigned)(gw * CPW + k), umx = (unsigned)A.mx, umy = (unsigned)A.my;
+    const unsigned q = uo / umx;
+    mi = int(uo - q * umx);
+    mk = int(q / umy);
+    mj = int(q - unsigned(mk) * umy);
+  }
 
   for (long long batch = gw; batch < nbatch; batch += nw) {
     __syncwarp();
     const long long o = batch * CPW + k;
     const bool valid = active && o < A.count;
-    const long long oo = valid ? o : 0;
-    const int ci = 2 * int(oo % A.mx) + A.cx;
-    const int cj = 2 * int((oo / A.mx) % A.my) + A.cy;
-    const int ck = 2 * int(oo / ((long long)A.mx * A.my)) + A.cz;
+    const int ci = 2 * mi + A.cx, cj = 2 * mj + A.cy, ck = 2 * mk + A.cz;
     const long long X0 = (long long)ci * P;
     const bool dir = A.dirichlet != 0;
     const bool xl = dir && ci == 0, xr = dir && ci == A.nc[0] - 1;
@@ -349,6 +358,13 @@ __global__ void __launch_bounds__(32 * PlaneCfg<N>::WARPS)
         }
       }
     }
+    mi += A.step_i;
+    int carry = 0;
+    if (mi >= A.mx) { mi -= A.mx; carry = 1; }
+    mj += A.step_j + carry;
+    carry = 0;
+    if (mj >= A.my) { mj -= A.my; carry = 1; }
+    mk += A.step_k + carry;
   }
   if (!y_ready) pdl_wait();
 }
@@ -404,6 +420,10 @@ int plane_vmult_impl(const sf_op *op, const float *x, float *y, cudaStream_t st)
   const bool kap = op->has_kappa;
   A.geo = (const float *)op->geoP.ptr;
   A.gstride = op->geoP_stride;
+  if (op->deformed && !A.geo) {
+    set_error("plane kernel geometry missing");
+    return SF_ERR_STATE;
+  }
   void (*kern)(const PlaneArgs<N>);
   if (affine) {
     if (kap) {
@@ -418,8 +438,10 @@ int plane_vmult_impl(const sf_op *op, const float *x, float *y, cudaStream_t st)
   const long long region = (geo_f + 2 * Cfg::CPW * Cfg::CS + 31) / 32 * 32;
   const size_t smem = 128 + size_t(Cfg::WARPS) * region * sizeof(float);
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   cudaSharedmemCarveoutMaxShared));
   int per_sm = 0;
-  SF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * Cfg::WARPS, smem));
+  SF_RET_IF(resident_blocks_per_sm((const void *)kern, 32 * Cfg::WARPS, smem, &per_sm));
   if (per_sm < 1) per_sm = 1;
   int n_sm = 0, dev = 0;
   SF_CUDA_TRY(cudaGetDevice(&dev));
@@ -439,16 +461,23 @@ int plane_vmult_impl(const sf_op *op, const float *x, float *y, cudaStream_t st)
     if (A.count == 0) continue;
     const long long nbatch = (A.count + Cfg::CPW - 1) / Cfg::CPW;
     long long blocks = std::min<long long>((nbatch + Cfg::WARPS - 1) / Cfg::WARPS, (long long)per_sm * n_sm);
+    const long long stride = blocks * Cfg::WARPS * Cfg::CPW;
+    A.step_i = int(stride % A.mx);
+    A.step_j = int((stride / A.mx) % A.my);
+    A.step_k = int(stride / ((long long)A.mx * A.my));
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)blocks);
     cfg.blockDim = dim3(32 * Cfg::WARPS);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
+    // colours 1..7 overlap with their predecessor (they read x and the
+    // geometry before griddepcontrol.wait and touch y only after it); the
+    // first colour is ordered normally behind whatever produced x
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = color > 0 ? 1 : 0;
     SF_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A));
   }
   return SF_OK;
@@ -486,13 +515,10 @@ int plane_repack_impl(sf_op *op, const double *G64, long long s64, const double 
 
 } // namespace
 
-// the plane kernel is enabled once validated on the GPU
-constexpr bool kPlaneEnabled = false;
-
 bool plane_path(const sf_op *op, int prec)
 {
-  return kPlaneEnabled && prec == SF_FP32 && op->desc.kind == SF_OP_LAPLACE && op->n <= 5 && (op->deformed || !op->has_kappa) &&
-         !op->force_line_kernel;
+  return op->kernel_variant == SF_KERNEL_PLANE && prec == SF_FP32 && op->desc.kind == SF_OP_LAPLACE &&
+         op->n <= 5 && (op->deformed || !op->has_kappa);
 }
 
 int launch_cont_vmult_plane(const sf_op *op, const float *x, float *y, cudaStream_t st)

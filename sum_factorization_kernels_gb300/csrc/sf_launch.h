@@ -14,6 +14,15 @@ int launch_cont_kappa_grad(const sf_op *op, int prec, const void *u, const void 
 int launch_geometry(const sf_op *op, double *G, cudaStream_t st);
 int launch_cont_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
 
+// sf_laplace_line.cu (all degrees, FP64 and FP32)
+int launch_cont_vmult_line(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st);
+
+// sf_laplace_pair.cu (FP32, two cells per thread in packed FP32x2)
+bool pair_path(const sf_op *op, int prec);
+int launch_cont_vmult_pair(const sf_op *op, const float *x, float *y, cudaStream_t st);
+int repack_pair_geometry(sf_op *op, const double *G64, long long s64, const double *kap64,
+                         cudaStream_t st);
+
 // sf_laplace_plane.cu (FP32, degrees 1..4)
 bool plane_path(const sf_op *op, int prec);
 int launch_cont_vmult_plane(const sf_op *op, const float *x, float *y, cudaStream_t st);
@@ -27,6 +36,17 @@ int launch_dg_vmult(const sf_op *op, int prec, int nrhs, bool transpose, const v
 int launch_dg_inverse_mass(const sf_op *op, int prec, int nrhs, const void *x, void *y,
                            cudaStream_t st);
 int launch_dg_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
+
+// blocks of a kernel that fit on one SM with the maximum shared-memory
+// carveout: the occupancy calculator does not account for the carveout
+// preference, so persistent grids size themselves from the limits directly
+int resident_blocks_per_sm(const void *kernel, int threads, size_t dyn_smem, int *blocks);
+
+#define SF_RET_IF(x)                                                           \
+  do {                                                                         \
+    int r_ = (x);                                                              \
+    if (r_ != SF_OK) return r_;                                                \
+  } while (0)
 
 // sf_vector.cu
 int launch_convert(long long n, int from, const void *x, int to, void *y, cudaStream_t st);

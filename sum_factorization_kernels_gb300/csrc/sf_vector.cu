@@ -7,6 +7,8 @@
 #include "sf_internal.h"
 #include "sf_launch.h"
 
+#include <algorithm>
+
 namespace sf {
 
 namespace {
@@ -78,6 +80,32 @@ __global__ void dot_final_kernel(const double *__restrict__ partial, int np, dou
 }
 
 } // namespace
+
+int resident_blocks_per_sm(const void *kernel, int threads, size_t dyn_smem, int *blocks)
+{
+  cudaFuncAttributes fa;
+  SF_CUDA_TRY(cudaFuncGetAttributes(&fa, kernel));
+  int dev = 0, max_thr = 0, max_smem = 0, regs = 0, max_blk = 0, reserved = 0;
+  SF_CUDA_TRY(cudaGetDevice(&dev));
+  SF_CUDA_TRY(cudaDeviceGetAttribute(&max_thr, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
+  SF_CUDA_TRY(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  SF_CUDA_TRY(cudaDeviceGetAttribute(&regs, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
+  SF_CUDA_TRY(cudaDeviceGetAttribute(&max_blk, cudaDevAttrMaxBlocksPerMultiprocessor, dev));
+  SF_CUDA_TRY(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
+  int b = std::min(max_thr / threads, max_blk);
+  // registers are allocated per warp in units of 256
+  const int warps = (threads + 31) / 32;
+  const int regs_per_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
+  if (regs_per_warp > 0) b = std::min(b, regs / (regs_per_warp * warps));
+  const size_t per_block = dyn_smem + fa.sharedSizeBytes + (size_t)reserved;
+  if (per_block > 0) b = std::min<long long>(b, (long long)(max_smem / per_block));
+  *blocks = b;
+  if (b < 1) {
+    set_error("kernel does not fit on an SM");
+    return SF_ERR_UNSUPPORTED;
+  }
+  return SF_OK;
+}
 
 int launch_convert(long long n, int from, const void *x, int to, void *y, cudaStream_t st)
 {

@@ -122,3 +122,73 @@ def test_symmetry_and_boundary_rows_large():
     r = torch.empty_like(x)
     op2.vmult(one, r)
     assert float(r.abs().max()) < 1e-12
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+@pytest.mark.parametrize("case", ["deformed", "kappa", "affine", "neumann_odd"])
+def test_fp32_kernels_agree(p, case):
+    """the FP32 plane-ownership kernel (degrees 1..4) against the generic
+    line-ownership kernel on meshes with odd and unit cell counts"""
+    torch = torch_cuda()
+    sf = _sf()
+    nc = {"deformed": (7, 6, 5), "kappa": (5, 4, 6), "affine": (6, 5, 3), "neumann_odd": (1, 3, 5)}[case]
+    op = sf.Operator(sf.OP_LAPLACE, degree=p, n_cells=nc, length=(1.0, 0.9, 1.1),
+                     deform=0.0 if case == "affine" else 0.05, dirichlet=0 if case == "neumann_odd" else 1)
+    rng = np.random.default_rng(p)
+    if case == "kappa":
+        op.set_coefficient(to_dev(torch, np.exp(0.5 * rng.standard_normal(op.n_cells * (p + 1) ** 3)),
+                                  torch.float64))
+    x = to_dev(torch, rng.uniform(-1, 1, op.n_dofs), torch.float32)
+    y_plane, y_gen, y_pair = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
+    op.set_kernel_variant(sf.KERNEL_PLANE)
+    op.vmult(x, y_plane)
+    op.set_kernel_variant(sf.KERNEL_GENERIC)
+    op.vmult(x, y_gen)
+    op.set_kernel_variant(sf.KERNEL_PAIR)
+    op.vmult(x, y_pair)
+    torch.cuda.synchronize()
+    assert op.device_status() == 0
+    assert rel(to_np(y_plane), to_np(y_gen)) < 2e-6
+    assert rel(to_np(y_pair), to_np(y_gen)) < 2e-6
+
+
+def test_fp32_plane_kernel_full_size_vs_fp64():
+    """64^3 deformed p=4: FP32 apply (plane kernel) against the FP64 apply,
+    twice in a row (geometry staging and colour ordering are stateless)"""
+    torch = torch_cuda()
+    sf = _sf()
+    op = sf.Operator(sf.OP_LAPLACE, degree=4, n_cells=(64, 64, 64), deform=0.05)
+    g = torch.Generator(device="cuda:0").manual_seed(5)
+    x64 = torch.rand(op.n_dofs, dtype=torch.float64, device="cuda:0", generator=g) * 2 - 1
+    y64 = torch.empty_like(x64)
+    op.vmult(x64, y64)
+    x32 = x64.float()
+    for variant in (sf.KERNEL_AUTO, sf.KERNEL_GENERIC, sf.KERNEL_PLANE, sf.KERNEL_PAIR):
+        op.set_kernel_variant(variant)
+        for _ in range(2):
+            y32 = torch.full_like(x32, float("nan"))
+            op.vmult(x32, y32)
+            assert float((y32.double() - y64).norm() / y64.norm()) < 3e-7
+    assert op.device_status() == 0
+
+
+@pytest.mark.parametrize("p", [5, 6, 7, 8])
+def test_fp32_pair_kernel_matches_generic_high_degree(p):
+    """paired FP32x2 kernel vs the line kernel for degrees 5..8 (odd cell
+    counts so that colours end with an unpaired cell), with kappa"""
+    torch = torch_cuda()
+    sf = _sf()
+    op = sf.Operator(sf.OP_LAPLACE, degree=p, n_cells=(5, 3, 3), deform=0.05)
+    rng = np.random.default_rng(p)
+    x = to_dev(torch, rng.uniform(-1, 1, op.n_dofs), torch.float32)
+    for kappa in (False, True):
+        if kappa:
+            op.set_coefficient(to_dev(torch, np.exp(0.5 * rng.standard_normal(op.n_cells * (p + 1) ** 3)),
+                                      torch.float64))
+        y_gen, y_pair = torch.empty_like(x), torch.empty_like(x)
+        op.set_kernel_variant(sf.KERNEL_GENERIC)
+        op.vmult(x, y_gen)
+        op.set_kernel_variant(sf.KERNEL_PAIR)
+        op.vmult(x, y_pair)
+        assert rel(to_np(y_pair), to_np(y_gen)) < 2e-6
+    assert op.device_status() == 0
