@@ -421,12 +421,18 @@ def run_ours(args):
             t64 = time_apply(opq, xq64, yq64, reps64, 2, stream)
             t32 = time_apply(opq, xq32, yq32, max(3, args.steps), 2, stream)
             err = float((yq32.double() - yq64).norm() / yq64.norm())
+            variants_q = {}
+            for name, var in (("line", sfgpu.KERNEL_GENERIC), ("pair_fp32x2", sfgpu.KERNEL_PAIR)):
+                opq.set_kernel_variant(var)
+                tv = time_apply(opq, xq32, yq32, max(3, args.steps // 2), 2, stream)
+                variants_q[name] = round(Nq / tv / 1e9, 3)
+            opq.set_kernel_variant(sfgpu.KERNEL_AUTO)
             b32 = algorithmic_bytes(q, Nq, opq.n_cells, 4)
             b64 = algorithmic_bytes(q, Nq, opq.n_cells, 8)
             ent = {"degree": q, "n_dofs": Nq,
                    "fp32_gdofs": round(Nq / t32 / 1e9, 3), "fp32_hbm_frac": round(b32 / t32 / 1e9 / peak, 4),
                    "fp64_gdofs": round(Nq / t64 / 1e9, 3), "fp64_hbm_frac": round(b64 / t64 / 1e9 / peak, 4),
-                   "fp32_rel_err_vs_fp64": float("%.3g" % err)}
+                   "fp32_rel_err_vs_fp64": float("%.3g" % err), "fp32_variants_gdofs": variants_q}
             sweep.append(ent)
             if q == p:
                 fp64_value = ent["fp64_gdofs"]

@@ -164,6 +164,14 @@ int sf_create(const sf_desc *desc, sf_op **out)
     delete op;
     return fail(SF_ERR_INVALID, "problem too large");
   }
+  // the Laplacian kernels address the nodes of a cell by 32-bit offsets
+  // within the degree + 1 node planes that the cell spans
+  if (d.kind == SF_OP_LAPLACE &&
+      ((long long)d.degree * d.n_cells[0] + 1) * ((long long)d.degree * d.n_cells[1] + 1) * (d.degree + 1) >=
+          (1LL << 31)) {
+    delete op;
+    return fail(SF_ERR_INVALID, "node plane too large: (p nx + 1)(p ny + 1)(p + 1) must stay below 2^31");
+  }
   {
     int r = op->dev_err.alloc(sizeof(int));
     if (r == SF_OK && cudaMemset(op->dev_err.ptr, 0, sizeof(int)) != cudaSuccess) r = SF_ERR_CUDA;

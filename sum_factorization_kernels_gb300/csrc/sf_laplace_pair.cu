@@ -9,8 +9,9 @@
 // shared-memory slab holds float2 pairs (64-bit accesses), and the geometry
 // is stored pair-interleaved ([pair][component][point][2], colour-major) so
 // one TMA bulk copy brings both cells' tensors.  Lanes beyond n^2 work on
-// a spare line of the slab and skip the global stores, so the sweeps need no
+// line 0 of the slab with their stores predicated off, so the sweeps need no
 // divergent branches.  Summation, colours and PDL as in the other kernels.
+#include "sf_cont_column.cuh"
 #include "sf_device.cuh"
 #include "sf_internal.h"
 #include "sf_launch.h"
@@ -27,7 +28,7 @@ struct PairCfg {
   static constexpr int P1 = N == 8 ? 9 : N;
   static constexpr int P2 = N == 7 ? 52 : N == 8 ? 72 : N * N;
   static constexpr int SLAB = P2 * N;          // float2 entries
-  static constexpr int SLAB_ALLOC = SLAB;
+  static constexpr int NSLAB = 3;              // slabs per group
   static constexpr int GROUPS = G == 1 ? 4 : (G == 2 ? 3 : 2);
 };
 
@@ -118,7 +119,7 @@ struct PairArgs {
   long long gstride;               // floats per pair block
   long long pair_base;             // first pair of this colour in the geometry
   int nc[3];
-  long long Nx, Ny, Nz;
+  int Nx, plane;                   // nodes per x line, per z plane
   float aff[3];
   int dirichlet;
   int color, cx, cy, cz, mx, my;
@@ -127,50 +128,23 @@ struct PairArgs {
   int step_i, step_j, step_k;      // walk stride (2 x groups) in (mi, mj, mk)
 };
 
-// per-cell information a thread needs for the gather and the scatter
-struct CellIdx {
-  long long gb;    // global index of local node (a, b, 0)
-  bool valid, side, zlo, zhi, zl, zh;
-  int mxy;
-};
-
-template <int N>
-__device__ __forceinline__ CellIdx cell_index(const PairArgs<N> &A, int mi, int mj, int mk, int a, int b, bool valid)
-{
-  constexpr int P = N - 1;
-  CellIdx c;
-  const int ci = 2 * mi + A.cx, cj = 2 * mj + A.cy, ck = 2 * mk + A.cz;
-  const bool dir = A.dirichlet != 0;
-  const long long X = (long long)ci * P + a, Y = (long long)cj * P + b, Z0 = (long long)ck * P;
-  c.gb = (Z0 * A.Ny + Y) * A.Nx + X;
-  c.valid = valid;
-  c.side = dir && (X == 0 || X == A.Nx - 1 || Y == 0 || Y == A.Ny - 1);
-  c.zlo = dir && ck == 0;
-  c.zhi = dir && ck == A.nc[2] - 1;
-  c.zl = ck > 0;
-  c.zh = ck < A.nc[2] - 1;
-  c.mxy = ((a == 0 && ci > 0) || (a == P && ci < A.nc[0] - 1) ? 1 : 0) |
-          ((b == 0 && cj > 0) || (b == P && cj < A.nc[1] - 1) ? 2 : 0);
-  return c;
-}
-
 template <int N, bool DEFORMED, bool KAPPA>
 __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
     pair_vmult_kernel(const __grid_constant__ PairArgs<N> A)
 {
   using Cfg = PairCfg<N>;
-  constexpr int P = N - 1, N2 = N * N, N3 = N * N * N;
+  constexpr int N2 = N * N, N3 = N * N * N;
   constexpr int G = Cfg::G, GROUPS = Cfg::GROUPS, P1 = Cfg::P1, P2 = Cfg::P2;
   constexpr int GT = 32 * G;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw);
   const int grp = threadIdx.x / GT, t = threadIdx.x % GT;
   const long long geo_f = DEFORMED ? A.gstride : 0;
-  const long long region = (geo_f * 4 + 4LL * Cfg::SLAB_ALLOC * 8 + 127) / 128 * 128;
+  const long long region = (geo_f * 4 + 8LL * Cfg::NSLAB * Cfg::SLAB + 127) / 128 * 128;
   unsigned char *gbase = smem_raw + 128 + grp * region;
   float *geo_s = reinterpret_cast<float *>(gbase);
   float2 *B0 = reinterpret_cast<float2 *>(gbase + geo_f * 4);
-  float2 *B1 = B0 + Cfg::SLAB_ALLOC, *B2 = B1 + Cfg::SLAB_ALLOC, *B3 = B2 + Cfg::SLAB_ALLOC;
+  float2 *B1 = B0 + Cfg::SLAB, *B2 = B1 + Cfg::SLAB;
   uint64_t *bar = bars + grp;
 
   // idle lanes (t >= n^2) run line 0 with their shared stores predicated
@@ -181,6 +155,8 @@ __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
   const int zc = a + P1 * b;
   const int xl = P1 * a + P2 * b;
   const int yl = a + P2 * b;
+  const int plane = A.plane;
+  const int toff = b * A.Nx + a;
 
   const long long npairs = (A.count + 1) / 2;
   const long long ng = (long long)gridDim.x * GROUPS;
@@ -211,7 +187,6 @@ __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
   pdl_trigger();
   uint32_t parity = 0;
   bool y_ready = false;
-  const float2 zero2 = make_float2(0.f, 0.f);
 
   for (long long pr = gid; pr < npairs; pr += ng) {
     // the two cells: ordinals 2 pr and 2 pr + 1
@@ -224,26 +199,32 @@ __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
       }
     }
     const bool hasB = 2 * pr + 1 < A.count;
-    const CellIdx CA = cell_index<N>(A, mi, mj, mk, a, b, active);
-    const CellIdx CB = cell_index<N>(A, bi, bj, bk, a, b, active && hasB);
-    const long long plane = A.Nx * A.Ny;
-    float2 v[N], g[N];
+    const int ai = 2 * mi + A.cx, aj = 2 * mj + A.cy, ak = 2 * mk + A.cz;
+    const int ei = 2 * bi + A.cx, ej = 2 * bj + A.cy, ek = 2 * bk + A.cz;
+    const bool dir = A.dirichlet != 0;
+    const ColumnMask mA = column_mask<N>(a, b, ai, aj, ak, A.nc, A.color, dir, active);
+    const ColumnMask mB = column_mask<N>(a, b, ei, ej, ek, A.nc, A.color, dir, active && hasB);
+    const long long nbA = cell_node_base<N>(ai, aj, ak, A.Nx, plane) + toff;
+    const long long nbB = cell_node_base<N>(ei, ej, ek, A.Nx, plane) + toff;
+    float2 v[N], g[N], gz[N];
+    {
+      float va[N], vb[N];
+      gather_column<N, float>(A.x + nbA, plane, mA.keep, va);
+      gather_column<N, float>(A.x + nbB, plane, mB.keep, vb);
 #pragma unroll
-    for (int c = 0; c < N; ++c) {
-      const bool ba = CA.side || (c == 0 && CA.zlo) || (c == P && CA.zhi);
-      const bool bb = CB.side || (c == 0 && CB.zlo) || (c == P && CB.zhi);
-      v[c].x = (CA.valid && !ba) ? __ldg(A.x + CA.gb + c * plane) : 0.f;
-      v[c].y = (CB.valid && !bb) ? __ldg(A.x + CB.gb + c * plane) : 0.f;
+      for (int c = 0; c < N; ++c) v[c] = make_float2(va[c], vb[c]);
     }
     eo2<N, 1>(A.S, v, v);
 #pragma unroll
-    for (int c = 0; c < N; ++c) if (active) B0[zc + P2 * c] = v[c];
+    for (int c = 0; c < N; ++c)
+      if (active) B0[zc + P2 * c] = v[c];
     cell_group_sync<G>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B0[xl + m];
     eo2<N, 1>(A.S, v, v);
 #pragma unroll
-    for (int m = 0; m < N; ++m) if (active) B0[xl + m] = v[m];
+    for (int m = 0; m < N; ++m)
+      if (active) B0[xl + m] = v[m];
     cell_group_sync<G>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B0[yl + P1 * m];
@@ -255,16 +236,16 @@ __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
       if (active) B2[yl + P1 * m] = g[m];
     }
     cell_group_sync<G>(grp);
+    // D_x into B0; D_z stays in registers (same thread, same column)
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[xl + m];
     eo2<N, -1>(A.D, v, g);
 #pragma unroll
-    for (int m = 0; m < N; ++m) if (active) B0[xl + m] = g[m];
+    for (int m = 0; m < N; ++m)
+      if (active) B0[xl + m] = g[m];
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[zc + P2 * m];
-    eo2<N, -1>(A.D, v, g);
-#pragma unroll
-    for (int m = 0; m < N; ++m) if (active) B3[zc + P2 * m] = g[m];
+    eo2<N, -1>(A.D, v, gz);
     cell_group_sync<G>(grp);
     // ---- quadrature points of column (a,b), both cells ----
     float2 tz[N];
@@ -278,15 +259,15 @@ __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
 #pragma unroll
       for (int c = 0; c < N; ++c) {
         const int s = zc + P2 * c;
-        const float2 gx = B0[s], gy = B2[s], gz = B3[s];
+        const float2 gx = B0[s], gy = B2[s];
         float2 tx, ty, tzc;
         if (DEFORMED) {
           const float2 *Gq = reinterpret_cast<const float2 *>(geo_s) + c * N2 + q0;
           const float2 g0 = Gq[0], g1 = Gq[N3], g2 = Gq[2 * N3], g3 = Gq[3 * N3], g4 = Gq[4 * N3],
                        g5 = Gq[5 * N3];
-          tx = f2fma(gz, g4, f2fma(gy, g3, f2mul(gx, g0)));
-          ty = f2fma(gz, g5, f2fma(gy, g1, f2mul(gx, g3)));
-          tzc = f2fma(gz, g2, f2fma(gy, g5, f2mul(gx, g4)));
+          tx = f2fma(gz[c], g4, f2fma(gy, g3, f2mul(gx, g0)));
+          ty = f2fma(gz[c], g5, f2fma(gy, g1, f2mul(gx, g3)));
+          tzc = f2fma(gz[c], g2, f2fma(gy, g5, f2mul(gx, g4)));
           if (KAPPA) {
             const float2 kq = Gq[6 * N3];
             tx = f2mul(tx, kq);
@@ -297,7 +278,7 @@ __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
           const float wq = wab * A.w[c];
           tx = f2mul(gx, make_float2(A.aff[0] * wq, A.aff[0] * wq));
           ty = f2mul(gy, make_float2(A.aff[1] * wq, A.aff[1] * wq));
-          tzc = f2mul(gz, make_float2(A.aff[2] * wq, A.aff[2] * wq));
+          tzc = f2mul(gz[c], make_float2(A.aff[2] * wq, A.aff[2] * wq));
         }
         if (active) B0[s] = tx;
         if (active) B2[s] = ty;
@@ -306,7 +287,8 @@ __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
     }
     eo2<N, -1>(A.DT, tz, g);
 #pragma unroll
-    for (int c = 0; c < N; ++c) if (active) B1[zc + P2 * c] = g[c];
+    for (int c = 0; c < N; ++c)
+      if (active) B1[zc + P2 * c] = g[c];
     if (DEFORMED) fence_proxy_async_smem();
     cell_group_sync<G>(grp);
     if (DEFORMED && t == 0 && pr + ng < npairs) issue(pr + ng);
@@ -314,7 +296,10 @@ __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
     for (int m = 0; m < N; ++m) v[m] = B0[xl + m];
     eo2<N, -1>(A.DT, v, g);
 #pragma unroll
-    for (int m = 0; m < N; ++m) if (active) B1[xl + m] = f2add(B1[xl + m], g[m]);
+    for (int m = 0; m < N; ++m) {
+      const float2 s = f2add(B1[xl + m], g[m]);
+      if (active) B1[xl + m] = s;
+    }
     cell_group_sync<G>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B2[yl + P1 * m];
@@ -323,13 +308,15 @@ __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
     for (int m = 0; m < N; ++m) g[m] = f2add(g[m], B1[yl + P1 * m]);
     eo2<N, 1>(A.ST, g, v);
 #pragma unroll
-    for (int m = 0; m < N; ++m) if (active) B1[yl + P1 * m] = v[m];
+    for (int m = 0; m < N; ++m)
+      if (active) B1[yl + P1 * m] = v[m];
     cell_group_sync<G>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[xl + m];
     eo2<N, 1>(A.ST, v, v);
 #pragma unroll
-    for (int m = 0; m < N; ++m) if (active) B1[xl + m] = v[m];
+    for (int m = 0; m < N; ++m)
+      if (active) B1[xl + m] = v[m];
     cell_group_sync<G>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[zc + P2 * m];
@@ -339,23 +326,16 @@ __global__ void __launch_bounds__(32 * PairCfg<N>::G * PairCfg<N>::GROUPS)
       pdl_wait();
       y_ready = true;
     }
+    {
+      float va[N], vb[N];
 #pragma unroll
-    for (int cell2 = 0; cell2 < 2; ++cell2) {
-      const CellIdx &C = cell2 ? CB : CA;
-      if (C.valid) {
-#pragma unroll
-        for (int c = 0; c < N; ++c) {
-          const bool bnd = C.side || (c == 0 && C.zlo) || (c == P && C.zhi);
-          const int mz = ((c == 0 && C.zl) || (c == P && C.zh)) ? 4 : 0;
-          const float val = cell2 ? v[c].y : v[c].x;
-          float *dst = A.y + C.gb + c * plane;
-          if (bnd) *dst = __ldg(A.x + C.gb + c * plane);
-          else if (A.color & (C.mxy | mz)) *dst += val;
-          else *dst = val;
-        }
+      for (int c = 0; c < N; ++c) {
+        va[c] = v[c].x;
+        vb[c] = v[c].y;
       }
+      if (active) scatter_column<N, float>(A.y + nbA, A.x + nbA, plane, mA, va);
+      if (active && hasB) scatter_column<N, float>(A.y + nbB, A.x + nbB, plane, mB, vb);
     }
-    (void)zero2;
     // advance the pair walk by 2 * ng ordinals
     mi += A.step_i;
     int carry = 0;
@@ -404,9 +384,8 @@ int pair_vmult_impl(const sf_op *op, const float *x, float *y, cudaStream_t st)
   A.DT = eo2_of<N>(s.D, true);
   for (int i = 0; i < N; ++i) A.w[i] = float(s.wq[i]);
   for (int d = 0; d < 3; ++d) A.nc[d] = op->desc.n_cells[d];
-  A.Nx = (long long)(N - 1) * A.nc[0] + 1;
-  A.Ny = (long long)(N - 1) * A.nc[1] + 1;
-  A.Nz = (long long)(N - 1) * A.nc[2] + 1;
+  A.Nx = (N - 1) * A.nc[0] + 1;
+  A.plane = A.Nx * ((N - 1) * A.nc[1] + 1);
   const double jxw = op->h[0] * op->h[1] * op->h[2];
   for (int d = 0; d < 3; ++d) A.aff[d] = float(jxw / (op->h[d] * op->h[d]));
   A.dirichlet = op->desc.dirichlet;
@@ -428,7 +407,7 @@ int pair_vmult_impl(const sf_op *op, const float *x, float *y, cudaStream_t st)
       deformed ? (kap ? pair_vmult_kernel<N, true, true> : pair_vmult_kernel<N, true, false>)
                : pair_vmult_kernel<N, false, false>;
   const long long geo_f = deformed ? A.gstride : 0;
-  const long long region = (geo_f * 4 + 4LL * Cfg::SLAB_ALLOC * 8 + 127) / 128 * 128;
+  const long long region = (geo_f * 4 + 8LL * Cfg::NSLAB * Cfg::SLAB + 127) / 128 * 128;
   const size_t smem = 128 + size_t(Cfg::GROUPS) * region;
   const int threads = 32 * Cfg::G * Cfg::GROUPS;
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
