@@ -370,9 +370,7 @@ def run_ours(args):
 
     # ---- the other kernel variant at the headline degree (plane ownership) ----
     variants = {"line_gdofs": round(value / world, 3)}
-    for name, var in (("pair_fp32x2_gdofs", sfgpu.KERNEL_PAIR), ("plane_gdofs", sfgpu.KERNEL_PLANE)):
-        if var == sfgpu.KERNEL_PLANE and p > 4:
-            continue
+    for name, var in (("pair_fp32x2_gdofs", sfgpu.KERNEL_PAIR),):
         op.set_kernel_variant(var)
         tv = time_apply(op, x32, y32, max(10, args.steps // 2), 3, stream)
         variants[name] = round(N / tv / 1e9, 3)

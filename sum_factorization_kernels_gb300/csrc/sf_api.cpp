@@ -76,16 +76,12 @@ int check_ptr(const void *p, int prec, const char *name)
 // derived FP32 copies of the FP64 geometry (and coefficient): the natural
 // layout for the generic kernels, the colour-major plane layout for the
 // FP32 degree 1..4 kernel
-// The plane and pair kernels read their own FP32 geometry layouts; these
-// copies exist only while the kernel variant that reads them is selected.
+// The pair kernel reads its own FP32 geometry layout; that copy exists only
+// while the pair variant is selected.
 int derive_variant_geometry(sf_op *op)
 {
   const bool fp32 = (op->desc.precisions & 2) && op->deformed && op->desc.kind == SF_OP_LAPLACE;
   const double *k64 = op->has_kappa ? (const double *)op->kap64.ptr : nullptr;
-  if (fp32 && op->kernel_variant == SF_KERNEL_PLANE && op->n <= 5)
-    SF_RET(repack_plane_geometry(op, (const double *)op->geo64.ptr, op->geo_stride, k64, 0));
-  else
-    op->geoP.release();
   if (fp32 && op->kernel_variant == SF_KERNEL_PAIR)
     SF_RET(repack_pair_geometry(op, (const double *)op->geo64.ptr, op->geo_stride, k64, 0));
   else

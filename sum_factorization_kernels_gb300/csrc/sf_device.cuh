@@ -97,6 +97,25 @@ __device__ __forceinline__ void cell_group_sync(int grp)
   }
 }
 
+// Division of 32-bit unsigned integers by a runtime constant d >= 1 with one
+// 64-bit high multiply: q = floor(m n / 2^64) with m = floor((2^64 - 1) / d)
+// + 1 is exact for every n < 2^32 (Lemire, Kaser and Kurz, "Faster
+// remainder by direct computation", Software: Practice and Experience
+// 49(6), 2019).  d = 1 (m would be 2^64) is flagged by m = 0.
+struct FastDiv {
+  unsigned long long m;
+};
+
+__host__ __device__ inline FastDiv make_fast_div(unsigned d)
+{
+  return FastDiv{d == 1u ? 0ull : ~0ull / d + 1ull};
+}
+
+__device__ __forceinline__ unsigned fast_div(unsigned n, FastDiv f)
+{
+  return f.m == 0ull ? n : (unsigned)__umul64hi(f.m, (unsigned long long)n);
+}
+
 // cells per thread block for n^2 threads per cell (about 128-256 threads)
 template <int N>
 struct CellsPerBlock {

@@ -35,8 +35,10 @@ struct DGArgs {
   EOMat<N, T> S, ST, D, DT, P;   // P = Sinv (Gauss values -> GLL nodes)
   T fv0[N], fv1[N], fd0[N], fd1[N];
   T w[N];
+  T iw[N];        // 1 / w
   T ij[3];        // inverse cell sizes
   T jxw;          // cell volume
+  T ijxw;         // 1 / jxw
   T jface[3];     // face area elements jxw * ij_d
   T tau[3];       // SIPG penalty per direction
   T cdir[3];      // SIPG: ij_d^2 jxw ; advection: a_d ij_d jxw
@@ -49,6 +51,7 @@ struct DGArgs {
   T *__restrict__ ct;            // Chebyshev: t
   T c_np, c_tm;
   int nc[3];
+  FastDiv div_nx, div_ny;        // division by nc[0], nc[1]
   long long n_cells, n_dofs;
 };
 
@@ -168,15 +171,15 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   T *F = smem + 3 * CPB * N3 + cs * (12 * N2);
 
   // ---- coalesced load of the block's cells ----
-  const long long ncell_blk = min((long long)CPB, A.n_cells - cell0);
-  const long long nval = ncell_blk * N3;
+  const int nval = (int)min((long long)CPB, A.n_cells - cell0) * N3;
   const T *src = x + cell0 * N3;
-  for (long long e = tid; e < nval; e += blockDim.x) Bblk[e] = __ldg(src + e);
+  for (int e = tid; e < nval; e += CPB * N2) Bblk[e] = __ldg(src + e);
   // ---- neighbour face layers ----
   if (valid) {
-    const unsigned uc = (unsigned)cell, unx = (unsigned)A.nc[0], uny = (unsigned)A.nc[1];
-    const unsigned q = uc / unx;
-    const int ix = int(uc - q * unx), iz = int(q / uny), iy = int(q - unsigned(iz) * uny);
+    const unsigned uc = (unsigned)cell;
+    const unsigned q = fast_div(uc, A.div_nx);
+    const unsigned iz = fast_div(q, A.div_ny);
+    const int ix = int(uc - q * (unsigned)A.nc[0]), iy = int(q - iz * (unsigned)A.nc[1]);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       // face-local index t: x faces (b,c) = (t%N, t/N), y faces (a,c), z faces (a,b)
@@ -266,9 +269,9 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
 #pragma unroll
   for (int m = 0; m < N; ++m) v[m] = rz[m] + B0[t + N2 * m] + B2[t + N2 * m];
   if (INVMASS) {
-    const T wab = A.w[a] * A.w[b];
+    const T iwab = A.ijxw * A.iw[a] * A.iw[b];
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = v[m] / (A.jxw * wab * A.w[m]);
+    for (int m = 0; m < N; ++m) v[m] *= iwab * A.iw[m];
     eo_apply<N, 1>(A.P, v, v);
   } else {
     eo_apply<N, 1>(A.ST, v, v);
@@ -295,14 +298,14 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   T *dst = A.y + roff + cell0 * N3;
   if (CHEB) {
     const long long o = cell0 * N3;
-    for (long long e = tid; e < nval; e += blockDim.x) {
+    for (int e = tid; e < nval; e += CPB * N2) {
       const T res = Rblk[e] - A.cb[o + e];
       const T tn = A.c_tm * A.ct[o + e] + A.c_np * A.cdinv[o + e] * res;
       A.ct[o + e] = tn;
       dst[e] = __ldg(x + o + e) - tn;
     }
   } else {
-    for (long long e = tid; e < nval; e += blockDim.x) dst[e] = Rblk[e];
+    for (int e = tid; e < nval; e += CPB * N2) dst[e] = Rblk[e];
   }
 }
 
@@ -345,8 +348,9 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   for (int m = 0; m < N; ++m) v[m] = B[a + N * m + N2 * b];
   eo_apply<N, 1>(A.ST, v, v);
   // now at Gauss point (a, m, c=b): divide by JxW w
+  const T iwab = A.ijxw * A.iw[a] * A.iw[b];
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = v[m] / (A.jxw * A.w[a] * A.w[m] * A.w[b]);
+  for (int m = 0; m < N; ++m) v[m] *= iwab * A.iw[m];
   eo_apply<N, 1>(A.P, v, v);
 #pragma unroll
   for (int m = 0; m < N; ++m) B[a + N * m + N2 * b] = v[m];
@@ -393,9 +397,11 @@ DGArgs<N, T> make_dg_args(const sf_op *op)
     A.fd0[i] = T(s.fd[0][i]);
     A.fd1[i] = T(s.fd[1][i]);
     A.w[i] = T(s.wq[i]);
+    A.iw[i] = T(1.0 / s.wq[i]);
   }
   const double jxw = op->h[0] * op->h[1] * op->h[2];
   A.jxw = T(jxw);
+  A.ijxw = T(1.0 / jxw);
   for (int d = 0; d < 3; ++d) {
     const double ij = 1.0 / op->h[d];
     A.ij[d] = T(ij);
@@ -405,6 +411,8 @@ DGArgs<N, T> make_dg_args(const sf_op *op)
     A.cdir[d] = op->desc.kind == SF_OP_DG_SIPG ? T(ij * ij * jxw) : T(op->desc.velocity[d] * ij * jxw);
     A.nc[d] = op->desc.n_cells[d];
   }
+  A.div_nx = make_fast_div((unsigned)A.nc[0]);
+  A.div_ny = make_fast_div((unsigned)A.nc[1]);
   A.hd0 = T(s.hermite_d0);
   A.n_cells = op->n_cells;
   A.n_dofs = op->n_dofs;

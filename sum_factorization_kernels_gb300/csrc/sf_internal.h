@@ -61,8 +61,6 @@ struct sf_op {
   sf::DevBuf kap64, kap32;      // [cell][n^3] coefficient
   bool has_kappa = false;
   sf::DevBuf scratch;           // operator-private scratch (transpose, M^-1)
-  sf::DevBuf geoP;              // FP32 geometry for the plane kernel (colour-major)
-  long long geoP_stride = 0;
   sf::DevBuf geoPair;           // FP32 geometry for the pair kernel (pair-interleaved)
   long long geoPair_stride = 0;
   sf::DevBuf dev_err;           // device error flags (bounded waits)

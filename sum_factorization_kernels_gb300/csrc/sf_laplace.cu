@@ -1,11 +1,10 @@
 // sf_laplace.cu -- continuous FE Laplacian -div(kappa grad u) on hexahedral
 // meshes of degree 1..8: operator apply, geometry, kappa-gradient, diagonal.
 //
-// The operator apply itself lives in sf_laplace_pair.cu (FP32, default),
-// sf_laplace_line.cu (FP64; FP32 on request) and sf_laplace_plane.cu (FP32,
-// degrees 1..4, on request); this file holds the
-// setup (geometry), diagonal and kappa-gradient kernels, which use the same
-// cell pipeline with one block of CPB cells and block barriers.
+// The operator apply itself lives in sf_laplace_line.cu (default, both
+// precisions) and sf_laplace_pair.cu (FP32x2 variant, on request); this file
+// holds the setup (geometry), diagonal and kappa-gradient kernels, which use
+// a cell pipeline with one block of CPB cells and block barriers.
 //
 // Per cell the operator is y_e = S^T (sum_d D_d^T t_d), t = kappa_q G_q D S x_e
 // (S: basis -> Gauss values, D: collocation derivative, G: merged
@@ -546,7 +545,6 @@ int cont_kgrad_n(const sf_op *op, int prec, const void *u, const void *l, void *
 int launch_cont_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
 {
   if (pair_path(op, prec)) return launch_cont_vmult_pair(op, (const float *)x, (float *)y, st);
-  if (plane_path(op, prec)) return launch_cont_vmult_plane(op, (const float *)x, (float *)y, st);
   return launch_cont_vmult_line(op, prec, x, y, st);
 }
 

@@ -23,12 +23,6 @@ int launch_cont_vmult_pair(const sf_op *op, const float *x, float *y, cudaStream
 int repack_pair_geometry(sf_op *op, const double *G64, long long s64, const double *kap64,
                          cudaStream_t st);
 
-// sf_laplace_plane.cu (FP32, degrees 1..4)
-bool plane_path(const sf_op *op, int prec);
-int launch_cont_vmult_plane(const sf_op *op, const float *x, float *y, cudaStream_t st);
-int repack_plane_geometry(sf_op *op, const double *G64, long long s64, const double *kap64,
-                          cudaStream_t st);
-
 // sf_dg.cu
 int launch_dg_vmult(const sf_op *op, int prec, int nrhs, bool transpose, const void *x, void *y,
                     const void *cheb_b, const void *cheb_dinv, void *cheb_t, double c_np,

@@ -124,11 +124,12 @@ def test_symmetry_and_boundary_rows_large():
     assert float(r.abs().max()) < 1e-12
 
 
-@pytest.mark.parametrize("p", [1, 2, 3, 4])
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 8])
 @pytest.mark.parametrize("case", ["deformed", "kappa", "affine", "neumann_odd"])
-def test_fp32_kernels_agree(p, case):
-    """the FP32 plane-ownership kernel (degrees 1..4) against the generic
-    line-ownership kernel on meshes with odd and unit cell counts"""
+def test_fp32_kernels_vs_fp64(p, case):
+    """the packed FP32 line kernel (several cells per warp group, so odd and
+    unit cell counts leave partly filled groups) and the FP32x2 pair kernel
+    against the FP64 apply"""
     torch = torch_cuda()
     sf = _sf()
     nc = {"deformed": (7, 6, 5), "kappa": (5, 4, 6), "affine": (6, 5, 3), "neumann_odd": (1, 3, 5)}[case]
@@ -138,23 +139,22 @@ def test_fp32_kernels_agree(p, case):
     if case == "kappa":
         op.set_coefficient(to_dev(torch, np.exp(0.5 * rng.standard_normal(op.n_cells * (p + 1) ** 3)),
                                   torch.float64))
-    x = to_dev(torch, rng.uniform(-1, 1, op.n_dofs), torch.float32)
-    y_plane, y_gen, y_pair = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
-    op.set_kernel_variant(sf.KERNEL_PLANE)
-    op.vmult(x, y_plane)
-    op.set_kernel_variant(sf.KERNEL_GENERIC)
-    op.vmult(x, y_gen)
-    op.set_kernel_variant(sf.KERNEL_PAIR)
-    op.vmult(x, y_pair)
-    torch.cuda.synchronize()
+    x64 = to_dev(torch, rng.uniform(-1, 1, op.n_dofs), torch.float64)
+    y64 = torch.empty_like(x64)
+    op.vmult(x64, y64)
+    x = x64.float()
+    for variant in (sf.KERNEL_AUTO, sf.KERNEL_PAIR):
+        op.set_kernel_variant(variant)
+        y = torch.full_like(x, float("nan"))
+        op.vmult(x, y)
+        torch.cuda.synchronize()
+        assert rel(to_np(y), to_np(y64)) < FP32_TOL[p], variant
     assert op.device_status() == 0
-    assert rel(to_np(y_plane), to_np(y_gen)) < 2e-6
-    assert rel(to_np(y_pair), to_np(y_gen)) < 2e-6
 
 
-def test_fp32_plane_kernel_full_size_vs_fp64():
-    """64^3 deformed p=4: FP32 apply (plane kernel) against the FP64 apply,
-    twice in a row (geometry staging and colour ordering are stateless)"""
+def test_fp32_full_size_vs_fp64():
+    """64^3 deformed p=4: FP32 applies against the FP64 apply, twice in a row
+    (geometry staging and colour ordering are stateless)"""
     torch = torch_cuda()
     sf = _sf()
     op = sf.Operator(sf.OP_LAPLACE, degree=4, n_cells=(64, 64, 64), deform=0.05)
@@ -163,7 +163,7 @@ def test_fp32_plane_kernel_full_size_vs_fp64():
     y64 = torch.empty_like(x64)
     op.vmult(x64, y64)
     x32 = x64.float()
-    for variant in (sf.KERNEL_AUTO, sf.KERNEL_GENERIC, sf.KERNEL_PLANE, sf.KERNEL_PAIR):
+    for variant in (sf.KERNEL_AUTO, sf.KERNEL_GENERIC, sf.KERNEL_PAIR):
         op.set_kernel_variant(variant)
         for _ in range(2):
             y32 = torch.full_like(x32, float("nan"))

@@ -108,3 +108,17 @@ def test_kappa_gradient_central_differences():
         km[q] -= hstep
         fd = (L(kp) - L(km)) / (2 * hstep)
         assert abs(fd - g[q]) <= 1e-6 * max(abs(fd), 1e-3 * np.abs(g).max()), (q, fd, g[q])
+
+
+def test_fast_division_formula():
+    """the 64-bit multiply-high division used by the DG kernels' cell decode
+    (m = floor((2^64-1)/d) + 1, q = floor(m n / 2^64)) is exact for 32-bit n"""
+    rng = np.random.default_rng(7)
+    ds = [2, 3, 5, 7, 48, 63, 64, 65, 1000, 2 ** 20, 2 ** 20 - 1, 2 ** 31 - 1, 2 ** 32 - 1]
+    ds += [int(v) for v in rng.integers(2, 2 ** 32, 50)]
+    ns = [0, 1, 2 ** 31 - 1, 2 ** 31, 2 ** 32 - 1] + [int(v) for v in rng.integers(0, 2 ** 32, 2000)]
+    for d in ds:
+        m = (2 ** 64 - 1) // d + 1
+        for n in ns + [d - 1, d, d + 1, 2 * d - 1, 2 * d]:
+            n &= 2 ** 32 - 1
+            assert (m * n) >> 64 == n // d
