@@ -29,6 +29,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Laplacian matvec GDoF/s + % HBM peak, FP32 vs FP64 at stated rel. error"
+# DRAM bytes (read + write) of one apply = 8 colour launches of the default
+# workload, measured by ncu with warm caches as in the timed loop
+# (--metrics dram__bytes_read.sum,dram__bytes_write.sum --cache-control none
+#  -k regex:line_vmult -s 24 -c 8 on this script with --steps 5 --warmup 3).
+MEASURED_TRAFFIC = {(4, 64): 1006150400}
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the 8 colour launches "
+                  "of one apply, caches warm (--cache-control none)")
 UNIT = "GDoF/s"
 DEFORM = 0.05
 
@@ -460,7 +467,9 @@ def run_ours(args):
                        "fp64_gdofs_same_degree": fp64_value, "kernel_variants": variants},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "traffic": None, "peak_kind": peak_kind,
+                         "traffic": MEASURED_TRAFFIC.get((p, args.ncells)),
+                         "traffic_source": TRAFFIC_SOURCE if (p, args.ncells) in MEASURED_TRAFFIC else None,
+                         "peak_kind": peak_kind,
                          "kernel": "line_vmult_kernel<%d,float,deformed> (8 colour launches per apply)" % (p + 1),
                          "algorithmic_bytes_per_apply": bytes_apply},
             "cpu_baseline": cpu,

@@ -1,0 +1,72 @@
+"""Time single operator applies through the C ABI (CUDA events, inputs in
+device memory): ``python -m sum_factorization_kernels_gb300.timing KIND ...``.
+
+KIND is ``laplace`` (continuous, deformed mesh), ``sipg`` (DG SIPG) or
+``advect`` (DG upwind advection with inverse mass).  Prints one line with the
+apply rate summed over the right-hand sides and the vector traffic it implies.
+Used to drive profiler captures of one kernel on a small case.
+"""
+from __future__ import annotations
+
+import argparse
+
+import torch
+
+from . import sfgpu as sf
+
+
+def make_operator(kind: str, degree: int, ncells: int):
+    n = (ncells,) * 3
+    if kind == "laplace":
+        return sf.Operator(sf.OP_LAPLACE, degree=degree, n_cells=n, deform=0.05)
+    if kind == "sipg":
+        return sf.Operator(sf.OP_DG_SIPG, degree=degree, n_cells=n)
+    if kind == "advect":
+        return sf.Operator(sf.OP_DG_ADVECT, degree=degree, n_cells=n, velocity=(1.0, 0.5, 0.25), inverse_mass=1)
+    raise ValueError("unknown operator kind %r" % kind)
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("kind", choices=["laplace", "sipg", "advect"])
+    ap.add_argument("--degree", type=int, default=4)
+    ap.add_argument("--ncells", type=int, default=32, help="cells per direction")
+    ap.add_argument("--prec", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--nrhs", type=int, default=1)
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    a = ap.parse_args(argv)
+    op = make_operator(a.kind, a.degree, a.ncells)
+    dt = torch.float32 if a.prec == "fp32" else torch.float64
+    n = op.n_dofs
+    g = torch.Generator(device="cuda").manual_seed(1)
+    x = (torch.rand(a.nrhs * n, device="cuda", dtype=torch.float64, generator=g) * 2 - 1).to(dt)
+    y = torch.empty_like(x)
+
+    def apply():
+        if a.nrhs > 1:
+            op.vmult_batched(x, y, a.nrhs)
+        else:
+            op.vmult(x, y)
+
+    for _ in range(a.warmup):
+        apply()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.reps):
+        apply()
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / a.reps
+    status = op.device_status()
+    print("%s p=%d %d^3 %s nrhs=%d: %.3f GDoF/s (summed over right-hand sides), %.1f GB/s of vector "
+          "traffic, %.1f us per apply, device status %d"
+          % (a.kind, a.degree, a.ncells, a.prec, a.nrhs, a.nrhs * n / t / 1e9,
+             2 * a.nrhs * n * x.element_size() / t / 1e9, t * 1e6, status))
+    if status != 0:
+        raise SystemExit("device status %d" % status)
+
+
+if __name__ == "__main__":
+    main()
