@@ -13,12 +13,13 @@
 // face injection.  Corrections relative to the reference: periodic x
 // neighbour index, transposed values in the last SIPG sweep.
 //
-// GPU mapping: a block holds CPB consecutive cells (n^2 threads each); the
-// block's cell data is one contiguous range of the vector, so it is loaded
-// and stored with coalesced vector accesses; each 1D sweep is line-local in
-// shared memory (see sf_laplace.cu); each thread also owns one point of each
-// face pair of its line, so the face fluxes are computed in the thread that
-// holds the matching line.
+// GPU mapping: a block holds CPB consecutive cells (n^2 threads each); a
+// thread reads and writes one z column of its cell straight from and to the
+// cell-major vector (each warp instruction covers runs of n^2 consecutive
+// entries), the x and y sweeps are line-local in three padded shared-memory
+// slabs per cell; each thread also owns one point of each face pair of its
+// line, so the face fluxes are computed in the thread that holds the
+// matching line.
 #include "sf_device.cuh"
 #include "sf_internal.h"
 #include "sf_launch.h"
@@ -145,12 +146,53 @@ __device__ __forceinline__ void line_residual(const DGArgs<N, T> &A, int d, cons
   }
 }
 
+// Shared-memory layout of the DG kernels: per cell three slabs with index
+// (a, b, c) = a + P1 b + P2 c and a per-cell skew, chosen from a
+// bank-conflict model of the three sweep patterns over the lanes of each
+// warp (a block holds CPB consecutive cells, cell-major lanes).
+struct DGLayout {
+  int P1, P2, SKEW;
+};
+
+constexpr DGLayout dg_layout(int n, int elem)
+{
+  return elem == 4 ? (n == 2   ? DGLayout{2, 5, 6}
+                      : n == 3 ? DGLayout{3, 9, 10}
+                      : n == 4 ? DGLayout{4, 19, 12}
+                      : n == 5 ? DGLayout{5, 25, 2}
+                      : n == 6 ? DGLayout{7, 42, 8}
+                      : n == 7 ? DGLayout{7, 56, 25}
+                      : n == 8 ? DGLayout{9, 72, 0}
+                               : DGLayout{9, 81, 6})
+                   : (n == 2   ? DGLayout{2, 5, 6}
+                      : n == 3 ? DGLayout{3, 18, 7}
+                      : n == 4 ? DGLayout{4, 19, 0}
+                      : n == 5 ? DGLayout{5, 25, 2}
+                      : n == 6 ? DGLayout{9, 54, 8}
+                      : n == 7 ? DGLayout{7, 49, 12}
+                      : n == 8 ? DGLayout{9, 72, 0}
+                               : DGLayout{9, 81, 6});
+}
+
+template <int N, typename T>
+struct DGCfg {
+  static constexpr int CPB = DGCells<N>::value;
+  static constexpr DGLayout L = dg_layout(N, (int)sizeof(T));
+  static constexpr int P1 = L.P1, P2 = L.P2;
+  static constexpr int SLAB = P2 * N;            // elements per slab
+  static constexpr int RS = 3 * SLAB + L.SKEW;   // slab region per cell
+  static constexpr int N2 = N * N;
+  static constexpr size_t SMEM = (size_t(CPB) * RS + size_t(CPB) * 12 * N2) * sizeof(T);
+  static_assert((P1 + 1) * (N - 1) < P2, "slab padding overlaps");
+};
+
 template <int N, typename T, int KIND, bool TRANSPOSE, bool INVMASS, bool CHEB>
 __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     dg_kernel(const __grid_constant__ DGArgs<N, T> A)
 {
+  using Cfg = DGCfg<N, T>;
   constexpr int N2 = N * N, N3 = N * N * N;
-  constexpr int CPB = DGCells<N>::value;
+  constexpr int CPB = Cfg::CPB, P1 = Cfg::P1, P2 = Cfg::P2;
   constexpr int NF = KIND == K_SIPG ? 12 : 6; // face arrays per cell
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
@@ -163,17 +205,24 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   const bool valid = cell < A.n_cells;
   const long long roff = (long long)blockIdx.y * A.n_dofs; // right-hand side offset
   const T *__restrict__ x = A.x + roff;
-  T *Bblk = smem;                       // CPB cells x n^3: input / results
-  T *B0 = Bblk + cs * N3;
-  T *B1 = smem + CPB * N3 + cs * N3;    // Gauss-point values
-  T *B2 = smem + 2 * CPB * N3 + cs * N3;
+  T *B0 = smem + cs * Cfg::RS;
+  T *B1 = B0 + Cfg::SLAB, *B2 = B1 + Cfg::SLAB;
   // face arrays: [dir][side][value, derivative][n^2]  (SIPG), values only (advection)
-  T *F = smem + 3 * CPB * N3 + cs * (12 * N2);
+  T *F = smem + CPB * Cfg::RS + cs * (12 * N2);
+  const int zc = a + P1 * b;      // z column (a, b)
+  const int xl = P1 * a + P2 * b; // x line (y=a, z=b), stride 1
+  const int yl = a + P2 * b;      // y line (x=a, z=b), stride P1
+  // this thread's z column in the cell-major vector: runs of n^2 consecutive
+  // entries per warp instruction (coalesced)
+  const long long col = cell * N3 + t;
 
-  // ---- coalesced load of the block's cells ----
-  const int nval = (int)min((long long)CPB, A.n_cells - cell0) * N3;
-  const T *src = x + cell0 * N3;
-  for (int e = tid; e < nval; e += CPB * N2) Bblk[e] = __ldg(src + e);
+  T v[N], r[N];
+  // ---- z column of the input, z sweep ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = valid ? __ldg(x + col + N2 * m) : T(0);
+  eo_apply<N, 1>(A.S, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B0[zc + P2 * m] = v[m];
   // ---- neighbour face layers ----
   if (valid) {
     const unsigned uc = (unsigned)cell;
@@ -191,8 +240,8 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
       if (d == 0) { off = N * f0 + N2 * f1; stride_n = 1; }
       else if (d == 1) { off = f0 + N2 * f1; stride_n = N; }
       else { off = f0 + N * f1; stride_n = N2; }
-      base_in[0] = neighbour(A, ix, iy, iz, d, 0) * N3 + off;
-      base_in[1] = neighbour(A, ix, iy, iz, d, 1) * N3 + off;
+      base_in[0] = neighbour(A, ix, iy, int(iz), d, 0) * N3 + off;
+      base_in[1] = neighbour(A, ix, iy, int(iz), d, 1) * N3 + off;
       // side 0 (face at 0): neighbour's layer p (value) and p-1; side 1: layers 0 and 1
       const T v0 = __ldg(x + base_in[0] + (N - 1) * stride_n);
       const T v1 = __ldg(x + base_in[1]);
@@ -207,13 +256,7 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     }
   }
   __syncthreads();
-  T v[N], r[N];
-  // ---- z sweep of the cell, first tangential direction of the faces ----
-#pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B0[t + N2 * m];
-  eo_apply<N, 1>(A.S, v, v);
-#pragma unroll
-  for (int m = 0; m < N; ++m) B0[t + N2 * m] = v[m];
+  // ---- first tangential direction of the faces ----
   for (int task = t; task < NF * N; task += N2) {
     const int arr = task / N, line = task % N;
     const int k = KIND == K_SIPG ? arr : 2 * arr; // advection uses the value arrays only
@@ -227,10 +270,10 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   __syncthreads();
   // ---- x sweep, second tangential direction of the faces ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B0[N * t + m];
+  for (int m = 0; m < N; ++m) v[m] = B0[xl + m];
   eo_apply<N, 1>(A.S, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B0[N * t + m] = v[m];
+  for (int m = 0; m < N; ++m) B0[xl + m] = v[m];
   for (int task = t; task < NF * N; task += N2) {
     const int arr = task / N, line = task % N;
     const int k = KIND == K_SIPG ? arr : 2 * arr;
@@ -244,68 +287,73 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   __syncthreads();
   // ---- y lines: Gauss-point values, y residual ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B0[a + N * m + N2 * b];
+  for (int m = 0; m < N; ++m) v[m] = B0[yl + P1 * m];
   eo_apply<N, 1>(A.S, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B1[a + N * m + N2 * b] = v[m];
+  for (int m = 0; m < N; ++m) B1[yl + P1 * m] = v[m];
   // y line t = (a, c=b): face point (a, c) has weight w_a w_c
   line_residual<KIND, TRANSPOSE, N, T>(A, 1, v, A.w[a] * A.w[b], F, t, r);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B2[a + N * m + N2 * b] = r[m];
+  for (int m = 0; m < N; ++m) B2[yl + P1 * m] = r[m];
   __syncthreads();
   // ---- x lines and z lines ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B1[N * t + m];
+  for (int m = 0; m < N; ++m) v[m] = B1[xl + m];
   // x line t = (b, c) = (t%N, t/N)
   line_residual<KIND, TRANSPOSE, N, T>(A, 0, v, A.w[a] * A.w[b], F, t, r);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B0[N * t + m] = r[m];
+  for (int m = 0; m < N; ++m) B0[xl + m] = r[m];
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B1[t + N2 * m];
+  for (int m = 0; m < N; ++m) v[m] = B1[zc + P2 * m];
   T rz[N];
   line_residual<KIND, TRANSPOSE, N, T>(A, 2, v, A.w[a] * A.w[b], F, t, rz);
   __syncthreads();
-  // ---- sum, then integrate / apply the inverse mass along z ----
+  // ---- sum; integrate / apply the inverse mass along x, y, then z ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = rz[m] + B0[t + N2 * m] + B2[t + N2 * m];
+  for (int m = 0; m < N; ++m) v[m] = rz[m] + B0[zc + P2 * m] + B2[zc + P2 * m];
   if (INVMASS) {
     const T iwab = A.ijxw * A.iw[a] * A.iw[b];
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] *= iwab * A.iw[m];
-    eo_apply<N, 1>(A.P, v, v);
-  } else {
-    eo_apply<N, 1>(A.ST, v, v);
   }
 #pragma unroll
-  for (int m = 0; m < N; ++m) B1[t + N2 * m] = v[m];
+  for (int m = 0; m < N; ++m) B1[zc + P2 * m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B1[N * t + m];
+  for (int m = 0; m < N; ++m) v[m] = B1[xl + m];
   if (INVMASS) eo_apply<N, 1>(A.P, v, v);
   else eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B1[N * t + m] = v[m];
+  for (int m = 0; m < N; ++m) B1[xl + m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B1[a + N * m + N2 * b];
+  for (int m = 0; m < N; ++m) v[m] = B1[yl + P1 * m];
   if (INVMASS) eo_apply<N, 1>(A.P, v, v);
   else eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B1[a + N * m + N2 * b] = v[m];
+  for (int m = 0; m < N; ++m) B1[yl + P1 * m] = v[m];
   __syncthreads();
-  // ---- coalesced store (plain or fused Chebyshev update) ----
-  T *Rblk = smem + CPB * N3;
-  T *dst = A.y + roff + cell0 * N3;
-  if (CHEB) {
-    const long long o = cell0 * N3;
-    for (int e = tid; e < nval; e += CPB * N2) {
-      const T res = Rblk[e] - A.cb[o + e];
-      const T tn = A.c_tm * A.ct[o + e] + A.c_np * A.cdinv[o + e] * res;
-      A.ct[o + e] = tn;
-      dst[e] = __ldg(x + o + e) - tn;
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B1[zc + P2 * m];
+  if (INVMASS) eo_apply<N, 1>(A.P, v, v);
+  else eo_apply<N, 1>(A.ST, v, v);
+  // ---- store the z column (plain or fused Chebyshev update) ----
+  if (valid) {
+    T *dst = A.y + roff + col;
+    if (CHEB) {
+      const long long o = col;
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        const long long e = o + N2 * m;
+        const T res = v[m] - A.cb[e];
+        const T tn = A.c_tm * A.ct[e] + A.c_np * A.cdinv[e] * res;
+        A.ct[e] = tn;
+        dst[N2 * m] = __ldg(x + e) - tn;
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < N; ++m) dst[N2 * m] = v[m];
     }
-  } else {
-    for (int e = tid; e < nval; e += CPB * N2) dst[e] = Rblk[e];
   }
 }
 
@@ -424,7 +472,6 @@ int dg_vmult_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T *y, c
                   const T *cdinv, T *ct, double c_np, double c_tm, cudaStream_t st)
 {
   constexpr int CPB = DGCells<N>::value;
-  constexpr int N3 = N * N * N;
   DGArgs<N, T> A = make_dg_args<N, T>(op);
   A.x = x;
   A.y = y;
@@ -445,7 +492,7 @@ int dg_vmult_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T *y, c
     kern = cheb ? dg_kernel<N, T, K_ADVECT, false, true, true> : dg_kernel<N, T, K_ADVECT, false, true, false>;
   else
     kern = cheb ? dg_kernel<N, T, K_ADVECT, false, false, true> : dg_kernel<N, T, K_ADVECT, false, false, false>;
-  const size_t smem = (size_t(3) * CPB * N3 + size_t(CPB) * 12 * N * N) * sizeof(T);
+  const size_t smem = DGCfg<N, T>::SMEM;
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    cudaSharedmemCarveoutMaxShared));
