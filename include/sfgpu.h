@@ -143,6 +143,25 @@ int sf_vmult_transpose_static(sf_op *op, int prec, int nrhs, const void *x, void
 int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv,
                       const void *x_old, void *x_new, void *t, double c_np,
                       double c_tm, void *stream);
+/* Fused Runge-Kutta stage of the DG advection operator, replaces
+ * do_rk_stage<true> (evaluation_dg_advect.h:679-707, stage update
+ * :651-667):  r = A src (with the inverse mass when the handle has
+ * inverse_mass = 1, the reference's operator), then
+ *   vec_np = upd + c_np * r   and, when c_tm != 0,   vec_tm = vec_np + c_tm * r
+ * (vec_tm is not touched when c_tm == 0 and may then be NULL).  upd may be the
+ * same vector as src, vec_np or vec_tm, as in the reference's do_time_step;
+ * src must not be vec_np or vec_tm.  nrhs vectors of n_dofs entries each,
+ * contiguous.  The reference's current_time argument only names the exact
+ * solution's transport direction, which here is the handle's velocity. */
+int sf_rk_stage(sf_op *op, int prec, int nrhs, const void *src, const void *upd, void *vec_np,
+                void *vec_tm, double c_np, double c_tm, void *stream);
+/* One step of the five-stage fourth-order low-storage Runge-Kutta scheme of
+ * do_time_step (evaluation_dg_advect.h:190-214) with step dt: five fused
+ * stages with the reference's coefficients and register rotation; sol_new
+ * is advanced in place, sol_old and sol_tmp are the scheme's two registers
+ * (contents on entry are not used; three distinct vectors). */
+int sf_lsrk_step(sf_op *op, int prec, int nrhs, void *sol_new, void *sol_old, void *sol_tmp, double dt,
+                 void *stream);
 /* The same update without the operator, replaces
  * emulate_cheby_vector_updates() (evaluation_dg_laplacian.h:556-601):
  *   t <- c_tm * t + c_np * diag_inv .* (ax - b);  x_new <- x_old - t */

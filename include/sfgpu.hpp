@@ -275,6 +275,14 @@ public:
                 h[c] = Number(std::sin(k * x * pi) * std::cos(k * y * pi) * std::cos(k * z * pi));
               }
     sol_new.upload(h);
+    for (int k2 = 0; k2 < 3; ++k2) {
+      n_cells_[k2] = n_cells[k2];
+      velocity_[k2] = d.velocity[k2];
+    }
+    // evaluation_dg_advect.h:160-165: 0.2 / (cells per unit length) / |a| / p
+    const double an = std::sqrt(velocity_[0] * velocity_[0] + velocity_[1] * velocity_[1] +
+                                velocity_[2] * velocity_[2]);
+    time_step = 0.2 / (n_cells[0] / 2.0) / an / degree;
   }
   std::size_t n_elements() const { return sol_new.size() / dofs_per_cell; }
   // evaluation_dg_advect.h:216-219: sol_tmp = M^-1 A sol_new
@@ -282,9 +290,54 @@ public:
   {
     check(sf_vmult(op_.get(), precision_of<Number>(), sol_new.begin(), sol_tmp.begin(), s));
   }
+  // evaluation_dg_advect.h:679-707: with evaluate_stage, vec_np = upd +
+  // c_np M^-1 A src and vec_tm = vec_np + c_tm M^-1 A src (when c_tm != 0);
+  // without, vec_np = M^-1 A src.  current_time only names the transport
+  // direction in the reference; the handle's velocity is used here.
+  template <bool evaluate_stage = true>
+  void do_rk_stage(const DeviceVector<Number> &src, const DeviceVector<Number> &upd,
+                   DeviceVector<Number> &vec_np, DeviceVector<Number> &vec_tm, double /*current_time*/,
+                   Number c_np, Number c_tm, cudaStream_t s = 0)
+  {
+    if (evaluate_stage)
+      check(sf_rk_stage(op_.get(), precision_of<Number>(), 1, src.begin(), upd.begin(), vec_np.begin(),
+                        vec_tm.begin(), double(c_np), double(c_tm), s));
+    else
+      check(sf_vmult(op_.get(), precision_of<Number>(), src.begin(), vec_np.begin(), s));
+  }
+  // evaluation_dg_advect.h:190-214: one LSRK(5,4) step of size time_step
+  void do_time_step(double &current_time, cudaStream_t s = 0)
+  {
+    check(sf_lsrk_step(op_.get(), precision_of<Number>(), 1, sol_new.begin(), sol_old.begin(), sol_tmp.begin(),
+                       time_step, s));
+    current_time += time_step;
+  }
+  // evaluation_dg_advect.h:253-283: max |exact(time) - sol_new| over the nodes
+  double compute_max_error(double time) const
+  {
+    const std::vector<Number> u = sol_new.download();
+    const std::vector<double> gll = gll_points();
+    const double pi = 3.14159265358979323846, k = 4.0;
+    double err = 0.0;
+    std::size_t c = 0;
+    for (unsigned iz = 0; iz < n_cells_[2]; ++iz)
+      for (unsigned iy = 0; iy < n_cells_[1]; ++iy)
+        for (unsigned ix = 0; ix < n_cells_[0]; ++ix)
+          for (int lz = 0; lz <= degree; ++lz)
+            for (int ly = 0; ly <= degree; ++ly)
+              for (int lx = 0; lx <= degree; ++lx, ++c) {
+                const double x = (ix + gll[lx]) * 2.0 / n_cells_[0] - time * velocity_[0];
+                const double y = (iy + gll[ly]) * 2.0 / n_cells_[1] - time * velocity_[1];
+                const double z = (iz + gll[lz]) * 2.0 / n_cells_[2] - time * velocity_[2];
+                const double e = std::sin(k * x * pi) * std::cos(k * y * pi) * std::cos(k * z * pi);
+                err = std::fmax(err, std::fabs(e - double(u[c])));
+              }
+    return err;
+  }
   const Operator &op() const { return op_; }
 
   DeviceVector<Number> sol_old, sol_new, sol_tmp;
+  double time_step = 0.0;
 
 private:
   static std::vector<double> gll_points()
@@ -313,6 +366,8 @@ private:
     return x;
   }
   Operator op_;
+  unsigned n_cells_[3] = {0, 0, 0};
+  double velocity_[3] = {0.0, 0.0, 0.0};
 };
 
 } // namespace sfgpu

@@ -71,6 +71,8 @@ def lib():
         for f in ("sfo_dg_sipg_apply", "sfo_dg_advect_apply", "sfo_dg_advect_apply_transpose"):
             getattr(L, f).argtypes = [C.POINTER(DG), _dp, _dp]
         L.sfo_dg_sipg_diagonal.argtypes = [C.POINTER(DG), _dp]
+        L.sfo_dg_rk_stage.argtypes = [C.POINTER(DG), _dp, _dp, _dp, _dp, C.c_double, C.c_double]
+        L.sfo_dg_lsrk_step.argtypes = [C.POINTER(DG), C.c_double, _dp, _dp, _dp]
         L.sfo_chebyshev_update.argtypes = [C.c_longlong, _dp, _dp, _dp, _dp, _dp, _dp,
                                            C.c_double, C.c_double]
         _lib = L
@@ -203,6 +205,17 @@ def dg_advect_apply(g, x):
 
 def dg_advect_apply_transpose(g, x):
     return _dg_call("sfo_dg_advect_apply_transpose", g, x)
+
+
+def dg_rk_stage(g, src, upd, vec_np, vec_tm, c_np, c_tm):
+    """fused Runge-Kutta stage, vec_np / vec_tm updated in place (float64
+    contiguous arrays; upd may be the same array as vec_np or vec_tm)"""
+    lib().sfo_dg_rk_stage(C.byref(g), src, upd, vec_np, vec_tm, c_np, c_tm)
+
+
+def dg_lsrk_step(g, dt, sol_new, sol_old, sol_tmp):
+    """one LSRK(5,4) step, all three arrays updated in place"""
+    lib().sfo_dg_lsrk_step(C.byref(g), dt, sol_new, sol_old, sol_tmp)
 
 
 def dg_sipg_diagonal(g):

@@ -56,6 +56,42 @@ static void advect(const int *nc, const double *h, const double *x, double *y)
   for (std::size_t i = 0; i < N; ++i) y[i] = np[i];
 }
 
+/* one fused Runge-Kutta stage of the reference: r = M^-1 K src,
+ * vec_np = upd + c_np r, vec_tm = vec_np + c_tm r (when c_tm != 0) */
+template <int p>
+static void rk_stage(const int *nc, const double *h, const double *src, const double *upd,
+                     double c_np, double c_tm, double *vnp, double *vtm)
+{
+  EvaluationDGAdvection<3, p, double> ev;
+  ev.blx = 2; ev.bly = 2; ev.blz = 2;
+  unsigned int n_cells[3] = {(unsigned)nc[0], (unsigned)nc[1], (unsigned)nc[2]};
+  ev.initialize(n_cells);
+  set_geometry(ev, h);
+  const std::size_t N = ev.n_elements() * ev.dofs_per_cell;
+  AlignedVector<double> s(N), u(N), np(N), tm(N);
+  for (std::size_t i = 0; i < N; ++i) { s[i] = src[i]; u[i] = upd[i]; tm[i] = vtm[i]; }
+  ev.template do_rk_stage<true>(s, u, np, tm, 0., c_np, c_tm);
+  for (std::size_t i = 0; i < N; ++i) { vnp[i] = np[i]; vtm[i] = tm[i]; }
+}
+
+/* nsteps calls of the reference's do_time_step (LSRK(5,4)) from sol_new = x,
+ * sol_old = sol_tmp = 0, with the given time step */
+template <int p>
+static void time_steps(const int *nc, const double *h, int nsteps, double dt, double *x)
+{
+  EvaluationDGAdvection<3, p, double> ev;
+  ev.blx = 2; ev.bly = 2; ev.blz = 2;
+  unsigned int n_cells[3] = {(unsigned)nc[0], (unsigned)nc[1], (unsigned)nc[2]};
+  ev.initialize(n_cells);
+  set_geometry(ev, h);
+  const std::size_t N = ev.n_elements() * ev.dofs_per_cell;
+  for (std::size_t i = 0; i < N; ++i) { ev.sol_new[i] = x[i]; ev.sol_old[i] = 0.; ev.sol_tmp[i] = 0.; }
+  ev.time_step = dt;
+  double t = 0.;
+  for (int s = 0; s < nsteps; ++s) ev.do_time_step(t);
+  for (std::size_t i = 0; i < N; ++i) x[i] = ev.sol_new[i];
+}
+
 template <int p>
 static void face_tables(double *face_eo, double *Sinv_eo)
 {
@@ -92,3 +128,12 @@ extern "C" int sfref_dg_advect(int degree, const int *nc, const double *h,
 
 extern "C" int sfref_dg_tables(int degree, double *face_eo, double *Sinv_eo)
 { SF_DISPATCH(face_tables, face_eo, Sinv_eo) }
+
+extern "C" int sfref_dg_rk_stage(int degree, const int *nc, const double *h, const double *src,
+                                 const double *upd, double c_np, double c_tm, double *vnp,
+                                 double *vtm)
+{ SF_DISPATCH(rk_stage, nc, h, src, upd, c_np, c_tm, vnp, vtm) }
+
+extern "C" int sfref_dg_time_steps(int degree, const int *nc, const double *h, int nsteps,
+                                   double dt, double *x)
+{ SF_DISPATCH(time_steps, nc, h, nsteps, dt, x) }

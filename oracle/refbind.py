@@ -136,6 +136,31 @@ def dg_advect(degree, n_cells, h, x):
     return y
 
 
+def dg_rk_stage(degree, n_cells, h, src, upd, c_np, c_tm, vec_tm=None):
+    """the reference's do_rk_stage<true>: returns (vec_np, vec_tm)"""
+    L = _lib("ref_dg")
+    L.sfref_dg_rk_stage.argtypes = [C.c_int, _ip, _dp, _dp, _dp, C.c_double, C.c_double, _dp, _dp]
+    N = len(src)
+    vnp = np.zeros(N)
+    vtm = np.zeros(N) if vec_tm is None else np.array(vec_tm, dtype=np.float64)
+    rc = L.sfref_dg_rk_stage(degree, np.array(n_cells, dtype=np.int32), np.array(h, dtype=np.float64),
+                             np.ascontiguousarray(src, dtype=np.float64),
+                             np.ascontiguousarray(upd, dtype=np.float64), c_np, c_tm, vnp, vtm)
+    assert rc == 0
+    return vnp, vtm
+
+
+def dg_time_steps(degree, n_cells, h, x, nsteps, dt):
+    """nsteps of the reference's do_time_step (LSRK(5,4)) from sol_new = x"""
+    L = _lib("ref_dg")
+    L.sfref_dg_time_steps.argtypes = [C.c_int, _ip, _dp, C.c_int, C.c_double, _dp]
+    y = np.array(x, dtype=np.float64)
+    rc = L.sfref_dg_time_steps(degree, np.array(n_cells, dtype=np.int32), np.array(h, dtype=np.float64),
+                               nsteps, dt, y)
+    assert rc == 0
+    return y
+
+
 def dg_tables(degree):
     L = _lib("ref_dg")
     L.sfref_dg_tables.argtypes = [C.c_int, _dp, _dp]

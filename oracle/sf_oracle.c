@@ -1275,6 +1275,41 @@ void sfo_dg_advect_apply(const sfo_dg *g, const double *x, double *y)
   }
 }
 
+void sfo_dg_rk_stage(const sfo_dg *g, const double *src, const double *upd,
+                     double *vec_np, double *vec_tm, double c_np, double c_tm)
+{
+  const long long N = sfo_dg_n_dofs(g);
+  double *r = (double *)malloc(sizeof(double) * N);
+  sfo_dg_advect_apply(g, src, r);
+  for (long long i = 0; i < N; ++i) {
+    const double np = upd[i] + c_np * r[i];
+    vec_np[i] = np;
+    if (c_tm != 0.) vec_tm[i] = np + c_tm * r[i];
+  }
+  free(r);
+}
+
+/* LSRK(5,4) coefficients and the register rotation of do_time_step
+ * (evaluation_dg_advect.h:192-212) */
+void sfo_dg_lsrk_step(const sfo_dg *g, double dt, double *sol_new, double *sol_old,
+                      double *sol_tmp)
+{
+  const double a21 = 970286171893. / 4311952581923.;
+  const double a32 = 6584761158862. / 12103376702013.;
+  const double a43 = 2251764453980. / 15575788980749.;
+  const double a54 = 26877169314380. / 34165994151039.;
+  const double b1 = 1153189308089. / 22510343858157.;
+  const double b2 = 1772645290293. / 4653164025191.;
+  const double b3 = -1672844663538. / 4480602732383.;
+  const double b4 = 2114624349019. / 3568978502595.;
+  const double b5 = 5198255086312. / 14908931495163.;
+  sfo_dg_rk_stage(g, sol_new, sol_new, sol_old, sol_tmp, a21 * dt, (b1 - a21) * dt);
+  sfo_dg_rk_stage(g, sol_old, sol_tmp, sol_new, sol_tmp, a32 * dt, (b2 - a32) * dt);
+  sfo_dg_rk_stage(g, sol_new, sol_tmp, sol_old, sol_tmp, a43 * dt, (b3 - a43) * dt);
+  sfo_dg_rk_stage(g, sol_old, sol_tmp, sol_tmp, sol_new, a54 * dt, (b4 - a54) * dt);
+  sfo_dg_rk_stage(g, sol_tmp, sol_new, sol_new, sol_tmp, b5 * dt, 0.0);
+}
+
 /* inverse mass matrix of the GLL basis with Gauss quadrature,
  * M^-1 = P W^-1 P^T per cell, P = Sinv (Gauss values -> GLL nodal values);
  * the reference applies P W^-1 on collocation residuals

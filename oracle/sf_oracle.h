@@ -112,6 +112,16 @@ void sfo_dg_sipg_apply(const sfo_dg *g, const double *x, double *y);
 void sfo_dg_sipg_diagonal(const sfo_dg *g, double *diag);
 void sfo_dg_advect_apply(const sfo_dg *g, const double *x, double *y);
 void sfo_dg_advect_apply_transpose(const sfo_dg *g, const double *x, double *y);
+/* fused Runge-Kutta stage (evaluation_dg_advect.h:286-290,651-707):
+ * r = advect_apply(src); vec_np = upd + c_np r; vec_tm = vec_np + c_tm r when
+ * c_tm != 0 (vec_tm untouched otherwise).  upd may alias vec_np or vec_tm. */
+void sfo_dg_rk_stage(const sfo_dg *g, const double *src, const double *upd,
+                     double *vec_np, double *vec_tm, double c_np, double c_tm);
+/* one step of the five-stage fourth-order low-storage Runge-Kutta scheme
+ * (evaluation_dg_advect.h:190-214) with step dt: sol_new advanced in place,
+ * sol_old and sol_tmp are the scheme's registers */
+void sfo_dg_lsrk_step(const sfo_dg *g, double dt, double *sol_new, double *sol_old,
+                      double *sol_tmp);
 
 /* ---------------- vector kernels ---------------- */
 void sfo_chebyshev_update(long long n, const double *ax, const double *b,

@@ -339,6 +339,49 @@ int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv, 
   return launch_vector_update(op->n_dofs, prec, x_new, b, diag_inv, x_old, x_new, t, c_np, c_tm, st);
 }
 
+int sf_rk_stage(sf_op *op, int prec, int nrhs, const void *src, const void *upd, void *vec_np, void *vec_tm,
+                double c_np, double c_tm, void *stream)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (op->desc.kind != SF_OP_DG_ADVECT) return fail(SF_ERR_STATE, "Runge-Kutta stages need SF_OP_DG_ADVECT");
+  SF_RET(check_prec(op, prec));
+  SF_RET(check_ptr(src, prec, "src"));
+  SF_RET(check_ptr(upd, prec, "upd"));
+  SF_RET(check_ptr(vec_np, prec, "vec_np"));
+  if (c_tm != 0.0) SF_RET(check_ptr(vec_tm, prec, "vec_tm"));
+  if (nrhs < 1 || nrhs > 64) return fail(SF_ERR_INVALID, "nrhs must be 1..64");
+  if (src == vec_np || (c_tm != 0.0 && src == vec_tm))
+    return fail(SF_ERR_INVALID, "src must not be an output vector");
+  if (c_tm != 0.0 && vec_np == vec_tm) return fail(SF_ERR_INVALID, "vec_np and vec_tm must differ");
+  return launch_dg_rk_stage(op, prec, nrhs, src, upd, vec_np, c_tm != 0.0 ? vec_tm : nullptr, c_np, c_tm,
+                            (cudaStream_t)stream);
+}
+
+// LSRK(5,4) of evaluation_dg_advect.h:192-212: coefficients and the rotation
+// of the three registers over the five stages
+int sf_lsrk_step(sf_op *op, int prec, int nrhs, void *sol_new, void *sol_old, void *sol_tmp, double dt,
+                 void *stream)
+{
+  if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (!sol_new || !sol_old || !sol_tmp) return fail(SF_ERR_NULL, "sol_new/sol_old/sol_tmp is NULL");
+  if (sol_new == sol_old || sol_new == sol_tmp || sol_old == sol_tmp)
+    return fail(SF_ERR_INVALID, "sol_new, sol_old and sol_tmp must be distinct");
+  const double a21 = 970286171893. / 4311952581923.;
+  const double a32 = 6584761158862. / 12103376702013.;
+  const double a43 = 2251764453980. / 15575788980749.;
+  const double a54 = 26877169314380. / 34165994151039.;
+  const double b1 = 1153189308089. / 22510343858157.;
+  const double b2 = 1772645290293. / 4653164025191.;
+  const double b3 = -1672844663538. / 4480602732383.;
+  const double b4 = 2114624349019. / 3568978502595.;
+  const double b5 = 5198255086312. / 14908931495163.;
+  SF_RET(sf_rk_stage(op, prec, nrhs, sol_new, sol_new, sol_old, sol_tmp, a21 * dt, (b1 - a21) * dt, stream));
+  SF_RET(sf_rk_stage(op, prec, nrhs, sol_old, sol_tmp, sol_new, sol_tmp, a32 * dt, (b2 - a32) * dt, stream));
+  SF_RET(sf_rk_stage(op, prec, nrhs, sol_new, sol_tmp, sol_old, sol_tmp, a43 * dt, (b3 - a43) * dt, stream));
+  SF_RET(sf_rk_stage(op, prec, nrhs, sol_old, sol_tmp, sol_tmp, sol_new, a54 * dt, (b4 - a54) * dt, stream));
+  return sf_rk_stage(op, prec, nrhs, sol_tmp, sol_new, sol_new, sol_tmp, b5 * dt, 0.0, stream);
+}
+
 int sf_vector_update(long long n, int prec, const void *ax, const void *b, const void *diag_inv,
                      const void *x_old, void *x_new, void *t, double c_np, double c_tm, void *stream)
 {

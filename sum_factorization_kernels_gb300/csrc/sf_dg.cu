@@ -30,6 +30,9 @@ namespace sf {
 namespace {
 
 enum { K_SIPG = 0, K_ADVECT = 1 };
+// epilogue of the apply: plain store, fused Chebyshev step, fused
+// Runge-Kutta stage
+enum { EPI_STORE = 0, EPI_CHEB = 1, EPI_RK = 2 };
 
 template <int N, typename T>
 struct DGArgs {
@@ -51,6 +54,10 @@ struct DGArgs {
   const T *__restrict__ cdinv;   // Chebyshev: inverse diagonal
   T *__restrict__ ct;            // Chebyshev: t
   T c_np, c_tm;
+  // Runge-Kutta stage: vec_np = upd + c_np r, vec_tm = vec_np + c_tm r;
+  // upd may alias vec_np or vec_tm (read before written, element by element)
+  const T *rk_upd;
+  T *rk_np, *rk_tm;
   int nc[3];
   FastDiv div_nx, div_ny;        // division by nc[0], nc[1]
   long long n_cells, n_dofs;
@@ -186,7 +193,7 @@ struct DGCfg {
   static_assert((P1 + 1) * (N - 1) < P2, "slab padding overlaps");
 };
 
-template <int N, typename T, int KIND, bool TRANSPOSE, bool INVMASS, bool CHEB>
+template <int N, typename T, int KIND, bool TRANSPOSE, bool INVMASS, int EPI>
 __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     dg_kernel(const __grid_constant__ DGArgs<N, T> A)
 {
@@ -337,10 +344,19 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   for (int m = 0; m < N; ++m) v[m] = B1[zc + P2 * m];
   if (INVMASS) eo_apply<N, 1>(A.P, v, v);
   else eo_apply<N, 1>(A.ST, v, v);
-  // ---- store the z column (plain or fused Chebyshev update) ----
+  // ---- store the z column (plain, fused Chebyshev or Runge-Kutta update) ----
   if (valid) {
     T *dst = A.y + roff + col;
-    if (CHEB) {
+    if (EPI == EPI_RK) {
+      const long long o = roff + col;
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        const long long e = o + N2 * m;
+        const T np = A.rk_upd[e] + A.c_np * v[m];
+        A.rk_np[e] = np;
+        if (A.c_tm != T(0)) A.rk_tm[e] = np + A.c_tm * v[m];
+      }
+    } else if (EPI == EPI_CHEB) {
       const long long o = col;
 #pragma unroll
       for (int m = 0; m < N; ++m) {
@@ -469,7 +485,8 @@ DGArgs<N, T> make_dg_args(const sf_op *op)
 
 template <int N, typename T>
 int dg_vmult_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T *y, const T *cb,
-                  const T *cdinv, T *ct, double c_np, double c_tm, cudaStream_t st)
+                  const T *cdinv, T *ct, double c_np, double c_tm, const T *rk_upd, T *rk_np, T *rk_tm,
+                  cudaStream_t st)
 {
   constexpr int CPB = DGCells<N>::value;
   DGArgs<N, T> A = make_dg_args<N, T>(op);
@@ -480,18 +497,24 @@ int dg_vmult_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T *y, c
   A.ct = ct;
   A.c_np = T(c_np);
   A.c_tm = T(c_tm);
+  A.rk_upd = rk_upd;
+  A.rk_np = rk_np;
+  A.rk_tm = rk_tm;
   const bool sipg = op->desc.kind == SF_OP_DG_SIPG;
-  const bool cheb = cb != nullptr;
+  const bool cheb = cb != nullptr, rk = rk_np != nullptr;
   const bool invm = !sipg && !transpose && op->desc.inverse_mass;
   void (*kern)(const DGArgs<N, T>);
   if (sipg)
-    kern = cheb ? dg_kernel<N, T, K_SIPG, false, false, true> : dg_kernel<N, T, K_SIPG, false, false, false>;
+    kern = cheb ? dg_kernel<N, T, K_SIPG, false, false, EPI_CHEB> : dg_kernel<N, T, K_SIPG, false, false, EPI_STORE>;
   else if (transpose)
-    kern = dg_kernel<N, T, K_ADVECT, true, false, false>;
+    kern = dg_kernel<N, T, K_ADVECT, true, false, EPI_STORE>;
   else if (invm)
-    kern = cheb ? dg_kernel<N, T, K_ADVECT, false, true, true> : dg_kernel<N, T, K_ADVECT, false, true, false>;
+    kern = rk ? dg_kernel<N, T, K_ADVECT, false, true, EPI_RK>
+         : cheb ? dg_kernel<N, T, K_ADVECT, false, true, EPI_CHEB> : dg_kernel<N, T, K_ADVECT, false, true, EPI_STORE>;
   else
-    kern = cheb ? dg_kernel<N, T, K_ADVECT, false, false, true> : dg_kernel<N, T, K_ADVECT, false, false, false>;
+    kern = rk ? dg_kernel<N, T, K_ADVECT, false, false, EPI_RK>
+         : cheb ? dg_kernel<N, T, K_ADVECT, false, false, EPI_CHEB>
+                : dg_kernel<N, T, K_ADVECT, false, false, EPI_STORE>;
   const size_t smem = DGCfg<N, T>::SMEM;
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -523,13 +546,16 @@ int dg_invmass_impl(const sf_op *op, int nrhs, const T *x, T *y, cudaStream_t st
 
 template <int N>
 int dg_vmult_n(const sf_op *op, int prec, int nrhs, bool tr, const void *x, void *y, const void *cb,
-               const void *cd, void *ct, double c_np, double c_tm, cudaStream_t st)
+               const void *cd, void *ct, double c_np, double c_tm, const void *upd, void *vnp, void *vtm,
+               cudaStream_t st)
 {
   if (prec == SF_FP64)
     return dg_vmult_impl<N, double>(op, nrhs, tr, (const double *)x, (double *)y, (const double *)cb,
-                                    (const double *)cd, (double *)ct, c_np, c_tm, st);
+                                    (const double *)cd, (double *)ct, c_np, c_tm, (const double *)upd,
+                                    (double *)vnp, (double *)vtm, st);
   return dg_vmult_impl<N, float>(op, nrhs, tr, (const float *)x, (float *)y, (const float *)cb,
-                                 (const float *)cd, (float *)ct, c_np, c_tm, st);
+                                 (const float *)cd, (float *)ct, c_np, c_tm, (const float *)upd, (float *)vnp,
+                                 (float *)vtm, st);
 }
 
 template <int N>
@@ -560,7 +586,15 @@ int launch_dg_vmult(const sf_op *op, int prec, int nrhs, bool transpose, const v
 {
   if (op->desc.n_cells[0] < 1) return SF_ERR_INVALID;
   SF_DEG_DISPATCH(op->desc.degree, dg_vmult_n, op, prec, nrhs, transpose, x, y, cb, cdinv, ct, c_np,
-                  c_tm, st)
+                  c_tm, nullptr, nullptr, nullptr, st)
+}
+
+int launch_dg_rk_stage(const sf_op *op, int prec, int nrhs, const void *src, const void *upd, void *vec_np,
+                       void *vec_tm, double c_np, double c_tm, cudaStream_t st)
+{
+  if (op->desc.kind != SF_OP_DG_ADVECT) return SF_ERR_STATE;
+  SF_DEG_DISPATCH(op->desc.degree, dg_vmult_n, op, prec, nrhs, false, src, vec_np, nullptr, nullptr, nullptr,
+                  c_np, c_tm, upd, vec_np, vec_tm, st)
 }
 
 int launch_dg_inverse_mass(const sf_op *op, int prec, int nrhs, const void *x, void *y,

@@ -29,6 +29,10 @@ int launch_dg_vmult(const sf_op *op, int prec, int nrhs, bool transpose, const v
                     double c_tm, cudaStream_t st);
 int launch_dg_inverse_mass(const sf_op *op, int prec, int nrhs, const void *x, void *y,
                            cudaStream_t st);
+// fused advection Runge-Kutta stage: r = M^-1 A src, vec_np = upd + c_np r,
+// vec_tm = vec_np + c_tm r (when c_tm != 0)
+int launch_dg_rk_stage(const sf_op *op, int prec, int nrhs, const void *src, const void *upd, void *vec_np,
+                       void *vec_tm, double c_np, double c_tm, cudaStream_t st);
 int launch_dg_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
 
 // blocks of a kernel that fit on one SM with the maximum shared-memory

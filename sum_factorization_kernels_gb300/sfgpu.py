@@ -30,6 +30,7 @@ EXPORTS = [
     "sf_vmult_transpose_batched", "sf_chebyshev_step", "sf_vector_update", "sf_diagonal",
     "sf_kappa_gradient", "sf_solve_opts_default", "sf_cg_solve", "sf_convert", "sf_dot",
     "sf_shape_tables", "sf_set_kernel_variant", "sf_device_status", "sf_vmult_transpose_static",
+    "sf_rk_stage", "sf_lsrk_step",
 ]
 
 
@@ -94,6 +95,8 @@ def lib():
         L.sf_set_kernel_variant.argtypes = [vp, i]
         L.sf_vmult_transpose_static.argtypes = [vp, i, i, vp, vp, vp]
         L.sf_device_status.argtypes = [vp, C.POINTER(i)]
+        L.sf_rk_stage.argtypes = [vp, i, i, vp, vp, vp, vp, d, d, vp]
+        L.sf_lsrk_step.argtypes = [vp, i, i, vp, vp, vp, d, vp]
         _lib = L
     return _lib
 
@@ -194,6 +197,16 @@ class Operator:
         check(lib().sf_chebyshev_step(self._h, prec_of(x_old), ptr(b), ptr(diag_inv), ptr(x_old),
                                       ptr(x_new), ptr(t), float(c_np), float(c_tm),
                                       stream_ptr(stream)))
+
+    def rk_stage(self, src, upd, vec_np, vec_tm, c_np, c_tm, nrhs=1, stream=None):
+        """do_rk_stage<true>: vec_np = upd + c_np A src, vec_tm = vec_np + c_tm A src"""
+        check(lib().sf_rk_stage(self._h, prec_of(src), int(nrhs), ptr(src), ptr(upd), ptr(vec_np), ptr(vec_tm),
+                                float(c_np), float(c_tm), stream_ptr(stream)))
+
+    def lsrk_step(self, sol_new, sol_old, sol_tmp, dt, nrhs=1, stream=None):
+        """do_time_step: one LSRK(5,4) step, sol_new advanced in place"""
+        check(lib().sf_lsrk_step(self._h, prec_of(sol_new), int(nrhs), ptr(sol_new), ptr(sol_old), ptr(sol_tmp),
+                                 float(dt), stream_ptr(stream)))
 
     def diagonal(self, out, stream=None):
         check(lib().sf_diagonal(self._h, prec_of(out), ptr(out), stream_ptr(stream)))

@@ -97,6 +97,25 @@ int main()
     std::printf("EvaluationDGAdvection<6,float>::do_matvec rel err %.3e\n", e);
     fails += !(e < 1e-5);
   }
+  // DG advection time stepping, p = 4, FP64: LSRK(5,4) of the analytic wave
+  // (the reference's do_time_step / compute_max_error driver)
+  {
+    const unsigned nc[3] = {16, 16, 16};
+    sfgpu::EvaluationDGAdvection<4, double> ev;
+    ev.initialize(nc);
+    double t = 0.0;
+    const double e0 = ev.compute_max_error(t);
+    std::vector<double> xo = ev.sol_new.download(), oo(xo.size(), 0.0), to(xo.size(), 0.0);
+    for (int s = 0; s < 20; ++s) ev.do_time_step(t);
+    cudaDeviceSynchronize();
+    const double e1 = ev.compute_max_error(t);
+    sfo_dg g{4, {16, 16, 16}, {0.125, 0.125, 0.125}, 1.0, {1.0, 0.15, -0.05}, 1};
+    for (int s = 0; s < 20; ++s) sfo_dg_lsrk_step(&g, ev.time_step, xo.data(), oo.data(), to.data());
+    const double ep = rel(ev.sol_new.download(), xo);
+    std::printf("EvaluationDGAdvection<4,double>::do_time_step x20 (t = %.4f): max error %.3e vs the exact "
+                "wave (initial %.3e), rel. difference to the oracle %.3e\n", t, e1, e0, ep);
+    fails += !(e1 < 2e-3 && e0 < 1e-14 && ep < 1e-12);
+  }
   std::printf(fails ? "FAILED\n" : "OK\n");
   return fails;
 }

@@ -175,8 +175,36 @@ def main():
     np.savez(os.path.join(HERE, "dg_advect.npz"), **out)
 
 
+def rk_fixtures():
+    """the reference's fused Runge-Kutta stage (do_rk_stage<true>) and its
+    LSRK(5,4) time step (do_time_step), own seed so the other fixtures keep
+    their values"""
+    rng = np.random.default_rng(20241207)
+    out = {}
+    for p in (1, 2, 4, 5):
+        nc, h = ((3, 2, 4) if p <= 4 else (3, 2, 2)), (0.3, 0.5, 0.2)
+        N = nc[0] * nc[1] * nc[2] * (p + 1) ** 3
+        src, upd, tm0 = rng.uniform(-1, 1, N), rng.uniform(-1, 1, N), rng.uniform(-1, 1, N)
+        for case, (c_np, c_tm) in (("a", (0.013, -0.007)), ("b", (0.021, 0.0))):
+            vnp, vtm = R.dg_rk_stage(p, nc, h, src, upd, c_np, c_tm, vec_tm=tm0)
+            out["np_%s_%d" % (case, p)], out["tm_%s_%d" % (case, p)] = vnp, vtm
+            out["c_%s_%d" % (case, p)] = np.array([c_np, c_tm])
+        x0 = rng.uniform(-1, 1, N)
+        dt = 0.2 * min(h) / (np.linalg.norm([1.0, 0.15, -0.05]) * p)
+        out["src_%d" % p], out["upd_%d" % p], out["tm0_%d" % p] = src, upd, tm0
+        out["x0_%d" % p], out["dt_%d" % p] = x0, np.array(dt)
+        out["steps3_%d" % p] = R.dg_time_steps(p, nc, h, x0, 3, dt)
+        out["nc_%d" % p], out["h_%d" % p] = np.array(nc), np.array(h)
+    np.savez(os.path.join(HERE, "dg_rk.npz"), **out)
+
+
 if __name__ == "__main__":
-    main()
+    import sys
+    if sys.argv[1:] == ["rk"]:
+        rk_fixtures()
+    else:
+        main()
+        rk_fixtures()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -127,3 +127,41 @@ def test_dg_advect(golden, p):
              velocity=(1.0, 0.15, -0.05), inverse_mass=1)
     y = O.dg_advect_apply(d, g["x_%d" % p])
     assert rel(y, g["y_%d" % p]) < 1e-14
+
+
+@pytest.mark.parametrize("p", [1, 2, 4, 5])
+@pytest.mark.parametrize("case", ["a", "b"])
+def test_dg_rk_stage(golden, p, case):
+    """fused Runge-Kutta stage against the reference's do_rk_stage<true>
+    (case b has c_tm = 0: vec_tm must stay untouched)"""
+    g = golden("dg_rk.npz")
+    d = O.dg(p, tuple(int(v) for v in g["nc_%d" % p]), tuple(g["h_%d" % p]),
+             velocity=(1.0, 0.15, -0.05), inverse_mass=1)
+    c_np, c_tm = (float(v) for v in g["c_%s_%d" % (case, p)])
+    vnp = np.zeros_like(g["src_%d" % p])
+    vtm = np.array(g["tm0_%d" % p])
+    O.dg_rk_stage(d, np.array(g["src_%d" % p]), np.array(g["upd_%d" % p]), vnp, vtm, c_np, c_tm)
+    assert rel(vnp, g["np_%s_%d" % (case, p)]) < 1e-14
+    assert rel(vtm, g["tm_%s_%d" % (case, p)]) < 1e-14
+    # the same stage with upd aliasing the output vectors, as do_time_step calls it
+    u = np.array(g["upd_%d" % p])
+    vtm2 = np.array(g["tm0_%d" % p]) if case == "b" else u
+    if case == "a":
+        O.dg_rk_stage(d, np.array(g["src_%d" % p]), u, vnp, u, c_np, c_tm)
+        assert rel(u, g["tm_a_%d" % p]) < 1e-14
+    else:
+        O.dg_rk_stage(d, np.array(g["src_%d" % p]), u, u, vtm2, c_np, c_tm)
+        assert rel(u, g["np_b_%d" % p]) < 1e-14
+
+
+@pytest.mark.parametrize("p", [1, 2, 4, 5])
+def test_dg_lsrk_steps(golden, p):
+    """three LSRK(5,4) steps against the reference's do_time_step"""
+    g = golden("dg_rk.npz")
+    d = O.dg(p, tuple(int(v) for v in g["nc_%d" % p]), tuple(g["h_%d" % p]),
+             velocity=(1.0, 0.15, -0.05), inverse_mass=1)
+    x = np.array(g["x0_%d" % p])
+    old, tmp = np.zeros_like(x), np.zeros_like(x)
+    for _ in range(3):
+        O.dg_lsrk_step(d, float(g["dt_%d" % p]), x, old, tmp)
+    assert rel(x, g["steps3_%d" % p]) < 1e-13
