@@ -309,12 +309,25 @@ def secondary_configs(stream, peak):
         for _ in range(reps):
             op.vmult_transpose_batched(xx, yy, 8, stream=stream)
         ev[2].record(stream)
+        # LSRK(5,4) time steps (do_time_step): five fused operator stages
+        old, tmp = torch.zeros_like(xx), torch.zeros_like(xx)
+        op.lsrk_step(xx, old, tmp, 1e-3, nrhs=8, stream=stream)
+        ev[3].record(stream)
+        for _ in range(reps):
+            op.lsrk_step(xx, old, tmp, 1e-3, nrhs=8, stream=stream)
+        ev.append(torch.cuda.Event(enable_timing=True))
+        ev[4].record(stream)
         torch.cuda.synchronize()
         tf = ev[0].elapsed_time(ev[1]) / 1e3 / reps
         tt = ev[1].elapsed_time(ev[2]) / 1e3 / reps
-        res[prec] = {"forward_gdofs_per_rhs": round(N / tf / 1e9, 3),
+        ts = ev[3].elapsed_time(ev[4]) / 1e3 / reps
+        res[prec] = {"forward_gdofs_total_8rhs": round(8 * N / tf / 1e9, 3),
                      "forward_hbm_frac": round(2 * dt.itemsize * 8 * N / tf / 1e9 / peak, 4),
-                     "transpose_gdofs_per_rhs": round(N / tt / 1e9, 3)}
+                     "transpose_gdofs_total_8rhs": round(8 * N / tt / 1e9, 3),
+                     # DoF-steps per second; 5 stages x (src, upd read; vec_np, vec_tm written),
+                     # the reference's memory model (test_dg_advect.cc:111-113)
+                     "lsrk_step_gdofs_total_8rhs": round(8 * N / ts / 1e9, 3),
+                     "lsrk_step_hbm_frac": round(20 * dt.itemsize * 8 * N / ts / 1e9 / peak, 4)}
     x64 = torch.rand(8 * N, device="cuda", dtype=torch.float64) * 2 - 1
     y64 = torch.rand(8 * N, device="cuda", dtype=torch.float64) * 2 - 1
     ax, aty = torch.empty_like(x64), torch.empty_like(y64)

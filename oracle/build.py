@@ -41,6 +41,34 @@ PATCHES = [
     ("evaluation_dg_advect.h", 435,
      "(ii-(n_cells[0]-1)*n_lanes)+dofs_per_cell",
      "(ii-(n_cells[0]-1)*n_lanes)*dofs_per_cell"),
+    ("precomputed_dg_laplacian.h", 142,
+     "(ii-(n_cells[0]-1)*n_lanes)+dofs_per_cell",
+     "(ii-(n_cells[0]-1)*n_lanes)*dofs_per_cell"),
+    # neighbour couplings of the precomputed SIPG matrices: the face-point
+    # values are taken at the swapped ends (phi_0 at 1, phi_{N-1} at 0), which
+    # are zero for the Hermite-like basis; the SIPG coupling of test phi_0(0)
+    # with the left neighbour's phi_j(1) is
+    # -tau phi_0(0) phi_j(1) - 1/2 phi_0'(0) phi_j(1) + 1/2 phi_j'(1) phi_0(0)
+    ("precomputed_dg_laplacian.h", 344, "basis.value(0, 1.)*basis.value(N-1, 0.)",
+     "basis.value(0, 0.)*basis.value(N-1, 1.)"),
+    ("precomputed_dg_laplacian.h", 345, "+", "-"),
+    ("precomputed_dg_laplacian.h", 346, "basis.derivative(0, 1.)*basis.value(N-1, 0.)",
+     "basis.derivative(0, 0.)*basis.value(N-1, 1.)"),
+    ("precomputed_dg_laplacian.h", 347, "-", "+"),
+    ("precomputed_dg_laplacian.h", 348, "basis.derivative(N-1, 0.)*basis.value(0, 1.)",
+     "basis.derivative(N-1, 1.)*basis.value(0, 0.)"),
+    ("precomputed_dg_laplacian.h", 349, "basis.value(0, 1.)*basis.value(N-2, 0.)",
+     "basis.value(0, 0.)*basis.value(N-2, 1.)"),
+    ("precomputed_dg_laplacian.h", 350, "+", "-"),
+    ("precomputed_dg_laplacian.h", 351, "basis.derivative(0, 1.)*basis.value(N-2, 0.)",
+     "basis.derivative(0, 0.)*basis.value(N-2, 1.)"),
+    ("precomputed_dg_laplacian.h", 352, "-", "+"),
+    ("precomputed_dg_laplacian.h", 353, "basis.derivative(N-2, 0.)*basis.value(0, 1.)",
+     "basis.derivative(N-2, 1.)*basis.value(0, 0.)"),
+    # odd n, add_into, stride != 1: the middle entry of the summand must be
+    # read at mid * stride (as the transposed branch at :159 does); only the
+    # precomputed Laplacian's y mass product takes this branch
+    ("matrix_vector_kernel.h", 86, "array_for_add[mid] +", "array_for_add[mid * stride] +"),
 ]
 
 

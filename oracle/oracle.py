@@ -71,6 +71,9 @@ def lib():
         for f in ("sfo_dg_sipg_apply", "sfo_dg_advect_apply", "sfo_dg_advect_apply_transpose"):
             getattr(L, f).argtypes = [C.POINTER(DG), _dp, _dp]
         L.sfo_dg_sipg_diagonal.argtypes = [C.POINTER(DG), _dp]
+        L.sfo_dg_precomputed_apply.argtypes = [C.POINTER(DG), _dp, _dp]
+        L.sfo_dg_precomputed_diagonal.argtypes = [C.POINTER(DG), _dp]
+        L.sfo_dg_precomputed_matrices.argtypes = [C.c_int, _dp, _dp, _dp]
         L.sfo_dg_rk_stage.argtypes = [C.POINTER(DG), _dp, _dp, _dp, _dp, C.c_double, C.c_double]
         L.sfo_dg_lsrk_step.argtypes = [C.POINTER(DG), C.c_double, _dp, _dp, _dp]
         L.sfo_chebyshev_update.argtypes = [C.c_longlong, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -205,6 +208,23 @@ def dg_advect_apply(g, x):
 
 def dg_advect_apply_transpose(g, x):
     return _dg_call("sfo_dg_advect_apply_transpose", g, x)
+
+
+def dg_precomputed_apply(g, x):
+    return _dg_call("sfo_dg_precomputed_apply", g, x)
+
+
+def dg_precomputed_diagonal(g):
+    d = np.zeros(dg_n_dofs(g))
+    lib().sfo_dg_precomputed_diagonal(C.byref(g), d)
+    return d
+
+
+def dg_precomputed_matrices(degree):
+    n = degree + 1
+    M, L, iv = np.zeros(n * n), np.zeros(n * n), np.zeros(2)
+    lib().sfo_dg_precomputed_matrices(degree, M, L, iv)
+    return M.reshape(n, n), L.reshape(n, n), iv
 
 
 def dg_rk_stage(g, src, upd, vec_np, vec_tm, c_np, c_tm):

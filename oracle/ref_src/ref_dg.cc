@@ -7,6 +7,7 @@
 #include "ref_shim.h"
 #include "evaluation_dg_laplacian.h"
 #include "evaluation_dg_advect.h"
+#include "precomputed_dg_laplacian.h"
 
 template <typename Ev>
 static void set_geometry(Ev &ev, const double *h)
@@ -92,6 +93,21 @@ static void time_steps(const int *nc, const double *h, int nsteps, double dt, do
   for (std::size_t i = 0; i < N; ++i) x[i] = ev.sol_new[i];
 }
 
+/* y = A x of the tensor-product SIPG Laplacian with precomputed 1D matrices
+ * (unit Cartesian cells, periodic) */
+template <int p>
+static void precomputed(const int *nc, const double *x, double *y)
+{
+  PrecomputedDGLaplacian<3, p, double> ev;
+  ev.blx = 2; ev.bly = 2; ev.blz = 2;
+  unsigned int n_cells[3] = {(unsigned)nc[0], (unsigned)nc[1], (unsigned)nc[2]};
+  ev.initialize(n_cells);
+  const std::size_t N = ev.n_elements() * ev.dofs_per_cell;
+  for (std::size_t i = 0; i < N; ++i) ev.input_array[i] = x[i];
+  ev.matrix_vector_product();
+  for (std::size_t i = 0; i < N; ++i) y[i] = ev.output_array[i];
+}
+
 template <int p>
 static void face_tables(double *face_eo, double *Sinv_eo)
 {
@@ -137,3 +153,6 @@ extern "C" int sfref_dg_rk_stage(int degree, const int *nc, const double *h, con
 extern "C" int sfref_dg_time_steps(int degree, const int *nc, const double *h, int nsteps,
                                    double dt, double *x)
 { SF_DISPATCH(time_steps, nc, h, nsteps, dt, x) }
+
+extern "C" int sfref_dg_precomputed(int degree, const int *nc, const double *x, double *y)
+{ SF_DISPATCH(precomputed, nc, x, y) }

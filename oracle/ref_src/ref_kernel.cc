@@ -39,6 +39,7 @@ static int dispatch_nn(int type, int cor, int add, int do_dg, const double *coef
   R(0, 1, 0, 0) R(0, 0, 0, 0) R(0, 1, 1, 0) R(0, 0, 1, 0)
   R(1, 1, 0, 0) R(1, 0, 0, 0) R(1, 1, 1, 0) R(1, 0, 1, 0)
   R(1, 1, 0, 1) R(1, 0, 0, 1) R(1, 1, 0, 2) R(1, 0, 0, 2) R(1, 0, 1, 2)
+  R(2, 1, 0, 0) R(2, 1, 1, 0)
 #undef R
   return -1;
 }

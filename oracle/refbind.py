@@ -161,6 +161,17 @@ def dg_time_steps(degree, n_cells, h, x, nsteps, dt):
     return y
 
 
+def dg_precomputed(degree, n_cells, x):
+    """the reference's PrecomputedDGLaplacian::matrix_vector_product (unit cells)"""
+    L = _lib("ref_dg")
+    L.sfref_dg_precomputed.argtypes = [C.c_int, _ip, _dp, _dp]
+    y = np.zeros(len(x))
+    rc = L.sfref_dg_precomputed(degree, np.array(n_cells, dtype=np.int32),
+                                np.ascontiguousarray(x, dtype=np.float64), y)
+    assert rc == 0
+    return y
+
+
 def dg_tables(degree):
     L = _lib("ref_dg")
     L.sfref_dg_tables.argtypes = [C.c_int, _dp, _dp]

@@ -1275,6 +1275,122 @@ void sfo_dg_advect_apply(const sfo_dg *g, const double *x, double *y)
   }
 }
 
+/* 1D matrices of precomputed_dg_laplacian.h:307-377 (fill_shape_values),
+ * formed from the Hermite-like values S and collocation derivatives D at the
+ * Gauss points (exact for the degree-p basis), with the corrected
+ * neighbour couplings */
+void sfo_dg_precomputed_matrices(int degree, double *M, double *L, double *iv)
+{
+  sfo_shape s;
+  sfo_shape_init(degree, SFO_BASIS_HERMITE, &s);
+  const int n = s.n;
+  double v0[SFO_MAX_N], v1[SFO_MAX_N], d0[SFO_MAX_N], d1[SFO_MAX_N], dq[SFO_MAX_N * SFO_MAX_N];
+  for (int i = 0; i < n; ++i) {
+    v0[i] = v1[i] = d0[i] = d1[i] = 0.0;
+    for (int q = 0; q < n; ++q) {
+      v0[i] += s.face_v[0][q] * s.S[q * n + i];
+      v1[i] += s.face_v[1][q] * s.S[q * n + i];
+      d0[i] += s.face_d[0][q] * s.S[q * n + i];
+      d1[i] += s.face_d[1][q] * s.S[q * n + i];
+      double t = 0.0;
+      for (int j = 0; j < n; ++j) t += s.D[q * n + j] * s.S[j * n + i];
+      dq[q * n + i] = t;
+    }
+  }
+  const double pen = (double)degree * (degree + 1);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double m = 0.0, l = 0.0;
+      for (int q = 0; q < n; ++q) {
+        m += s.wq[q] * s.S[q * n + i] * s.S[q * n + j];
+        l += s.wq[q] * dq[q * n + i] * dq[q * n + j];
+      }
+      l += pen * v0[i] * v0[j] + 0.5 * d0[i] * v0[j] + 0.5 * d0[j] * v0[i];
+      l += pen * v1[i] * v1[j] - 0.5 * d1[i] * v1[j] - 0.5 * d1[j] * v1[i];
+      M[i * n + j] = m;
+      L[i * n + j] = l;
+    }
+  iv[0] = -pen * v0[0] * v1[n - 1] - 0.5 * d0[0] * v1[n - 1] + 0.5 * d1[n - 1] * v0[0];
+  iv[1] = -pen * v0[0] * v1[n - 2] - 0.5 * d0[0] * v1[n - 2] + 0.5 * d1[n - 2] * v0[0];
+}
+
+/* out += c * A along direction dir of an n^3 cell block (x fastest) */
+static void block_matvec(int n, const double *A, int dir, double c, const double *in, double *out)
+{
+  const int st = dir == 0 ? 1 : (dir == 1 ? n : n * n);
+  for (int k = 0; k < n * n; ++k) {
+    const int base = dir == 0 ? k * n : (dir == 1 ? (k % n) + (k / n) * n * n : k);
+    for (int i = 0; i < n; ++i) {
+      double t = 0.0;
+      for (int j = 0; j < n; ++j) t += A[i * n + j] * in[base + j * st];
+      out[base + i * st] += c * t;
+    }
+  }
+}
+
+void sfo_dg_precomputed_apply(const sfo_dg *g, const double *x, double *y)
+{
+  const int n = g->degree + 1, dpc = n * n * n;
+  double M[SFO_MAX_N * SFO_MAX_N], L[SFO_MAX_N * SFO_MAX_N], iv[2];
+  sfo_dg_precomputed_matrices(g->degree, M, L, iv);
+  const int nx = g->n_cells[0], ny = g->n_cells[1], nz = g->n_cells[2];
+  const long long C = (long long)nx * ny * nz;
+  const double vol = g->h[0] * g->h[1] * g->h[2];
+#pragma omp parallel for schedule(static)
+  for (long long c = 0; c < C; ++c) {
+    const int ix = (int)(c % nx), iy = (int)((c / nx) % ny), iz = (int)(c / ((long long)nx * ny));
+    const int ic[3] = {ix, iy, iz}, ncs[3] = {nx, ny, nz};
+    const double *u = x + c * dpc;
+    double t[1000], t2[1000], t3[1000];
+    double *out = y + c * dpc;
+    for (int q = 0; q < dpc; ++q) out[q] = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      const int st = d == 0 ? 1 : (d == 1 ? n : n * n);
+      int jl[3] = {ix, iy, iz}, jr[3] = {ix, iy, iz};
+      jl[d] = ic[d] == 0 ? ncs[d] - 1 : ic[d] - 1;
+      jr[d] = ic[d] == ncs[d] - 1 ? 0 : ic[d] + 1;
+      const double *ul = x + (((long long)jl[2] * ny + jl[1]) * nx + jl[0]) * dpc;
+      const double *ur = x + (((long long)jr[2] * ny + jr[1]) * nx + jr[0]) * dpc;
+      for (int q = 0; q < dpc; ++q) t[q] = 0.0;
+      block_matvec(n, L, d, 1.0, u, t);
+      /* neighbour layers: lines along d, base index without the d coordinate */
+      for (int k = 0; k < n * n; ++k) {
+        const int base = d == 0 ? k * n : (d == 1 ? (k % n) + (k / n) * n * n : k);
+        t[base] += iv[0] * ul[base + (n - 1) * st] + iv[1] * ul[base + (n - 2) * st];
+        t[base + st] += iv[1] * ul[base + (n - 1) * st];
+        t[base + (n - 1) * st] += iv[0] * ur[base] + iv[1] * ur[base + st];
+        t[base + (n - 2) * st] += iv[1] * ur[base];
+      }
+      /* mass matrices in the two other directions */
+      const int e = (d + 1) % 3, f = (d + 2) % 3;
+      for (int q = 0; q < dpc; ++q) t2[q] = 0.0;
+      block_matvec(n, M, e, 1.0, t, t2);
+      for (int q = 0; q < dpc; ++q) t3[q] = 0.0;
+      block_matvec(n, M, f, 1.0, t2, t3);
+      const double cd = vol / (g->h[d] * g->h[d]);
+      for (int q = 0; q < dpc; ++q) out[q] += cd * t3[q];
+    }
+  }
+}
+
+void sfo_dg_precomputed_diagonal(const sfo_dg *g, double *diag)
+{
+  const int n = g->degree + 1, dpc = n * n * n;
+  double M[SFO_MAX_N * SFO_MAX_N], L[SFO_MAX_N * SFO_MAX_N], iv[2];
+  sfo_dg_precomputed_matrices(g->degree, M, L, iv);
+  const double vol = g->h[0] * g->h[1] * g->h[2];
+  const double c[3] = {vol / (g->h[0] * g->h[0]), vol / (g->h[1] * g->h[1]), vol / (g->h[2] * g->h[2])};
+  const long long C = (long long)g->n_cells[0] * g->n_cells[1] * g->n_cells[2];
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const double v = c[0] * L[i * n + i] * M[j * n + j] * M[k * n + k] +
+                         c[1] * M[i * n + i] * L[j * n + j] * M[k * n + k] +
+                         c[2] * M[i * n + i] * M[j * n + j] * L[k * n + k];
+        for (long long cc = 0; cc < C; ++cc) diag[cc * dpc + (k * n + j) * n + i] = v;
+      }
+}
+
 void sfo_dg_rk_stage(const sfo_dg *g, const double *src, const double *upd,
                      double *vec_np, double *vec_tm, double c_np, double c_tm)
 {

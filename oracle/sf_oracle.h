@@ -123,6 +123,17 @@ void sfo_dg_rk_stage(const sfo_dg *g, const double *src, const double *upd,
 void sfo_dg_lsrk_step(const sfo_dg *g, double dt, double *sol_new, double *sol_old,
                       double *sol_tmp);
 
+/* tensor-product SIPG Laplacian with precomputed 1D matrices
+ * (precomputed_dg_laplacian.h:96-377), Hermite-like basis, periodic:
+ *   A = sum_d c_d (L (+) couplings)_d x M x M,  c_d = hx hy hz / h_d^2
+ * (c_d = 1 on the reference's unit cells).  M: 1D mass, L: 1D stiffness
+ * with the own-face SIPG terms, penalty p(p+1); iv[0], iv[1]: couplings of
+ * the end nodes with the neighbour's two nearest node layers (the reference
+ * evaluates them at swapped face points, which makes them vanish). */
+void sfo_dg_precomputed_matrices(int degree, double *M, double *L, double *iv);
+void sfo_dg_precomputed_apply(const sfo_dg *g, const double *x, double *y);
+void sfo_dg_precomputed_diagonal(const sfo_dg *g, double *diag);
+
 /* ---------------- vector kernels ---------------- */
 void sfo_chebyshev_update(long long n, const double *ax, const double *b,
                           const double *diag_inv, const double *x_old,

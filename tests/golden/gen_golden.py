@@ -198,13 +198,31 @@ def rk_fixtures():
     np.savez(os.path.join(HERE, "dg_rk.npz"), **out)
 
 
+def precomputed_fixtures():
+    """the reference's PrecomputedDGLaplacian on unit cells (periodic), with
+    the neighbour-coupling and odd-n add-into lines patched (oracle/build.py
+    PATCHES); inputs stored in FP32 to keep the file small"""
+    rng = np.random.default_rng(20241208)
+    out = {}
+    for p in (1, 2, 3, 4, 5, 6, 8):
+        nc = (3, 2, 2) if p <= 4 else (2, 2, 2)
+        N = nc[0] * nc[1] * nc[2] * (p + 1) ** 3
+        x = rng.uniform(-1, 1, N).astype(np.float32)
+        out["x_%d" % p], out["y_%d" % p] = x, R.dg_precomputed(p, nc, x.astype(np.float64))
+        out["nc_%d" % p] = np.array(nc)
+    np.savez(os.path.join(HERE, "dg_precomputed.npz"), **out)
+
+
 if __name__ == "__main__":
     import sys
     if sys.argv[1:] == ["rk"]:
         rk_fixtures()
+    elif sys.argv[1:] == ["precomputed"]:
+        precomputed_fixtures()
     else:
         main()
         rk_fixtures()
+        precomputed_fixtures()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

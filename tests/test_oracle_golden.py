@@ -165,3 +165,13 @@ def test_dg_lsrk_steps(golden, p):
     for _ in range(3):
         O.dg_lsrk_step(d, float(g["dt_%d" % p]), x, old, tmp)
     assert rel(x, g["steps3_%d" % p]) < 1e-13
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6, 8])
+def test_dg_precomputed(golden, p):
+    """tensor-product SIPG with precomputed 1D matrices against the
+    reference's PrecomputedDGLaplacian (unit cells)"""
+    g = golden("dg_precomputed.npz")
+    d = O.dg(p, tuple(int(v) for v in g["nc_%d" % p]), (1.0, 1.0, 1.0))
+    y = O.dg_precomputed_apply(d, g["x_%d" % p].astype(np.float64))
+    assert rel(y, g["y_%d" % p]) < 1e-14

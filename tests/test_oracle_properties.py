@@ -122,3 +122,21 @@ def test_fast_division_formula():
         for n in ns + [d - 1, d, d + 1, 2 * d - 1, 2 * d]:
             n &= 2 ** 32 - 1
             assert (m * n) >> 64 == n // d
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_precomputed_sipg_matrix_properties(p):
+    """symmetric, positive semi-definite with the constants as null space,
+    diagonal equal to the assembled one, uniform scaling h -> s h scales the
+    operator by s (anisotropic cells)"""
+    d = O.dg(p, (3, 2, 2), (0.5, 0.8, 0.3))
+    n = O.dg_n_dofs(d)
+    A = dense(lambda x: O.dg_precomputed_apply(d, x), n)
+    assert np.abs(A - A.T).max() < 1e-12 * np.abs(A).max()
+    ev = np.linalg.eigvalsh(0.5 * (A + A.T))
+    assert ev.min() > -1e-10 * ev.max()
+    assert np.abs(A @ np.ones(n)).max() < 1e-12 * np.abs(A).max()
+    assert np.abs(np.diag(A) - O.dg_precomputed_diagonal(d)).max() < 1e-12 * np.abs(A).max()
+    d2 = O.dg(p, (3, 2, 2), (1.5, 2.4, 0.9))
+    x = np.random.default_rng(p).uniform(-1, 1, n)
+    assert np.abs(O.dg_precomputed_apply(d2, x) - 3.0 * A @ x).max() < 1e-12 * np.abs(A @ x).max() * 3
