@@ -61,7 +61,12 @@ typedef enum { SF_FP64 = 0, SF_FP32 = 1 } sf_prec;
 typedef enum {
   SF_OP_LAPLACE = 0,   /* continuous FE Laplacian -div(kappa grad u)           */
   SF_OP_DG_SIPG = 1,   /* DG symmetric interior penalty Laplacian, periodic     */
-  SF_OP_DG_ADVECT = 2  /* DG upwind advection, periodic                        */
+  SF_OP_DG_ADVECT = 2, /* DG upwind advection, periodic                        */
+  SF_OP_DG_PRECOMPUTED = 3 /* DG SIPG Laplacian in tensor-product form with
+                          precomputed 1D mass and stiffness matrices, Hermite-
+                          like basis, penalty p(p+1), periodic; replaces
+                          PrecomputedDGLaplacian (precomputed_dg_laplacian.h:
+                          44-377): sf_vmult = matrix_vector_product() */
 } sf_op_kind;
 
 typedef enum { SF_BASIS_GLL = 0, SF_BASIS_HERMITE = 1 } sf_basis;
@@ -71,7 +76,8 @@ typedef struct {
   int degree;          /* 1..8                                                  */
   int n_cells[3];      /* hexahedral cells per direction                        */
   double length[3];    /* domain [0,Lx]x[0,Ly]x[0,Lz]                           */
-  int basis;           /* SF_OP_LAPLACE only (DG SIPG: Hermite-like, DG advect: GLL) */
+  int basis;           /* SF_OP_LAPLACE only (DG SIPG and precomputed:
+                          Hermite-like, DG advect: GLL)                         */
   double deform;       /* SF_OP_LAPLACE: amplitude a of the mapping
                           x_i <- x_i + a sin(2 pi x_j) sin(2 pi x_k), (i,j,k)
                           cyclic; 0 = affine (geometry not stored)            */

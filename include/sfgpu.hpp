@@ -234,6 +234,41 @@ private:
   Operator op_;
 };
 
+// DG SIPG Laplacian in tensor-product form with precomputed 1D matrices
+// (precomputed_dg_laplacian.h:33-391): unit cells unless lengths are given.
+template <int degree, typename Number>
+class PrecomputedDGLaplacian {
+public:
+  static constexpr unsigned int dimension = 3;
+  static constexpr unsigned int dofs_per_cell = (degree + 1) * (degree + 1) * (degree + 1);
+  unsigned int blx = 0, bly = 0, blz = 0;
+
+  // precomputed_dg_laplacian.h:44-82: input_array = 1, output_array = 0
+  void initialize(const unsigned *n_cells, const double *length = nullptr)
+  {
+    double unit[3] = {double(n_cells[0]), double(n_cells[1]), double(n_cells[2])};
+    sf_desc d = make_desc(SF_OP_DG_PRECOMPUTED, degree, n_cells, length ? length : unit);
+    op_ = Operator(d);
+    const std::size_t n = (std::size_t)op_.n_dofs();
+    input_array.resize(n);
+    output_array.resize(n);
+    input_array.fill(Number(1));
+    output_array.fill(Number(0));
+  }
+  std::size_t n_elements() const { return input_array.size() / dofs_per_cell; }
+  // precomputed_dg_laplacian.h:279-305: output_array = A input_array
+  void matrix_vector_product(cudaStream_t s = 0)
+  {
+    check(sf_vmult(op_.get(), precision_of<Number>(), input_array.begin(), output_array.begin(), s));
+  }
+  const Operator &op() const { return op_; }
+
+  DeviceVector<Number> input_array, output_array;
+
+private:
+  Operator op_;
+};
+
 // DG upwind advection on the periodic box [0,2]^3 (evaluation_dg_advect.h:96-845).
 template <int degree, typename Number>
 class EvaluationDGAdvection {

@@ -125,7 +125,7 @@ int sf_create(const sf_desc *desc, sf_op **out)
   if (!desc || !out) return fail(SF_ERR_NULL, "desc/op is NULL");
   *out = nullptr;
   const sf_desc &d = *desc;
-  if (d.kind < SF_OP_LAPLACE || d.kind > SF_OP_DG_ADVECT) return fail(SF_ERR_INVALID, "unknown operator kind");
+  if (d.kind < SF_OP_LAPLACE || d.kind > SF_OP_DG_PRECOMPUTED) return fail(SF_ERR_INVALID, "unknown operator kind");
   if (d.degree < 1 || d.degree > kMaxDegree) return fail(SF_ERR_UNSUPPORTED, "degree must be 1..8");
   for (int k = 0; k < 3; ++k) {
     if (d.n_cells[k] < 1 || d.n_cells[k] > (1 << 20)) return fail(SF_ERR_INVALID, "n_cells out of range");
@@ -140,7 +140,8 @@ int sf_create(const sf_desc *desc, sf_op **out)
   sf_op *op = new (std::nothrow) sf_op();
   if (!op) return fail(SF_ERR_OOM, "host allocation failed");
   op->desc = d;
-  const int basis = d.kind == SF_OP_LAPLACE ? d.basis : (d.kind == SF_OP_DG_SIPG ? SF_BASIS_HERMITE : SF_BASIS_GLL);
+  const int basis = d.kind == SF_OP_LAPLACE ? d.basis
+                    : (d.kind == SF_OP_DG_ADVECT ? SF_BASIS_GLL : SF_BASIS_HERMITE);
   op->desc.basis = basis;
   fill_shape(d.degree, basis, op->shape);
   op->n = d.degree + 1;
@@ -271,6 +272,8 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
   if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
   if (op->desc.kind == SF_OP_LAPLACE) return launch_cont_vmult(op, prec, x, y, st);
+  if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
+    return launch_dg_precomputed(op, prec, 1, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
   return launch_dg_vmult(op, prec, 1, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
 }
 
@@ -297,6 +300,8 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
                                (char *)y + r * op->n_dofs * es, st));
     return SF_OK;
   }
+  if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
+    return launch_dg_precomputed(op, prec, nrhs, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
   return launch_dg_vmult(op, prec, nrhs, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
 }
 
@@ -334,6 +339,8 @@ int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv, 
   cudaStream_t st = (cudaStream_t)stream;
   if (op->desc.kind == SF_OP_DG_SIPG || op->desc.kind == SF_OP_DG_ADVECT)
     return launch_dg_vmult(op, prec, 1, false, x_old, x_new, b, diag_inv, t, c_np, c_tm, st);
+  if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
+    return launch_dg_precomputed(op, prec, 1, x_old, x_new, b, diag_inv, t, c_np, c_tm, st);
   // continuous: operator into x_new, then the fused vector update in place
   SF_RET(launch_cont_vmult(op, prec, x_old, x_new, st));
   return launch_vector_update(op->n_dofs, prec, x_new, b, diag_inv, x_old, x_new, t, c_np, c_tm, st);
@@ -404,6 +411,8 @@ int sf_diagonal(sf_op *op, int prec, void *diag, void *stream)
   SF_RET(check_prec(op, prec));
   SF_RET(check_ptr(diag, prec, "diag"));
   if (op->desc.kind == SF_OP_LAPLACE) return launch_cont_diagonal(op, prec, diag, (cudaStream_t)stream);
+  if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
+    return launch_dg_precomputed_diagonal(op, prec, diag, (cudaStream_t)stream);
   return launch_dg_diagonal(op, prec, diag, (cudaStream_t)stream);
 }
 

@@ -21,6 +21,7 @@
 // line, so the face fluxes are computed in the thread that holds the
 // matching line.
 #include "sf_device.cuh"
+#include "sf_dg_common.cuh"
 #include "sf_internal.h"
 #include "sf_launch.h"
 #include "sf_tables.h"
@@ -63,22 +64,11 @@ struct DGArgs {
   long long n_cells, n_dofs;
 };
 
-template <int N>
-struct DGCells {
-  // cells per block, about 128-256 threads
-  static constexpr int value = N == 2 ? 32 : N == 3 ? 14 : N == 4 ? 8 : N == 5 ? 5 : N == 6 ? 7
-                               : N == 7 ? 5 : N == 8 ? 2 : 3;
-};
 
-// periodic neighbour of the cell (ix, iy, iz) across face `side` of
-// direction `dir` (no division: a +-1 step with wrap-around)
 template <int N, typename T>
 __device__ __forceinline__ long long neighbour(const DGArgs<N, T> &A, int ix, int iy, int iz, int dir, int side)
 {
-  if (dir == 0) ix = side ? (ix + 1 == A.nc[0] ? 0 : ix + 1) : (ix == 0 ? A.nc[0] - 1 : ix - 1);
-  if (dir == 1) iy = side ? (iy + 1 == A.nc[1] ? 0 : iy + 1) : (iy == 0 ? A.nc[1] - 1 : iy - 1);
-  if (dir == 2) iz = side ? (iz + 1 == A.nc[2] ? 0 : iz + 1) : (iz == 0 ? A.nc[2] - 1 : iz - 1);
-  return ((long long)iz * A.nc[1] + iy) * A.nc[0] + ix;
+  return periodic_neighbour(A.nc, ix, iy, iz, dir, side);
 }
 
 // face flux at one face point.  side 0: face at coordinate 0 (outer normal
@@ -151,34 +141,6 @@ __device__ __forceinline__ void line_residual(const DGArgs<N, T> &A, int d, cons
       r[m] = fma(A.fd1[m], fdp, r[m]);
     }
   }
-}
-
-// Shared-memory layout of the DG kernels: per cell three slabs with index
-// (a, b, c) = a + P1 b + P2 c and a per-cell skew, chosen from a
-// bank-conflict model of the three sweep patterns over the lanes of each
-// warp (a block holds CPB consecutive cells, cell-major lanes).
-struct DGLayout {
-  int P1, P2, SKEW;
-};
-
-constexpr DGLayout dg_layout(int n, int elem)
-{
-  return elem == 4 ? (n == 2   ? DGLayout{2, 5, 6}
-                      : n == 3 ? DGLayout{3, 9, 10}
-                      : n == 4 ? DGLayout{4, 19, 12}
-                      : n == 5 ? DGLayout{5, 25, 2}
-                      : n == 6 ? DGLayout{7, 42, 8}
-                      : n == 7 ? DGLayout{7, 56, 25}
-                      : n == 8 ? DGLayout{9, 72, 0}
-                               : DGLayout{9, 81, 6})
-                   : (n == 2   ? DGLayout{2, 5, 6}
-                      : n == 3 ? DGLayout{3, 18, 7}
-                      : n == 4 ? DGLayout{4, 19, 0}
-                      : n == 5 ? DGLayout{5, 25, 2}
-                      : n == 6 ? DGLayout{9, 54, 8}
-                      : n == 7 ? DGLayout{7, 49, 12}
-                      : n == 8 ? DGLayout{9, 72, 0}
-                               : DGLayout{9, 81, 6});
 }
 
 template <int N, typename T>

@@ -1,0 +1,370 @@
+// sf_dg_precomputed.cu -- DG SIPG Laplacian in tensor-product form with
+// precomputed 1D matrices (the reference's PrecomputedDGLaplacian,
+// precomputed_dg_laplacian.h:96-377), Hermite-like basis, periodic
+// Cartesian mesh:
+//
+//   A = sum_d c_d (L + couplings)_d (x) M (x) M,   c_d = hx hy hz / h_d^2,
+//
+// M the 1D mass matrix, L the 1D stiffness matrix with the own-face SIPG
+// terms (penalty p(p+1), reference coordinates), and two coefficients iv0,
+// iv1 coupling the end nodes with the neighbour's two nearest node layers
+// (a Hermite-like end value and normal derivative live on two layers).  On
+// unit cells c_d = 1 and A is the reference's operator; the reference
+// evaluates iv0 and iv1 at swapped face points (which makes them vanish),
+// this library uses the couplings of the SIPG bilinear form.
+//
+// GPU mapping as in sf_dg.cu: CPB consecutive cells per block, n^2 threads
+// per cell, z columns read and written straight from the cell-major vector,
+// three padded slabs per cell.  Five phases, four block barriers:
+//   z:  X = x;  Az = c_z (L_z x + z couplings)
+//   x:  B  = c_x (L_x x + x couplings);        Az = M_x Az
+//   y:  B  = M_y B;  Az = M_y Az;   X = c_y (L_y x + y couplings)
+//   x:  B += M_x X
+//   z:  y = M_z B + Az                       (or the fused Chebyshev step)
+#include "sf_device.cuh"
+#include "sf_dg_common.cuh"
+#include "sf_internal.h"
+#include "sf_launch.h"
+#include "sf_tables.h"
+
+namespace sf {
+
+namespace {
+
+template <int N, typename T>
+struct PDGArgs {
+  EOMat<N, T> M, L;        // symmetric and centro-symmetric 1D matrices
+  T iv0, iv1;              // neighbour couplings
+  T c[3];                  // hx hy hz / h_d^2
+  const T *__restrict__ x;
+  T *__restrict__ y;
+  const T *__restrict__ cb;      // Chebyshev: rhs
+  const T *__restrict__ cdinv;   // Chebyshev: inverse diagonal
+  T *__restrict__ ct;            // Chebyshev: t
+  T c_np, c_tm;
+  int nc[3];
+  FastDiv div_nx, div_ny;
+  long long n_cells, n_dofs;
+};
+
+template <int N, typename T>
+struct PDGCfg {
+  static constexpr int CPB = DGCells<N>::value;
+  static constexpr DGLayout L = dg_layout(N, (int)sizeof(T));
+  static constexpr int P1 = L.P1, P2 = L.P2;
+  static constexpr int SLAB = P2 * N;
+  static constexpr int RS = 3 * SLAB + L.SKEW;
+  static constexpr size_t SMEM = size_t(CPB) * RS * sizeof(T);
+};
+
+// line residual of the 1D operator L plus the couplings with the two
+// neighbours' end layers: lo1, lo2 = left neighbour's nodes n-1, n-2 of this
+// line, hi1, hi2 = right neighbour's nodes 0, 1
+template <int N, typename T>
+__device__ __forceinline__ void stiffness_line(const PDGArgs<N, T> &A, const T (&v)[N], T lo1, T lo2, T hi1,
+                                               T hi2, T scale, T (&r)[N])
+{
+  eo_apply<N, 1>(A.L, v, r);
+  r[0] += A.iv0 * lo1 + A.iv1 * lo2;
+  r[1] += A.iv1 * lo1;
+  r[N - 1] += A.iv0 * hi1 + A.iv1 * hi2;
+  r[N - 2] += A.iv1 * hi1;
+#pragma unroll
+  for (int m = 0; m < N; ++m) r[m] *= scale;
+}
+
+template <int N, typename T, bool CHEB>
+__global__ void __launch_bounds__(DGCells<N>::value *N *N)
+    dg_precomputed_kernel(const __grid_constant__ PDGArgs<N, T> A)
+{
+  using Cfg = PDGCfg<N, T>;
+  constexpr int N2 = N * N, N3 = N * N * N;
+  constexpr int CPB = Cfg::CPB, P1 = Cfg::P1, P2 = Cfg::P2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *smem = reinterpret_cast<T *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int cs = tid / N2;
+  const int t = tid - cs * N2;
+  const int a = t % N, b = t / N;
+  const long long cell = (long long)blockIdx.x * CPB + cs;
+  const bool valid = cell < A.n_cells;
+  T *X = smem + cs * Cfg::RS;
+  T *Az = X + Cfg::SLAB, *B = Az + Cfg::SLAB;
+  const int zc = a + P1 * b;      // z column (a, b)
+  const int xl = P1 * a + P2 * b; // x line (y=a, z=b), stride 1
+  const int yl = a + P2 * b;      // y line (x=a, z=b), stride P1
+  const long long col = cell * N3 + t;
+  const long long roff = (long long)blockIdx.y * A.n_dofs; // right-hand side offset
+  const T *__restrict__ x = A.x + roff;
+
+  // neighbour cells (periodic) in the three directions
+  long long nb[3][2] = {{cell, cell}, {cell, cell}, {cell, cell}};
+  if (valid) {
+    const unsigned uc = (unsigned)cell;
+    const unsigned q = fast_div(uc, A.div_nx);
+    const unsigned iz = fast_div(q, A.div_ny);
+    const int ix = int(uc - q * (unsigned)A.nc[0]), iy = int(q - iz * (unsigned)A.nc[1]);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      nb[d][0] = periodic_neighbour(A.nc, ix, iy, int(iz), d, 0);
+      nb[d][1] = periodic_neighbour(A.nc, ix, iy, int(iz), d, 1);
+    }
+  }
+  T v[N], r[N];
+  // ---- z: the z column of x; z stiffness with couplings ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = valid ? __ldg(x + col + N2 * m) : T(0);
+#pragma unroll
+  for (int m = 0; m < N; ++m) X[zc + P2 * m] = v[m];
+  {
+    T lo1 = T(0), lo2 = T(0), hi1 = T(0), hi2 = T(0);
+    if (valid) {
+      const T *xl_ = x + nb[2][0] * N3 + t, *xr_ = x + nb[2][1] * N3 + t;
+      lo1 = __ldg(xl_ + N2 * (N - 1));
+      lo2 = __ldg(xl_ + N2 * (N - 2));
+      hi1 = __ldg(xr_);
+      hi2 = __ldg(xr_ + N2);
+    }
+    stiffness_line<N, T>(A, v, lo1, lo2, hi1, hi2, A.c[2], r);
+  }
+#pragma unroll
+  for (int m = 0; m < N; ++m) Az[zc + P2 * m] = r[m];
+  __syncthreads();
+  // ---- x: x stiffness with couplings into B; mass along x of Az ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = X[xl + m];
+  {
+    // x line (y=a, z=b): node (m, a, b) at m + N a + N2 b
+    T lo1 = T(0), lo2 = T(0), hi1 = T(0), hi2 = T(0);
+    if (valid) {
+      const T *xl_ = x + nb[0][0] * N3 + N * a + N2 * b, *xr_ = x + nb[0][1] * N3 + N * a + N2 * b;
+      lo1 = __ldg(xl_ + (N - 1));
+      lo2 = __ldg(xl_ + (N - 2));
+      hi1 = __ldg(xr_);
+      hi2 = __ldg(xr_ + 1);
+    }
+    stiffness_line<N, T>(A, v, lo1, lo2, hi1, hi2, A.c[0], r);
+  }
+#pragma unroll
+  for (int m = 0; m < N; ++m) B[xl + m] = r[m];
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = Az[xl + m];
+  eo_apply<N, 1>(A.M, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) Az[xl + m] = v[m];
+  __syncthreads();
+  // ---- y: mass along y of B and Az; y stiffness with couplings into X ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B[yl + P1 * m];
+  eo_apply<N, 1>(A.M, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B[yl + P1 * m] = v[m];
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = Az[yl + P1 * m];
+  eo_apply<N, 1>(A.M, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) Az[yl + P1 * m] = v[m];
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = X[yl + P1 * m];
+  {
+    // y line (x=a, z=b): node (a, m, b) at a + N m + N2 b
+    T lo1 = T(0), lo2 = T(0), hi1 = T(0), hi2 = T(0);
+    if (valid) {
+      const T *xl_ = x + nb[1][0] * N3 + a + N2 * b, *xr_ = x + nb[1][1] * N3 + a + N2 * b;
+      lo1 = __ldg(xl_ + N * (N - 1));
+      lo2 = __ldg(xl_ + N * (N - 2));
+      hi1 = __ldg(xr_);
+      hi2 = __ldg(xr_ + N);
+    }
+    stiffness_line<N, T>(A, v, lo1, lo2, hi1, hi2, A.c[1], r);
+  }
+#pragma unroll
+  for (int m = 0; m < N; ++m) X[yl + P1 * m] = r[m];
+  __syncthreads();
+  // ---- x: B += M_x X ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = X[xl + m];
+  eo_apply<N, 1>(A.M, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) B[xl + m] += v[m];
+  __syncthreads();
+  // ---- z: y = M_z B + Az ----
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] = B[zc + P2 * m];
+  eo_apply<N, 1>(A.M, v, v);
+#pragma unroll
+  for (int m = 0; m < N; ++m) v[m] += Az[zc + P2 * m];
+  if (valid) {
+    T *dst = A.y + roff + col;
+    if (CHEB) {
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        const long long e = col + N2 * m;
+        const T res = v[m] - A.cb[e];
+        const T tn = A.c_tm * A.ct[e] + A.c_np * A.cdinv[e] * res;
+        A.ct[e] = tn;
+        dst[N2 * m] = __ldg(x + e) - tn;
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < N; ++m) dst[N2 * m] = v[m];
+    }
+  }
+}
+
+// fill a vector with a per-cell pattern of n^3 values
+template <typename T>
+__global__ void precomputed_pattern_kernel(long long n, int n3, const T *__restrict__ pat, T *__restrict__ y)
+{
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = pat[i % n3];
+}
+
+// 1D matrices in FP64 from the Hermite-like tables: values and collocation
+// derivatives at the Gauss points, Gauss-Lagrange extrapolation to the faces
+// (exact for the degree-p basis); fill_shape_values of
+// precomputed_dg_laplacian.h:307-377 with the SIPG couplings
+struct Matrices1D {
+  double M[kMaxN][kMaxN], L[kMaxN][kMaxN], iv0, iv1;
+};
+
+Matrices1D precomputed_matrices(const Shape1D &s)
+{
+  const int n = s.n;
+  Matrices1D R{};
+  double v0[kMaxN], v1[kMaxN], d0[kMaxN], d1[kMaxN], dq[kMaxN][kMaxN];
+  for (int i = 0; i < n; ++i) {
+    v0[i] = v1[i] = d0[i] = d1[i] = 0.0;
+    for (int q = 0; q < n; ++q) {
+      v0[i] += s.fv[0][q] * s.S[q][i];
+      v1[i] += s.fv[1][q] * s.S[q][i];
+      d0[i] += s.fd[0][q] * s.S[q][i];
+      d1[i] += s.fd[1][q] * s.S[q][i];
+      double t = 0.0;
+      for (int j = 0; j < n; ++j) t += s.D[q][j] * s.S[j][i];
+      dq[q][i] = t;
+    }
+  }
+  const double pen = double(s.degree) * (s.degree + 1);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double m = 0.0, l = 0.0;
+      for (int q = 0; q < n; ++q) {
+        m += s.wq[q] * s.S[q][i] * s.S[q][j];
+        l += s.wq[q] * dq[q][i] * dq[q][j];
+      }
+      l += pen * v0[i] * v0[j] + 0.5 * d0[i] * v0[j] + 0.5 * d0[j] * v0[i];
+      l += pen * v1[i] * v1[j] - 0.5 * d1[i] * v1[j] - 0.5 * d1[j] * v1[i];
+      R.M[i][j] = m;
+      R.L[i][j] = l;
+    }
+  R.iv0 = -pen * v0[0] * v1[n - 1] - 0.5 * d0[0] * v1[n - 1] + 0.5 * d1[n - 1] * v0[0];
+  R.iv1 = -pen * v0[0] * v1[n - 2] - 0.5 * d0[0] * v1[n - 2] + 0.5 * d1[n - 2] * v0[0];
+  return R;
+}
+
+template <int N, typename T>
+int precomputed_impl(const sf_op *op, int nrhs, const T *x, T *y, const T *cb, const T *cdinv, T *ct,
+                     double c_np, double c_tm, cudaStream_t st)
+{
+  using Cfg = PDGCfg<N, T>;
+  const Matrices1D mats = precomputed_matrices(op->shape);
+  PDGArgs<N, T> A{};
+  A.M = make_eo<N, T>([&](int i, int j) { return mats.M[i][j]; });
+  A.L = make_eo<N, T>([&](int i, int j) { return mats.L[i][j]; });
+  A.iv0 = T(mats.iv0);
+  A.iv1 = T(mats.iv1);
+  const double vol = op->h[0] * op->h[1] * op->h[2];
+  for (int d = 0; d < 3; ++d) {
+    A.c[d] = T(vol / (op->h[d] * op->h[d]));
+    A.nc[d] = op->desc.n_cells[d];
+  }
+  A.div_nx = make_fast_div((unsigned)A.nc[0]);
+  A.div_ny = make_fast_div((unsigned)A.nc[1]);
+  A.n_cells = op->n_cells;
+  A.n_dofs = op->n_dofs;
+  A.x = x;
+  A.y = y;
+  A.cb = cb;
+  A.cdinv = cdinv;
+  A.ct = ct;
+  A.c_np = T(c_np);
+  A.c_tm = T(c_tm);
+  void (*kern)(const PDGArgs<N, T>) = cb ? dg_precomputed_kernel<N, T, true> : dg_precomputed_kernel<N, T, false>;
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   cudaSharedmemCarveoutMaxShared));
+  const long long blocks = (op->n_cells + Cfg::CPB - 1) / Cfg::CPB;
+  kern<<<dim3((unsigned)blocks, (unsigned)nrhs), dim3(Cfg::CPB * N * N), Cfg::SMEM, st>>>(A);
+  SF_CUDA_TRY(cudaGetLastError());
+  return SF_OK;
+}
+
+template <int N>
+int precomputed_n(const sf_op *op, int prec, int nrhs, const void *x, void *y, const void *cb, const void *cd,
+                  void *ct, double c_np, double c_tm, cudaStream_t st)
+{
+  if (prec == SF_FP64)
+    return precomputed_impl<N, double>(op, nrhs, (const double *)x, (double *)y, (const double *)cb,
+                                       (const double *)cd, (double *)ct, c_np, c_tm, st);
+  return precomputed_impl<N, float>(op, nrhs, (const float *)x, (float *)y, (const float *)cb,
+                                    (const float *)cd, (float *)ct, c_np, c_tm, st);
+}
+
+} // namespace
+
+int launch_dg_precomputed(const sf_op *op, int prec, int nrhs, const void *x, void *y, const void *cb,
+                          const void *cdinv, void *ct, double c_np, double c_tm, cudaStream_t st)
+{
+  switch (op->n) {
+  case 2: return precomputed_n<2>(op, prec, nrhs, x, y, cb, cdinv, ct, c_np, c_tm, st);
+  case 3: return precomputed_n<3>(op, prec, nrhs, x, y, cb, cdinv, ct, c_np, c_tm, st);
+  case 4: return precomputed_n<4>(op, prec, nrhs, x, y, cb, cdinv, ct, c_np, c_tm, st);
+  case 5: return precomputed_n<5>(op, prec, nrhs, x, y, cb, cdinv, ct, c_np, c_tm, st);
+  case 6: return precomputed_n<6>(op, prec, nrhs, x, y, cb, cdinv, ct, c_np, c_tm, st);
+  case 7: return precomputed_n<7>(op, prec, nrhs, x, y, cb, cdinv, ct, c_np, c_tm, st);
+  case 8: return precomputed_n<8>(op, prec, nrhs, x, y, cb, cdinv, ct, c_np, c_tm, st);
+  case 9: return precomputed_n<9>(op, prec, nrhs, x, y, cb, cdinv, ct, c_np, c_tm, st);
+  default: set_error("unsupported degree"); return SF_ERR_UNSUPPORTED;
+  }
+}
+
+// diagonal: sum_d c_d L_ii (x) M_jj (x) M_kk per cell (the couplings are off
+// the diagonal), computed in FP64 on the host and broadcast to all cells
+int launch_dg_precomputed_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st)
+{
+  const Matrices1D m = precomputed_matrices(op->shape);
+  const int n = op->n, n3 = n * n * n;
+  const double vol = op->h[0] * op->h[1] * op->h[2];
+  double c[3];
+  for (int d = 0; d < 3; ++d) c[d] = vol / (op->h[d] * op->h[d]);
+  double pat[kMaxN * kMaxN * kMaxN];
+  float patf[kMaxN * kMaxN * kMaxN];
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const double v = c[0] * m.L[i][i] * m.M[j][j] * m.M[k][k] + c[1] * m.M[i][i] * m.L[j][j] * m.M[k][k] +
+                         c[2] * m.M[i][i] * m.M[j][j] * m.L[k][k];
+        pat[(k * n + j) * n + i] = v;
+        patf[(k * n + j) * n + i] = float(v);
+      }
+  DevBuf buf;
+  const size_t es = prec == SF_FP64 ? sizeof(double) : sizeof(float);
+  int r = buf.alloc(n3 * es);
+  if (r) return r;
+  SF_CUDA_TRY(cudaMemcpyAsync(buf.ptr, prec == SF_FP64 ? (const void *)pat : (const void *)patf, n3 * es,
+                              cudaMemcpyHostToDevice, st));
+  if (prec == SF_FP64)
+    precomputed_pattern_kernel<double><<<152 * 8, 256, 0, st>>>(op->n_dofs, n3, (const double *)buf.ptr,
+                                                               (double *)diag);
+  else
+    precomputed_pattern_kernel<float><<<152 * 8, 256, 0, st>>>(op->n_dofs, n3, (const float *)buf.ptr,
+                                                              (float *)diag);
+  SF_CUDA_TRY(cudaGetLastError());
+  // the staging buffer is released when buf goes out of scope
+  SF_CUDA_TRY(cudaStreamSynchronize(st));
+  return SF_OK;
+}
+
+} // namespace sf

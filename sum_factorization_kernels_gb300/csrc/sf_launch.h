@@ -35,6 +35,11 @@ int launch_dg_rk_stage(const sf_op *op, int prec, int nrhs, const void *src, con
                        void *vec_tm, double c_np, double c_tm, cudaStream_t st);
 int launch_dg_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
 
+// sf_dg_precomputed.cu: tensor-product SIPG with precomputed 1D matrices
+int launch_dg_precomputed(const sf_op *op, int prec, int nrhs, const void *x, void *y, const void *cheb_b,
+                          const void *cheb_dinv, void *cheb_t, double c_np, double c_tm, cudaStream_t st);
+int launch_dg_precomputed_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
+
 // blocks of a kernel that fit on one SM with the maximum shared-memory
 // carveout: the occupancy calculator does not account for the carveout
 // preference, so persistent grids size themselves from the limits directly

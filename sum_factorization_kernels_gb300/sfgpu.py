@@ -18,7 +18,7 @@ STATUS = {0: "SF_OK", -1: "SF_ERR_INVALID", -2: "SF_ERR_NULL", -3: "SF_ERR_UNSUP
           -4: "SF_ERR_CUDA", -5: "SF_ERR_OOM", -6: "SF_ERR_NOT_CONVERGED",
           -7: "SF_ERR_BREAKDOWN", -8: "SF_ERR_ALIGN", -9: "SF_ERR_STATE"}
 FP64, FP32 = 0, 1
-OP_LAPLACE, OP_DG_SIPG, OP_DG_ADVECT = 0, 1, 2
+OP_LAPLACE, OP_DG_SIPG, OP_DG_ADVECT, OP_DG_PRECOMPUTED = 0, 1, 2, 3
 BASIS_GLL, BASIS_HERMITE = 0, 1
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2

@@ -1,8 +1,9 @@
 """Time single operator applies through the C ABI (CUDA events, inputs in
 device memory): ``python -m sum_factorization_kernels_gb300.timing KIND ...``.
 
-KIND is ``laplace`` (continuous, deformed mesh), ``sipg`` (DG SIPG) or
-``advect`` (DG upwind advection with inverse mass).  Prints one line with the
+KIND is ``laplace`` (continuous, deformed mesh), ``sipg`` (DG SIPG),
+``advect`` (DG upwind advection with inverse mass) or ``precomputed`` (DG
+SIPG in tensor-product form with precomputed 1D matrices).  Prints one line with the
 apply rate summed over the right-hand sides and the vector traffic it implies.
 Used to drive profiler captures of one kernel on a small case.
 """
@@ -23,12 +24,14 @@ def make_operator(kind: str, degree: int, ncells: int):
         return sf.Operator(sf.OP_DG_SIPG, degree=degree, n_cells=n)
     if kind == "advect":
         return sf.Operator(sf.OP_DG_ADVECT, degree=degree, n_cells=n, velocity=(1.0, 0.5, 0.25), inverse_mass=1)
+    if kind == "precomputed":
+        return sf.Operator(sf.OP_DG_PRECOMPUTED, degree=degree, n_cells=n)
     raise ValueError("unknown operator kind %r" % kind)
 
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("kind", choices=["laplace", "sipg", "advect"])
+    ap.add_argument("kind", choices=["laplace", "sipg", "advect", "precomputed"])
     ap.add_argument("--degree", type=int, default=4)
     ap.add_argument("--ncells", type=int, default=32, help="cells per direction")
     ap.add_argument("--prec", choices=["fp32", "fp64"], default="fp32")
