@@ -214,9 +214,11 @@ def time_apply(op, x, y, steps, warmup, stream):
 def secondary_configs(stream, peak):
     """the other configurations of the metric, measured once each: config 1
     (Q4 16^3 affine FP64, error vs the reference's golden vector), config 3
-    (DG SIPG p=5 48^3 CG to 1e-10: FP32-inner/FP64-refined vs all-FP64),
+    (DG SIPG p=5 48^3 CG to 1e-10: FP32-inner/FP64-refined vs all-FP64; the
+    same problem with the precomputed tensor-product SIPG operator),
     config 4 (variable kappa p=4 32^3: forward and adjoint), config 5 (DG
-    advection p=4 48^3, 8 right-hand sides: forward / transpose, dot test)"""
+    advection p=4 48^3, 8 right-hand sides: forward / transpose, LSRK(5,4)
+    time steps, dot test)"""
     import numpy as np
     import torch
 
@@ -260,7 +262,25 @@ def secondary_configs(stream, peak):
     if res["mixed_fp32_inner"]["seconds"] > 0:
         res["fp64_over_mixed_wall_time"] = round(res["all_fp64"]["seconds"] / res["mixed_fp32_inner"]["seconds"], 2)
     out["dg_sipg_p5_48c_cg"] = res
-    del op, b
+    del op
+    # the same SIPG problem class in the tensor-product form with precomputed
+    # 1D matrices (PrecomputedDGLaplacian): apply and mixed-precision CG
+    op = sfgpu.Operator(sfgpu.OP_DG_PRECOMPUTED, degree=5, n_cells=(48, 48, 48), length=(1.0, 1.0, 1.0))
+    t32 = time_apply(op, xd32, yd32, 20, 3, stream)
+    t64 = time_apply(op, xd64, yd64, 5, 2, stream)
+    res = {"n_dofs": N, "apply_fp32_gdofs": round(N / t32 / 1e9, 3),
+           "apply_fp32_hbm_frac": round(2 * 4 * N / t32 / 1e9 / peak, 4),
+           "apply_fp64_gdofs": round(N / t64 / 1e9, 3)}
+    xs = torch.zeros_like(b)
+    opts = sfgpu.default_solve_opts(mode=sfgpu.SOLVE_MIXED, precond=sfgpu.PRECOND_CHEBYSHEV, cheb_degree=5,
+                                    rtol=1e-10, project_constant=1, max_iter=4000)
+    op.cg_solve(b, torch.zeros_like(b), opts)
+    code, st = op.cg_solve(b, xs, opts)
+    res["mixed_fp32_inner"] = {"status": code, "iterations": st.iterations, "outer": st.outer_iterations,
+                               "rel_residual": float("%.3g" % st.rel_residual), "seconds": round(st.seconds, 3),
+                               "operator_applies": st.operator_applies}
+    out["dg_precomputed_p5_48c"] = res
+    del op, b, xd32, yd32, xd64, yd64
     torch.cuda.empty_cache()
     # ---- config 4 ----
     op = sfgpu.Operator(sfgpu.OP_LAPLACE, degree=4, n_cells=(32, 32, 32), deform=0.05)
