@@ -17,8 +17,10 @@
 // colour launches, first-touch store / add, programmatic dependent launch
 // for colours 1..7 (see sf_cont_column.cuh).
 //
-// The slab paddings (P1, P2, per-cell skews) come from a search of the
-// shared-memory bank conflicts of the access patterns for each (n, W, K).
+// The slab paddings (P1, P2, Q1, Q2, per-cell skews) come from a search of
+// the shared-memory bank conflicts of the access patterns for each (n, W,
+// K); slab B2, read and written only along y lines and z columns, lives in
+// its own region with a layout that is conflict-free for those two patterns.
 #include "sf_cont_column.cuh"
 #include "sf_device.cuh"
 #include "sf_internal.h"
@@ -31,31 +33,34 @@ namespace sf {
 namespace {
 
 // W warps per group, K cells per group, GROUPS groups per block; slab
-// index (a, b, c) = a + P1 b + P2 c; SKEW pads the per-cell slab region,
-// GPAD the per-cell geometry block in shared memory (elements); MINB is the
-// resident-block target handed to the register allocator.
+// index (a, b, c) = a + P1 b + P2 c for slabs B0 and B1 (which see x, y and
+// z line patterns), SKEW pads their per-cell region; slab B2 (y and z
+// patterns only) has its own layout a + Q1 b + Q2 c and per-cell skew SKEW2
+// in a separate region; GPAD pads the per-cell geometry block in shared
+// memory (elements); MINB is the resident-block target handed to the
+// register allocator.
 struct PackParams {
-  int W, K, GROUPS, P1, P2, SKEW, GPAD, MINB;
+  int W, K, GROUPS, P1, P2, SKEW, GPAD, MINB, Q1, Q2, SKEW2;
 };
 
 constexpr PackParams pack_params(int n, int elem)
 {
-  return elem == 4 ? (n == 2   ? PackParams{1, 8, 4, 2, 5, 6, 4, 1}
-                      : n == 3 ? PackParams{2, 7, 2, 3, 9, 10, 4, 1}
-                      : n == 4 ? PackParams{1, 2, 4, 4, 19, 12, 16, 1}
-                      : n == 5 ? PackParams{4, 5, 2, 5, 25, 6, 12, 4}
-                      : n == 6 ? PackParams{7, 6, 1, 7, 42, 8, 20, 1}
-                      : n == 7 ? PackParams{5, 3, 1, 7, 56, 25, 0, 1}
-                      : n == 8 ? PackParams{2, 1, 2, 9, 72, 0, 0, 1}
-                               : PackParams{8, 3, 1, 9, 81, 14, 0, 1})
-                   : (n == 2   ? PackParams{1, 8, 4, 2, 5, 6, 4, 1}
-                      : n == 3 ? PackParams{2, 7, 2, 3, 18, 7, 8, 1}
-                      : n == 4 ? PackParams{1, 2, 4, 4, 19, 0, 0, 1}
-                      : n == 5 ? PackParams{4, 5, 1, 5, 25, 6, 0, 1}
-                      : n == 6 ? PackParams{7, 6, 1, 7, 42, 8, 4, 1}
-                      : n == 7 ? PackParams{5, 3, 1, 7, 49, 12, 0, 1}
-                      : n == 8 ? PackParams{2, 1, 2, 9, 72, 0, 0, 1}
-                               : PackParams{3, 1, 2, 9, 81, 0, 0, 1});
+  return elem == 4 ? (n == 2   ? PackParams{1, 8, 4, 2, 5, 0, 4, 1, 2, 6, 0}
+                      : n == 3 ? PackParams{2, 7, 2, 3, 9, 5, 4, 1, 3, 11, 8}
+                      : n == 4 ? PackParams{1, 2, 4, 4, 19, 24, 16, 1, 4, 20, 0}
+                      : n == 5 ? PackParams{4, 5, 2, 5, 25, 3, 12, 4, 5, 37, 0}
+                      : n == 6 ? PackParams{7, 6, 1, 7, 42, 4, 20, 1, 6, 38, 0}
+                      : n == 7 ? PackParams{5, 3, 1, 7, 56, 1, 0, 1, 7, 52, 5}
+                      : n == 8 ? PackParams{2, 1, 2, 9, 72, 0, 0, 1, 8, 72, 0}
+                               : PackParams{8, 3, 1, 9, 81, 7, 0, 1, 9, 85, 20})
+                   : (n == 2   ? PackParams{1, 8, 4, 2, 5, 0, 4, 1, 2, 6, 0}
+                      : n == 3 ? PackParams{2, 7, 2, 3, 18, 13, 8, 1, 3, 19, 0}
+                      : n == 4 ? PackParams{1, 2, 4, 4, 19, 0, 0, 1, 4, 20, 0}
+                      : n == 5 ? PackParams{4, 5, 1, 5, 25, 3, 0, 1, 5, 37, 0}
+                      : n == 6 ? PackParams{7, 6, 1, 7, 42, 4, 4, 1, 6, 38, 0}
+                      : n == 7 ? PackParams{5, 3, 1, 7, 49, 9, 0, 1, 7, 55, 0}
+                      : n == 8 ? PackParams{2, 1, 2, 9, 72, 0, 0, 1, 8, 72, 0}
+                               : PackParams{3, 1, 2, 9, 81, 0, 0, 1, 9, 89, 0});
 }
 
 template <int N, typename T>
@@ -63,16 +68,19 @@ struct LineCfg {
   static constexpr PackParams PP = pack_params(N, (int)sizeof(T));
   static constexpr int W = PP.W, K = PP.K, GROUPS = PP.GROUPS, P1 = PP.P1, P2 = PP.P2;
   static constexpr int N2 = N * N, N3 = N * N * N;
-  static constexpr int SLAB = P2 * N;              // elements per slab
-  static constexpr int RS = 3 * SLAB + PP.SKEW;    // slab region per cell
+  static constexpr int Q1 = PP.Q1, Q2 = PP.Q2;
+  static constexpr int SLAB = P2 * N;              // elements per slab B0, B1
+  static constexpr int RS = 2 * SLAB + PP.SKEW;    // B0 + B1 region per cell
+  static constexpr int RS2 = Q2 * N + PP.SKEW2;    // B2 region per cell
   static constexpr int AL = 16 / (int)sizeof(T);   // elements per 16 bytes
   static constexpr int GEO = (6 * N3 + 3) / 4 * 4; // geometry block in global memory
   static constexpr int GS = GEO + PP.GPAD;         // geometry block in shared memory
   static constexpr int GT = 32 * W;                // threads per group
   static constexpr long long GROUP_BYTES =
-      ((long long)K * (GS + RS) * (long long)sizeof(T) + 127) / 128 * 128;
+      ((long long)K * (GS + RS + RS2) * (long long)sizeof(T) + 127) / 128 * 128;
   static_assert(K * N2 <= GT, "cells do not fit the group");
   static_assert((P1 + 1) * (N - 1) < P2, "slab padding overlaps");
+  static_assert((Q1 + 1) * (N - 1) < Q2 && Q1 >= N, "B2 slab padding overlaps");
   static_assert(GS % AL == 0, "geometry blocks must stay 16-byte aligned");
 };
 
@@ -102,7 +110,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
 {
   using Cfg = LineCfg<N, T>;
   constexpr int N2 = Cfg::N2, N3 = Cfg::N3, K = Cfg::K, W = Cfg::W, GT = Cfg::GT;
-  constexpr int P1 = Cfg::P1, P2 = Cfg::P2, SLAB = Cfg::SLAB;
+  constexpr int P1 = Cfg::P1, P2 = Cfg::P2, SLAB = Cfg::SLAB, Q1 = Cfg::Q1, Q2 = Cfg::Q2;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw);
   const int grp = threadIdx.x / GT, t = threadIdx.x % GT;
@@ -117,10 +125,13 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
   const int a = l % N, b = l / N; // z column (a,b) / y line (a,c=b) / x line (b'=a, c'=b)
   T *geo_s = reinterpret_cast<T *>(gbase) + k * Cfg::GS;
   T *B0 = reinterpret_cast<T *>(gbase) + K * Cfg::GS + k * Cfg::RS;
-  T *B1 = B0 + SLAB, *B2 = B1 + SLAB;
+  T *B1 = B0 + SLAB;
+  T *B2 = reinterpret_cast<T *>(gbase) + K * (Cfg::GS + Cfg::RS) + k * Cfg::RS2;
   const int zc = a + P1 * b;      // z column base
   const int xl = P1 * a + P2 * b; // x line (b'=a, c'=b) base, stride 1
   const int yl = a + P2 * b;      // y line (a, c=b) base, stride P1
+  const int zc2 = a + Q1 * b;     // the same z column in B2, stride Q2
+  const int yl2 = a + Q2 * b;     // the same y line in B2, stride Q1
   const int plane = A.plane;
   const int toff = b * A.Nx + a;  // node (a, b, 0) relative to the cell's node (0, 0, 0)
 
@@ -201,7 +212,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
 #pragma unroll
     for (int m = 0; m < N; ++m) {
       if (used) B1[yl + P1 * m] = v[m];
-      if (used) B2[yl + P1 * m] = g[m];
+      if (used) B2[yl2 + Q1 * m] = g[m];
     }
     cell_group_sync<W>(grp);
     // ---- D_x into B0; D_z stays in registers (same thread, same column) ----
@@ -231,7 +242,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
 #pragma unroll
       for (int c = 0; c < N; ++c) {
         const int s = zc + P2 * c;
-        const T gx = B0[s], gy = B2[s];
+        const T gx = B0[s], gy = B2[zc2 + Q2 * c];
         T tx, ty, tzc;
         if (DEFORMED) {
           const T *Gq = geo_s + c * N2 + l;
@@ -253,7 +264,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
           tzc *= kq;
         }
         if (used) B0[s] = tx;
-        if (used) B2[s] = ty;
+        if (used) B2[zc2 + Q2 * c] = ty;
         tz[c] = tzc;
       }
       eo_apply<N, -1>(A.DT, tz, g);
@@ -291,7 +302,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
     }
     cell_group_sync<W>(grp);
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = B2[yl + P1 * m];
+    for (int m = 0; m < N; ++m) v[m] = B2[yl2 + Q1 * m];
     eo_apply<N, -1>(A.DT, v, g);
 #pragma unroll
     for (int m = 0; m < N; ++m) g[m] += B1[yl + P1 * m];
