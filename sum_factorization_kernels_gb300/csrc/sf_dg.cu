@@ -96,6 +96,50 @@ __device__ __forceinline__ void face_flux(const DGArgs<N, T> &A, int d, int side
   }
 }
 
+// Face arrays of a cell: NF arrays of n^2 face points, array (d, side,
+// value/derivative) at index 4 d + 2 side + deriv for SIPG (12 arrays) and
+// 2 d + side for advection (6 value arrays).  Arrays are FA apart, cells
+// NF FA + SKEW apart; the tangential sweeps give lane `task` the line of
+// array task / n (arr-major) or task % NF (line-major).  FA, SKEW and the
+// map come from a bank-conflict model of the face writes, the two sweeps
+// and the residual reads over the lanes of each warp.
+struct DGFaceLayout {
+  int FA, SKEW, LINE_MAJOR;
+};
+
+constexpr DGFaceLayout dg_face_layout(int n, bool sipg)
+{
+  return sipg ? (n == 2   ? DGFaceLayout{5, 0, 1}
+                 : n == 3 ? DGFaceLayout{9, 5, 1}
+                 : n == 4 ? DGFaceLayout{19, 12, 0}
+                 : n == 5 ? DGFaceLayout{30, 17, 1}
+                 : n == 6 ? DGFaceLayout{37, 8, 1}
+                 : n == 7 ? DGFaceLayout{56, 17, 0}
+                 : n == 8 ? DGFaceLayout{67, 0, 1}
+                          : DGFaceLayout{81, 5, 0})
+              : (n == 2   ? DGFaceLayout{5, 6, 1}
+                 : n == 3 ? DGFaceLayout{9, 5, 0}
+                 : n == 4 ? DGFaceLayout{21, 18, 0}
+                 : n == 5 ? DGFaceLayout{25, 3, 0}
+                 : n == 6 ? DGFaceLayout{37, 6, 1}
+                 : n == 7 ? DGFaceLayout{56, 1, 0}
+                 : n == 8 ? DGFaceLayout{67, 0, 1}
+                          : DGFaceLayout{81, 11, 0});
+}
+
+template <int KIND>
+__host__ __device__ constexpr int face_arrays()
+{
+  return KIND == K_SIPG ? 12 : 6;
+}
+
+// array index of (direction, side, value = 0 / derivative = 1)
+template <int KIND>
+__device__ __forceinline__ constexpr int face_index(int d, int side, int deriv)
+{
+  return KIND == K_SIPG ? 4 * d + 2 * side + deriv : 2 * d + side;
+}
+
 // Everything for one line of direction d held by this thread: values at Gauss
 // points u[], neighbour face data at index fi, produce the line residual r[]
 // (collocation space) = cell term + face injections.
@@ -103,7 +147,6 @@ template <int KIND, bool TRANSPOSE, int N, typename T>
 __device__ __forceinline__ void line_residual(const DGArgs<N, T> &A, int d, const T (&u)[N], T wt,
                                               const T *F, int fi, T (&r)[N])
 {
-  constexpr int N2 = N * N;
   // own face values/derivatives (reference coordinates)
   const T vm = dot_row<N, T>(A.fv0, u), vp = dot_row<N, T>(A.fv1, u);
   T dm = T(0), dp = T(0);
@@ -111,11 +154,13 @@ __device__ __forceinline__ void line_residual(const DGArgs<N, T> &A, int d, cons
     dm = dot_row<N, T>(A.fd0, u);
     dp = dot_row<N, T>(A.fd1, u);
   }
-  const T *Fm = F + (4 * d) * N2, *Fp = F + (4 * d + 2) * N2;
+  constexpr int FA = dg_face_layout(N, KIND == K_SIPG).FA;
+  const T *Fm = F + face_index<KIND>(d, 0, 0) * FA, *Fp = F + face_index<KIND>(d, 1, 0) * FA;
   T fvm, fdm, fvp, fdp;
-  face_flux<KIND, TRANSPOSE, N, T>(A, d, 0, vm, dm, Fm[fi], KIND == K_SIPG ? Fm[N2 + fi] : T(0), wt,
+  // the derivative array follows the value array of the same face (SIPG)
+  face_flux<KIND, TRANSPOSE, N, T>(A, d, 0, vm, dm, Fm[fi], KIND == K_SIPG ? Fm[FA + fi] : T(0), wt,
                                    fvm, fdm);
-  face_flux<KIND, TRANSPOSE, N, T>(A, d, 1, vp, dp, Fp[fi], KIND == K_SIPG ? Fp[N2 + fi] : T(0), wt,
+  face_flux<KIND, TRANSPOSE, N, T>(A, d, 1, vp, dp, Fp[fi], KIND == K_SIPG ? Fp[FA + fi] : T(0), wt,
                                    fvp, fdp);
   T g[N];
   if (KIND == K_SIPG) {
@@ -150,9 +195,16 @@ struct DGCfg {
   static constexpr int P1 = L.P1, P2 = L.P2;
   static constexpr int SLAB = P2 * N;            // elements per slab
   static constexpr int RS = 3 * SLAB + L.SKEW;   // slab region per cell
-  static constexpr int N2 = N * N;
-  static constexpr size_t SMEM = (size_t(CPB) * RS + size_t(CPB) * 12 * N2) * sizeof(T);
   static_assert((P1 + 1) * (N - 1) < P2, "slab padding overlaps");
+  // face region per cell of an operator kind
+  static constexpr int face_stride(bool sipg)
+  {
+    return (sipg ? 12 : 6) * dg_face_layout(N, sipg).FA + dg_face_layout(N, sipg).SKEW;
+  }
+  static constexpr size_t smem(bool sipg)
+  {
+    return (size_t(CPB) * RS + size_t(CPB) * face_stride(sipg)) * sizeof(T);
+  }
 };
 
 template <int N, typename T, int KIND, bool TRANSPOSE, bool INVMASS, int EPI>
@@ -162,7 +214,9 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   using Cfg = DGCfg<N, T>;
   constexpr int N2 = N * N, N3 = N * N * N;
   constexpr int CPB = Cfg::CPB, P1 = Cfg::P1, P2 = Cfg::P2;
-  constexpr int NF = KIND == K_SIPG ? 12 : 6; // face arrays per cell
+  constexpr int NF = face_arrays<KIND>(); // face arrays per cell
+  constexpr DGFaceLayout FL = dg_face_layout(N, KIND == K_SIPG);
+  constexpr int FA = FL.FA;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
   const int tid = threadIdx.x;
@@ -177,7 +231,7 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   T *B0 = smem + cs * Cfg::RS;
   T *B1 = B0 + Cfg::SLAB, *B2 = B1 + Cfg::SLAB;
   // face arrays: [dir][side][value, derivative][n^2]  (SIPG), values only (advection)
-  T *F = smem + CPB * Cfg::RS + cs * (12 * N2);
+  T *F = smem + CPB * Cfg::RS + cs * Cfg::face_stride(KIND == K_SIPG);
   const int zc = a + P1 * b;      // z column (a, b)
   const int xl = P1 * a + P2 * b; // x line (y=a, z=b), stride 1
   const int yl = a + P2 * b;      // y line (x=a, z=b), stride P1
@@ -214,22 +268,21 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
       // side 0 (face at 0): neighbour's layer p (value) and p-1; side 1: layers 0 and 1
       const T v0 = __ldg(x + base_in[0] + (N - 1) * stride_n);
       const T v1 = __ldg(x + base_in[1]);
-      F[(4 * d + 0) * N2 + t] = v0;
-      F[(4 * d + 2) * N2 + t] = v1;
+      F[face_index<KIND>(d, 0, 0) * FA + t] = v0;
+      F[face_index<KIND>(d, 1, 0) * FA + t] = v1;
       if (KIND == K_SIPG) {
         const T u0 = __ldg(x + base_in[0] + (N - 2) * stride_n);
         const T u1 = __ldg(x + base_in[1] + stride_n);
-        F[(4 * d + 1) * N2 + t] = A.hd0 * (u0 - v0);
-        F[(4 * d + 3) * N2 + t] = -A.hd0 * (u1 - v1);
+        F[face_index<KIND>(d, 0, 1) * FA + t] = A.hd0 * (u0 - v0);
+        F[face_index<KIND>(d, 1, 1) * FA + t] = -A.hd0 * (u1 - v1);
       }
     }
   }
   __syncthreads();
   // ---- first tangential direction of the faces ----
   for (int task = t; task < NF * N; task += N2) {
-    const int arr = task / N, line = task % N;
-    const int k = KIND == K_SIPG ? arr : 2 * arr; // advection uses the value arrays only
-    T *Fa = F + k * N2 + line * N;
+    const int arr = FL.LINE_MAJOR ? task % NF : task / N, line = FL.LINE_MAJOR ? task / NF : task % N;
+    T *Fa = F + arr * FA + line * N;
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = Fa[m];
     eo_apply<N, 1>(A.S, v, v);
@@ -244,9 +297,8 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
 #pragma unroll
   for (int m = 0; m < N; ++m) B0[xl + m] = v[m];
   for (int task = t; task < NF * N; task += N2) {
-    const int arr = task / N, line = task % N;
-    const int k = KIND == K_SIPG ? arr : 2 * arr;
-    T *Fa = F + k * N2 + line;
+    const int arr = FL.LINE_MAJOR ? task % NF : task / N, line = FL.LINE_MAJOR ? task / NF : task % N;
+    T *Fa = F + arr * FA + line;
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = Fa[N * m];
     eo_apply<N, 1>(A.S, v, v);
@@ -477,7 +529,7 @@ int dg_vmult_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T *y, c
     kern = rk ? dg_kernel<N, T, K_ADVECT, false, false, EPI_RK>
          : cheb ? dg_kernel<N, T, K_ADVECT, false, false, EPI_CHEB>
                 : dg_kernel<N, T, K_ADVECT, false, false, EPI_STORE>;
-  const size_t smem = DGCfg<N, T>::SMEM;
+  const size_t smem = DGCfg<N, T>::smem(sipg);
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    cudaSharedmemCarveoutMaxShared));
