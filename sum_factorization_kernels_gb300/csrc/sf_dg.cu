@@ -392,38 +392,39 @@ template <int N, typename T>
 __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     dg_inverse_mass_kernel(const __grid_constant__ DGArgs<N, T> A)
 {
+  // one padded slab per cell; z columns read and written straight from the
+  // cell-major vectors: P^T along z (registers), x, y; scale by 1/(JxW w) at
+  // the Gauss points; P along y, x, z (registers)
   constexpr int N2 = N * N, N3 = N * N * N;
   constexpr int CPB = DGCells<N>::value;
+  constexpr DGLayout L = dg_layout(N, (int)sizeof(T));
+  constexpr int P1 = L.P1, P2 = L.P2, RS1 = P2 * N + L.SKEW;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
   const int tid = threadIdx.x;
   const int cs = tid / N2;
   const int t = tid - cs * N2;
   const int a = t % N, b = t / N;
-  const long long cell0 = (long long)blockIdx.x * CPB;
-  const long long roff = (long long)blockIdx.y * A.n_dofs;
-  T *B = smem + cs * N3;
-  const long long nval = min((long long)CPB, A.n_cells - cell0) * N3;
-  const T *src = A.x + roff + cell0 * N3;
-  for (long long e = tid; e < nval; e += blockDim.x) smem[e] = __ldg(src + e);
-  __syncthreads();
-  // P^T in z, x, y; scale; P in z, x, y  (P^T = transposed Sinv)
-  EOMat<N, T> PT; // built on the fly from P: transposed tables passed in ST slot
+  const long long cell = (long long)blockIdx.x * CPB + cs;
+  const bool valid = cell < A.n_cells;
+  const long long col = (long long)blockIdx.y * A.n_dofs + cell * N3 + t;
+  T *B = smem + cs * RS1;
+  const int zc = a + P1 * b, xl = P1 * a + P2 * b, yl = a + P2 * b;
   T v[N];
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[t + N2 * m];
+  for (int m = 0; m < N; ++m) v[m] = valid ? __ldg(A.x + col + N2 * m) : T(0);
   eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[t + N2 * m] = v[m];
+  for (int m = 0; m < N; ++m) B[zc + P2 * m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[N * t + m];
+  for (int m = 0; m < N; ++m) v[m] = B[xl + m];
   eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[N * t + m] = v[m];
+  for (int m = 0; m < N; ++m) B[xl + m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[a + N * m + N2 * b];
+  for (int m = 0; m < N; ++m) v[m] = B[yl + P1 * m];
   eo_apply<N, 1>(A.ST, v, v);
   // now at Gauss point (a, m, c=b): divide by JxW w
   const T iwab = A.ijxw * A.iw[a] * A.iw[b];
@@ -431,23 +432,21 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   for (int m = 0; m < N; ++m) v[m] *= iwab * A.iw[m];
   eo_apply<N, 1>(A.P, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[a + N * m + N2 * b] = v[m];
+  for (int m = 0; m < N; ++m) B[yl + P1 * m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[N * t + m];
+  for (int m = 0; m < N; ++m) v[m] = B[xl + m];
   eo_apply<N, 1>(A.P, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[N * t + m] = v[m];
+  for (int m = 0; m < N; ++m) B[xl + m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[t + N2 * m];
+  for (int m = 0; m < N; ++m) v[m] = B[zc + P2 * m];
   eo_apply<N, 1>(A.P, v, v);
+  if (valid) {
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[t + N2 * m] = v[m];
-  __syncthreads();
-  (void)PT;
-  T *dst = A.y + roff + cell0 * N3;
-  for (long long e = tid; e < nval; e += blockDim.x) dst[e] = smem[e];
+    for (int m = 0; m < N; ++m) A.y[col + N2 * m] = v[m];
+  }
 }
 
 // fill a vector with a per-cell pattern of n^3 values (uniform Cartesian mesh)
@@ -543,13 +542,13 @@ template <int N, typename T>
 int dg_invmass_impl(const sf_op *op, int nrhs, const T *x, T *y, cudaStream_t st)
 {
   constexpr int CPB = DGCells<N>::value;
-  constexpr int N3 = N * N * N;
+  constexpr DGLayout L = dg_layout(N, (int)sizeof(T));
   DGArgs<N, T> A = make_dg_args<N, T>(op);
   // the transposed tables of P go into the ST slot
   A.ST = eo_of<N, T>(op->shape.Sinv, true);
   A.x = x;
   A.y = y;
-  const size_t smem = size_t(CPB) * N3 * sizeof(T);
+  const size_t smem = size_t(CPB) * (L.P2 * N + L.SKEW) * sizeof(T);
   SF_CUDA_TRY(cudaFuncSetAttribute(dg_inverse_mass_kernel<N, T>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long blocks = (op->n_cells + CPB - 1) / CPB;

@@ -38,6 +38,7 @@ def main(argv=None) -> None:
     ap.add_argument("--nrhs", type=int, default=1)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--transpose", action="store_true", help="time the transposed apply")
     a = ap.parse_args(argv)
     op = make_operator(a.kind, a.degree, a.ncells)
     dt = torch.float32 if a.prec == "fp32" else torch.float64
@@ -47,7 +48,9 @@ def main(argv=None) -> None:
     y = torch.empty_like(x)
 
     def apply():
-        if a.nrhs > 1:
+        if a.transpose:
+            op.vmult_transpose_batched(x, y, a.nrhs)
+        elif a.nrhs > 1:
             op.vmult_batched(x, y, a.nrhs)
         else:
             op.vmult(x, y)
@@ -63,9 +66,9 @@ def main(argv=None) -> None:
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) / 1e3 / a.reps
     status = op.device_status()
-    print("%s p=%d %d^3 %s nrhs=%d: %.3f GDoF/s (summed over right-hand sides), %.1f GB/s of vector "
+    print("%s%s p=%d %d^3 %s nrhs=%d: %.3f GDoF/s (summed over right-hand sides), %.1f GB/s of vector "
           "traffic, %.1f us per apply, device status %d"
-          % (a.kind, a.degree, a.ncells, a.prec, a.nrhs, a.nrhs * n / t / 1e9,
+          % (a.kind, " (transpose)" if a.transpose else "", a.degree, a.ncells, a.prec, a.nrhs, a.nrhs * n / t / 1e9,
              2 * a.nrhs * n * x.element_size() / t / 1e9, t * 1e6, status))
     if status != 0:
         raise SystemExit("device status %d" % status)
