@@ -89,9 +89,17 @@ int derive_variant_geometry(sf_op *op)
   return SF_OK;
 }
 
+// derived copies of the FP64 geometry: the walk-ordered blocks of the line
+// kernel (each prepared precision), the natural FP32 copy and the variant's
 int derive_fp32_geometry(sf_op *op)
 {
-  if (!(op->desc.precisions & 2) || !op->deformed) return SF_OK;
+  if (!op->deformed) return SF_OK;
+  if (op->desc.precisions & 1) SF_RET(pack_line_geometry(op, SF_FP64));
+  if (!(op->desc.precisions & 2)) {
+    SF_CUDA_TRY(cudaDeviceSynchronize());
+    return SF_OK;
+  }
+  SF_RET(pack_line_geometry(op, SF_FP32));
   const size_t entries = (size_t)op->n_cells * op->geo_stride;
   if (op->geo32.bytes != entries * sizeof(float)) SF_RET(op->geo32.alloc(entries * sizeof(float)));
   SF_RET(launch_convert((long long)entries, SF_FP64, op->geo64.ptr, SF_FP32, op->geo32.ptr, 0));

@@ -62,6 +62,7 @@ struct sf_op {
   bool has_kappa = false;
   sf::DevBuf scratch;           // operator-private scratch (transpose, M^-1)
   sf::DevBuf geoPair;           // FP32 geometry for the pair kernel (pair-interleaved)
+  sf::DevBuf geoLine64, geoLine32; // geometry in the line kernel's walk order
   long long geoPair_stride = 0;
   sf::DevBuf dev_err;           // device error flags (bounded waits)
   int kernel_variant = 0;       // sf_kernel_variant

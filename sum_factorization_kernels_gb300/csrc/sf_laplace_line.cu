@@ -11,8 +11,12 @@
 // so the groups of one block run independently.
 //
 // The grid is persistent: a group walks a strided list of the colour's
-// cells, K consecutive ordinals per step.  The next step's K geometry blocks
-// are fetched by TMA bulk copies right after the quadrature-point operation
+// cells, K consecutive ordinals per step.  The geometry is stored in the
+// order of that walk (a copy of the natural [cell][6][n^3] tensors made at
+// setup): per colour class, blocks of K ordinals, each block [6][n][K n^2]
+// so that lane t reads word c K n^2 + t of each component (consecutive
+// lanes, consecutive words: no bank conflicts).  The next step's block is
+// fetched by one TMA bulk copy right after the quadrature-point operation
 // of the current step (one mbarrier per group, bounded wait).  Summation: 8
 // colour launches, first-touch store / add, programmatic dependent launch
 // for colours 1..7 (see sf_cont_column.cuh).
@@ -36,31 +40,30 @@ namespace {
 // index (a, b, c) = a + P1 b + P2 c for slabs B0 and B1 (which see x, y and
 // z line patterns), SKEW pads their per-cell region; slab B2 (y and z
 // patterns only) has its own layout a + Q1 b + Q2 c and per-cell skew SKEW2
-// in a separate region; GPAD pads the per-cell geometry block in shared
-// memory (elements); MINB is the resident-block target handed to the
+// in a separate region; MINB is the resident-block target handed to the
 // register allocator.
 struct PackParams {
-  int W, K, GROUPS, P1, P2, SKEW, GPAD, MINB, Q1, Q2, SKEW2;
+  int W, K, GROUPS, P1, P2, SKEW, MINB, Q1, Q2, SKEW2;
 };
 
 constexpr PackParams pack_params(int n, int elem)
 {
-  return elem == 4 ? (n == 2   ? PackParams{1, 8, 4, 2, 5, 0, 4, 1, 2, 6, 0}
-                      : n == 3 ? PackParams{2, 7, 2, 3, 9, 5, 4, 1, 3, 11, 8}
-                      : n == 4 ? PackParams{1, 2, 4, 4, 19, 24, 16, 1, 4, 20, 0}
-                      : n == 5 ? PackParams{4, 5, 2, 5, 25, 3, 12, 4, 5, 37, 0}
-                      : n == 6 ? PackParams{7, 6, 1, 7, 42, 4, 20, 1, 6, 38, 0}
-                      : n == 7 ? PackParams{5, 3, 1, 7, 56, 1, 0, 1, 7, 52, 5}
-                      : n == 8 ? PackParams{2, 1, 2, 9, 72, 0, 0, 1, 8, 72, 0}
-                               : PackParams{8, 3, 1, 9, 81, 7, 0, 1, 9, 85, 20})
-                   : (n == 2   ? PackParams{1, 8, 4, 2, 5, 0, 4, 1, 2, 6, 0}
-                      : n == 3 ? PackParams{2, 7, 2, 3, 18, 13, 8, 1, 3, 19, 0}
-                      : n == 4 ? PackParams{1, 2, 4, 4, 19, 0, 0, 1, 4, 20, 0}
-                      : n == 5 ? PackParams{4, 5, 1, 5, 25, 3, 0, 1, 5, 37, 0}
-                      : n == 6 ? PackParams{7, 6, 1, 7, 42, 4, 4, 1, 6, 38, 0}
-                      : n == 7 ? PackParams{5, 3, 1, 7, 49, 9, 0, 1, 7, 55, 0}
-                      : n == 8 ? PackParams{2, 1, 2, 9, 72, 0, 0, 1, 8, 72, 0}
-                               : PackParams{3, 1, 2, 9, 81, 0, 0, 1, 9, 89, 0});
+  return elem == 4 ? (n == 2   ? PackParams{1, 8, 4, 2, 5, 0, 1, 2, 6, 0}
+                      : n == 3 ? PackParams{2, 7, 2, 3, 9, 5, 1, 3, 11, 8}
+                      : n == 4 ? PackParams{1, 2, 4, 4, 19, 24, 1, 4, 20, 0}
+                      : n == 5 ? PackParams{4, 5, 2, 5, 25, 3, 4, 5, 37, 0}
+                      : n == 6 ? PackParams{7, 6, 1, 7, 42, 4, 1, 6, 38, 0}
+                      : n == 7 ? PackParams{5, 3, 1, 7, 56, 1, 1, 7, 52, 5}
+                      : n == 8 ? PackParams{2, 1, 2, 9, 72, 0, 1, 8, 72, 0}
+                               : PackParams{8, 3, 1, 9, 81, 7, 1, 9, 85, 20})
+                   : (n == 2   ? PackParams{1, 8, 4, 2, 5, 0, 1, 2, 6, 0}
+                      : n == 3 ? PackParams{2, 7, 2, 3, 18, 13, 1, 3, 19, 0}
+                      : n == 4 ? PackParams{1, 2, 4, 4, 19, 0, 1, 4, 20, 0}
+                      : n == 5 ? PackParams{4, 5, 1, 5, 25, 3, 1, 5, 37, 0}
+                      : n == 6 ? PackParams{7, 6, 1, 7, 42, 4, 1, 6, 38, 0}
+                      : n == 7 ? PackParams{5, 3, 1, 7, 49, 9, 1, 7, 55, 0}
+                      : n == 8 ? PackParams{2, 1, 2, 9, 72, 0, 1, 8, 72, 0}
+                               : PackParams{3, 1, 2, 9, 81, 0, 1, 9, 89, 0});
 }
 
 template <int N, typename T>
@@ -73,16 +76,34 @@ struct LineCfg {
   static constexpr int RS = 2 * SLAB + PP.SKEW;    // B0 + B1 region per cell
   static constexpr int RS2 = Q2 * N + PP.SKEW2;    // B2 region per cell
   static constexpr int AL = 16 / (int)sizeof(T);   // elements per 16 bytes
-  static constexpr int GEO = (6 * N3 + 3) / 4 * 4; // geometry block in global memory
-  static constexpr int GS = GEO + PP.GPAD;         // geometry block in shared memory
+  static constexpr int KN2 = K * N2;               // lanes that own a line
+  static constexpr int GB = (6 * N * KN2 + AL - 1) / AL * AL; // geometry block of K cells
   static constexpr int GT = 32 * W;                // threads per group
   static constexpr long long GROUP_BYTES =
-      ((long long)K * (GS + RS + RS2) * (long long)sizeof(T) + 127) / 128 * 128;
-  static_assert(K * N2 <= GT, "cells do not fit the group");
+      ((long long)(GB + K * (RS + RS2)) * (long long)sizeof(T) + 127) / 128 * 128;
+  static_assert(KN2 <= GT, "cells do not fit the group");
   static_assert((P1 + 1) * (N - 1) < P2, "slab padding overlaps");
   static_assert((Q1 + 1) * (N - 1) < Q2 && Q1 >= N, "B2 slab padding overlaps");
-  static_assert(GS % AL == 0, "geometry blocks must stay 16-byte aligned");
+  static_assert(GB * sizeof(T) < (1u << 20), "geometry block exceeds the mbarrier transaction count");
 };
+
+// number of cells of colour `color` and the offset of its first geometry
+// block in the walk-ordered layout (elements)
+template <int N, typename T>
+long long line_color_geometry(const int (&nc)[3], int color, long long *count)
+{
+  using Cfg = LineCfg<N, T>;
+  long long base = 0;
+  for (int c = 0;; ++c) {
+    const long long cnt = (long long)((nc[0] - (c & 1) + 1) / 2) * ((nc[1] - ((c >> 1) & 1) + 1) / 2) *
+                          ((nc[2] - ((c >> 2) & 1) + 1) / 2);
+    if (c == color) {
+      *count = cnt;
+      return base;
+    }
+    base += (cnt + Cfg::K - 1) / Cfg::K * Cfg::GB;
+  }
+}
 
 template <int N, typename T>
 struct LineArgs {
@@ -90,7 +111,7 @@ struct LineArgs {
   T w[N];
   const T *__restrict__ x;
   T *__restrict__ y;
-  const T *__restrict__ geo;    // natural layout [cell][6][n^3], block GEO elements
+  const T *__restrict__ geo;    // this colour's walk-ordered geometry blocks (GB elements each)
   const T *__restrict__ kappa;  // [cell][n^3] or null
   int nc[3];
   int Nx, plane;                // nodes per x line, per z plane
@@ -117,16 +138,18 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
   unsigned char *gbase = smem_raw + 128 + grp * Cfg::GROUP_BYTES;
   uint64_t *bar = bars + grp;
 
-  // Lanes beyond K n^2 run line 0 of cell 0 with every store predicated
-  // off, so the sweeps carry no divergent branches.
+  // Lanes beyond K n^2 repeat the last used lane's line with every store
+  // predicated off, so the sweeps carry no divergent branches and their
+  // shared-memory addresses coincide with a lane of the same warp (a
+  // broadcast, no extra bank conflict).
   const bool used = t < K * N2;
-  const int tt = used ? t : 0;
+  const int tt = used ? t : K * N2 - 1;
   const int k = tt / N2, l = tt % N2;
   const int a = l % N, b = l / N; // z column (a,b) / y line (a,c=b) / x line (b'=a, c'=b)
-  T *geo_s = reinterpret_cast<T *>(gbase) + k * Cfg::GS;
-  T *B0 = reinterpret_cast<T *>(gbase) + K * Cfg::GS + k * Cfg::RS;
+  T *geo_s = reinterpret_cast<T *>(gbase);
+  T *B0 = reinterpret_cast<T *>(gbase) + Cfg::GB + k * Cfg::RS;
   T *B1 = B0 + SLAB;
-  T *B2 = reinterpret_cast<T *>(gbase) + K * (Cfg::GS + Cfg::RS) + k * Cfg::RS2;
+  T *B2 = reinterpret_cast<T *>(gbase) + Cfg::GB + K * Cfg::RS + k * Cfg::RS2;
   const int zc = a + P1 * b;      // z column base
   const int xl = P1 * a + P2 * b; // x line (b'=a, c'=b) base, stride 1
   const int yl = a + P2 * b;      // y line (a, c=b) base, stride P1
@@ -138,7 +161,8 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
   const long long ng = (long long)gridDim.x * Cfg::GROUPS;
   const long long gid = (long long)blockIdx.x * Cfg::GROUPS + grp;
   const long long step = ng * K;
-  constexpr uint32_t geo_bytes = (uint32_t)(Cfg::GEO * sizeof(T));
+  constexpr uint32_t geo_bytes = (uint32_t)(Cfg::GB * sizeof(T));
+  long long blk = gid; // geometry block of the current step (ordinal / K)
 
   // position (mi, mj, mk) of this lane's first cell in the colour's index
   // space; later cells follow by a division-free strided walk
@@ -157,15 +181,13 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
     pol = l2_policy_evict_first();
     if (t == 0) {
       mbar_init(bar, 1);
-      if (gid * K < A.count)
-        mbar_arrive_expect_tx(bar, geo_bytes * (uint32_t)min((long long)K, A.count - gid * K));
       fence_mbar_init();
+      if (gid * K < A.count) {
+        mbar_arrive_expect_tx(bar, geo_bytes);
+        tma_load_1d_hint(geo_s, A.geo + blk * Cfg::GB, geo_bytes, bar, pol);
+      }
     }
     cell_group_sync<W>(grp);
-    if (used && l == 0 && o < A.count) {
-      const long long cell = ((long long)(2 * mk + A.cz) * A.nc[1] + (2 * mj + A.cy)) * A.nc[0] + (2 * mi + A.cx);
-      tma_load_1d_hint(geo_s, A.geo + cell * Cfg::GEO, geo_bytes, bar, pol);
-    }
   }
   pdl_trigger();
   uint32_t parity = 0;
@@ -233,8 +255,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
       parity ^= 1;
       // the next step's copies are issued after the group barrier below;
       // announce their bytes now (the barrier is already in its next phase)
-      if (t == 0 && more)
-        mbar_arrive_expect_tx(bar, geo_bytes * (uint32_t)min((long long)K, A.count - (o0 + step)));
+      if (t == 0 && more) mbar_arrive_expect_tx(bar, geo_bytes);
     }
     T tz[N];
     {
@@ -245,8 +266,9 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
         const T gx = B0[s], gy = B2[zc2 + Q2 * c];
         T tx, ty, tzc;
         if (DEFORMED) {
-          const T *Gq = geo_s + c * N2 + l;
-          const T g0 = Gq[0], g1 = Gq[N3], g2 = Gq[2 * N3], g3 = Gq[3 * N3], g4 = Gq[4 * N3], g5 = Gq[5 * N3];
+          constexpr int GC = N * Cfg::KN2; // component stride of the block
+          const T *Gq = geo_s + c * Cfg::KN2 + tt;
+          const T g0 = Gq[0], g1 = Gq[GC], g2 = Gq[2 * GC], g3 = Gq[3 * GC], g4 = Gq[4 * GC], g5 = Gq[5 * GC];
           tx = gx * g0 + gy * g3 + gz[c] * g4;
           ty = gx * g3 + gy * g1 + gz[c] * g5;
           tzc = gx * g4 + gy * g5 + gz[c] * g2;
@@ -276,10 +298,8 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
     cell_group_sync<W>(grp);
     // geometry buffers free: fetch the next step's blocks
     const bool nvalid = used && o + step < A.count;
-    if (DEFORMED && more && nvalid && l == 0) {
-      const long long cell = ((long long)(2 * nk + A.cz) * A.nc[1] + (2 * nj + A.cy)) * A.nc[0] + (2 * ni + A.cx);
-      tma_load_1d_hint(geo_s, A.geo + cell * Cfg::GEO, geo_bytes, bar, pol);
-    }
+    blk += ng;
+    if (DEFORMED && more && t == 0) tma_load_1d_hint(geo_s, A.geo + blk * Cfg::GB, geo_bytes, bar, pol);
     // loads overlapped with the integration sweeps: the y values this
     // column adds to, and the next cell's x column
     if (!y_ready) {
@@ -333,6 +353,66 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
   if (!y_ready) pdl_wait();
 }
 
+// walk-ordered copy of one colour's geometry: entry (blk, e, c, k n^2 + l) =
+// component e at point (l, c) of the colour's cell with ordinal blk K + k;
+// zero past the colour's last cell and in the block padding
+template <int N, typename T>
+__global__ void line_pack_geometry_kernel(const double *__restrict__ G, long long gstride, T *__restrict__ out,
+                                          long long total, long long count, int nc0, int nc1, int cx, int cy,
+                                          int cz, int mx, int my)
+{
+  using Cfg = LineCfg<N, T>;
+  constexpr int KN2 = Cfg::KN2, N2 = Cfg::N2;
+  const long long str = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += str) {
+    const long long blk = i / Cfg::GB;
+    const int r = int(i - blk * Cfg::GB);
+    T v = T(0);
+    if (r < 6 * N * KN2) {
+      const int ec = r / KN2, tl = r - ec * KN2;
+      const int e = ec / N, c = ec - e * N;
+      const int k = tl / N2, l = tl - k * N2;
+      const long long o = blk * Cfg::K + k;
+      if (o < count) {
+        const long long q = o / mx, mk = q / my;
+        const long long mi = o - q * mx, mj = q - mk * my;
+        const long long cell = ((2 * mk + cz) * nc1 + (2 * mj + cy)) * nc0 + (2 * mi + cx);
+        v = T(G[cell * gstride + (long long)e * Cfg::N3 + c * N2 + l]);
+      }
+    }
+    out[i] = v;
+  }
+}
+
+template <int N, typename T>
+int line_pack_impl(sf_op *op, DevBuf &buf)
+{
+  using Cfg = LineCfg<N, T>;
+  int nc[3];
+  for (int d = 0; d < 3; ++d) nc[d] = op->desc.n_cells[d];
+  long long cnt7 = 0;
+  const long long total = line_color_geometry<N, T>(nc, 7, &cnt7) + (cnt7 + Cfg::K - 1) / Cfg::K * Cfg::GB;
+  const size_t bytes = (size_t)total * sizeof(T);
+  if (buf.bytes != bytes) {
+    const int e = buf.alloc(bytes);
+    if (e != SF_OK) return e;
+  }
+  for (int color = 0; color < 8; ++color) {
+    long long count = 0;
+    const long long base = line_color_geometry<N, T>(nc, color, &count);
+    const long long n = (count + Cfg::K - 1) / Cfg::K * Cfg::GB;
+    if (n == 0) continue;
+    const int cx = color & 1, cy = (color >> 1) & 1, cz = (color >> 2) & 1;
+    const int mx = (nc[0] - cx + 1) / 2, my = (nc[1] - cy + 1) / 2;
+    const long long blocks = std::min<long long>((n + 255) / 256, 152 * 32);
+    line_pack_geometry_kernel<N, T><<<(unsigned)blocks, 256>>>((const double *)op->geo64.ptr, op->geo_stride,
+                                                              (T *)buf.ptr + base, n, count, nc[0], nc[1], cx,
+                                                              cy, cz, mx, my);
+    SF_CUDA_TRY(cudaGetLastError());
+  }
+  return SF_OK;
+}
+
 template <int N, typename T>
 int line_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
 {
@@ -354,10 +434,10 @@ int line_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
   A.y = y;
   A.err = (int *)op->dev_err.ptr;
   const bool deformed = op->deformed, kap = op->has_kappa;
-  A.geo = (const T *)(sizeof(T) == 8 ? op->geo64.ptr : op->geo32.ptr);
+  const T *geo = (const T *)(sizeof(T) == 8 ? op->geoLine64.ptr : op->geoLine32.ptr);
   A.kappa = (const T *)(sizeof(T) == 8 ? op->kap64.ptr : op->kap32.ptr);
-  if (deformed && (!A.geo || op->geo_stride != Cfg::GEO)) {
-    set_error("line kernel: geometry missing or with an unexpected block size");
+  if (deformed && !geo) {
+    set_error("line kernel: walk-ordered geometry missing");
     return SF_ERR_STATE;
   }
   if (kap && !A.kappa) {
@@ -384,8 +464,8 @@ int line_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
     A.cz = (color >> 2) & 1;
     A.mx = (A.nc[0] - A.cx + 1) / 2;
     A.my = (A.nc[1] - A.cy + 1) / 2;
-    const int mz = (A.nc[2] - A.cz + 1) / 2;
-    A.count = (long long)A.mx * A.my * mz;
+    const long long gbase = line_color_geometry<N, T>(A.nc, color, &A.count);
+    A.geo = deformed ? geo + gbase : nullptr;
     if (A.count == 0) continue;
     const long long steps = (A.count + Cfg::K - 1) / Cfg::K;
     const long long blocks =
@@ -416,7 +496,29 @@ int line_vmult_n(const sf_op *op, int prec, const void *x, void *y, cudaStream_t
   return line_vmult_impl<N, float>(op, (const float *)x, (float *)y, st);
 }
 
+template <int N>
+int line_pack_n(sf_op *op, int prec)
+{
+  if (prec == SF_FP64) return line_pack_impl<N, double>(op, op->geoLine64);
+  return line_pack_impl<N, float>(op, op->geoLine32);
+}
+
 } // namespace
+
+int pack_line_geometry(sf_op *op, int prec)
+{
+  switch (op->n) {
+  case 2: return line_pack_n<2>(op, prec);
+  case 3: return line_pack_n<3>(op, prec);
+  case 4: return line_pack_n<4>(op, prec);
+  case 5: return line_pack_n<5>(op, prec);
+  case 6: return line_pack_n<6>(op, prec);
+  case 7: return line_pack_n<7>(op, prec);
+  case 8: return line_pack_n<8>(op, prec);
+  case 9: return line_pack_n<9>(op, prec);
+  default: set_error("unsupported degree"); return SF_ERR_UNSUPPORTED;
+  }
+}
 
 int launch_cont_vmult_line(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
 {

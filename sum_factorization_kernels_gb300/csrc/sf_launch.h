@@ -16,6 +16,8 @@ int launch_cont_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st)
 
 // sf_laplace_line.cu (all degrees, FP64 and FP32)
 int launch_cont_vmult_line(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st);
+// walk-ordered copy of the FP64 geometry for the line kernel (geoLine64 / geoLine32)
+int pack_line_geometry(sf_op *op, int prec);
 
 // sf_laplace_pair.cu (FP32, two cells per thread in packed FP32x2)
 bool pair_path(const sf_op *op, int prec);
