@@ -21,10 +21,10 @@
 // colour launches, first-touch store / add, programmatic dependent launch
 // for colours 1..7 (see sf_cont_column.cuh).
 //
-// The slab paddings (P1, P2, Q1, Q2, per-cell skews) come from a search of
-// the shared-memory bank conflicts of the access patterns for each (n, W,
-// K); slab B2, read and written only along y lines and z columns, lives in
-// its own region with a layout that is conflict-free for those two patterns.
+// The lane-to-cell map, the line each lane owns in the x and y sweeps and
+// the strides of the three slabs come from a search of the shared-memory
+// bank conflicts of the access patterns for each (n, W, K); slab B2, read
+// and written only along y lines and z columns, has a layout of its own.
 #include "sf_cont_column.cuh"
 #include "sf_device.cuh"
 #include "sf_internal.h"
@@ -36,54 +36,74 @@ namespace sf {
 
 namespace {
 
-// W warps per group, K cells per group, GROUPS groups per block; slab
-// index (a, b, c) = a + P1 b + P2 c for slabs B0 and B1 (which see x, y and
-// z line patterns), SKEW pads their per-cell region; slab B2 (y and z
-// patterns only) has its own layout a + Q1 b + Q2 c and per-cell skew SKEW2
-// in a separate region; MINB is the resident-block target handed to the
-// register allocator.
+// Shared-memory layout of one slab: entry (x, y, z) of cell k at
+// k RS + SX x + SY y + SZ z.
+struct SlabLayout {
+  int SX, SY, SZ, RS;
+};
+
+// W warps per group, K cells per group, GROUPS groups per block, MINB the
+// resident-block target handed to the register allocator.  INTER: lane t
+// works on cell t % K, line t / K (else cell t / n^2, line t % n^2).  The
+// lane with line l = a + n b owns z column (a, b), in the x sweeps the x
+// line (y, z) = (a, b), or (b, a) with XS, in the y sweeps the y line
+// (x, z) = (a, b), or (b, a) with YS.  Slabs B0 and B1 see x, y and z
+// patterns, B2 y and z patterns; each lives in a region of its own.
 struct PackParams {
-  int W, K, GROUPS, P1, P2, SKEW, MINB, Q1, Q2, SKEW2;
+  int W, K, GROUPS, MINB, INTER, XS, YS;
+  SlabLayout B0, B1, B2;
 };
 
 constexpr PackParams pack_params(int n, int elem)
 {
-  return elem == 4 ? (n == 2   ? PackParams{1, 8, 4, 2, 5, 0, 1, 2, 6, 0}
-                      : n == 3 ? PackParams{2, 7, 2, 3, 9, 5, 1, 3, 11, 8}
-                      : n == 4 ? PackParams{1, 2, 4, 4, 19, 24, 1, 4, 20, 0}
-                      : n == 5 ? PackParams{4, 5, 2, 5, 25, 3, 4, 5, 37, 0}
-                      : n == 6 ? PackParams{7, 6, 1, 7, 42, 4, 1, 6, 38, 0}
-                      : n == 7 ? PackParams{5, 3, 1, 7, 56, 1, 1, 7, 52, 5}
-                      : n == 8 ? PackParams{2, 1, 2, 9, 72, 0, 1, 8, 72, 0}
-                               : PackParams{8, 3, 1, 9, 81, 7, 1, 9, 85, 20})
-                   : (n == 2   ? PackParams{1, 8, 4, 2, 5, 0, 1, 2, 6, 0}
-                      : n == 3 ? PackParams{2, 7, 2, 3, 18, 13, 1, 3, 19, 0}
-                      : n == 4 ? PackParams{1, 2, 4, 4, 19, 0, 1, 4, 20, 0}
-                      : n == 5 ? PackParams{4, 5, 1, 5, 25, 3, 1, 5, 37, 0}
-                      : n == 6 ? PackParams{7, 6, 1, 7, 42, 4, 1, 6, 38, 0}
-                      : n == 7 ? PackParams{5, 3, 1, 7, 49, 9, 1, 7, 55, 0}
-                      : n == 8 ? PackParams{2, 1, 2, 9, 72, 0, 1, 8, 72, 0}
-                               : PackParams{3, 1, 2, 9, 81, 0, 1, 9, 89, 0});
+  return elem == 4 ? (n == 2   ? PackParams{1, 8, 4, 1, 0, 0, 0, {1, 2, 5, 20}, {1, 2, 5, 20}, {1, 2, 6, 12}}
+                      : n == 3 ? PackParams{2, 7, 2, 1, 0, 0, 0, {1, 3, 9, 59}, {1, 3, 9, 59}, {1, 3, 11, 41}}
+                      : n == 4 ? PackParams{1, 2, 4, 1, 0, 0, 0, {1, 4, 19, 176}, {1, 4, 19, 176}, {1, 4, 20, 80}}
+                      : n == 5 ? PackParams{4, 5, 2, 4, 1, 1, 0, {1, 5, 33, 173}, {1, 5, 33, 173}, {1, 5, 37, 173}}
+                      : n == 6 ? PackParams{7, 6, 1, 1, 0, 0, 0, {1, 7, 42, 508}, {1, 7, 42, 508}, {1, 6, 38, 228}}
+                      : n == 7 ? PackParams{5, 3, 1, 1, 0, 0, 0, {1, 7, 56, 785}, {1, 7, 56, 785}, {1, 7, 52, 369}}
+                      : n == 8 ? PackParams{2, 1, 2, 1, 0, 0, 0, {1, 9, 72, 1152}, {1, 9, 72, 1152}, {1, 8, 72, 576}}
+                               : PackParams{8, 3, 1, 1, 0, 0, 0, {1, 9, 81, 1465}, {1, 9, 81, 1465}, {1, 9, 85, 785}})
+                   : (n == 2   ? PackParams{1, 8, 4, 1, 0, 0, 0, {1, 2, 5, 20}, {1, 2, 5, 20}, {1, 2, 6, 12}}
+                      : n == 3 ? PackParams{2, 7, 2, 1, 0, 0, 0, {1, 3, 18, 121}, {1, 3, 18, 121}, {1, 3, 19, 57}}
+                      : n == 4 ? PackParams{1, 2, 4, 1, 0, 0, 0, {1, 4, 19, 152}, {1, 4, 19, 152}, {1, 4, 20, 80}}
+                      : n == 5 ? PackParams{4, 5, 1, 1, 0, 0, 0, {1, 5, 25, 253}, {1, 5, 25, 253}, {1, 5, 37, 185}}
+                      : n == 6 ? PackParams{7, 6, 1, 1, 0, 0, 0, {1, 7, 42, 508}, {1, 7, 42, 508}, {1, 6, 38, 228}}
+                      : n == 7 ? PackParams{5, 3, 1, 1, 0, 0, 0, {1, 7, 49, 695}, {1, 7, 49, 695}, {1, 7, 55, 385}}
+                      : n == 8 ? PackParams{2, 1, 2, 1, 0, 0, 0, {1, 9, 72, 1152}, {1, 9, 72, 1152}, {1, 8, 72, 576}}
+                               : PackParams{3, 1, 2, 1, 0, 0, 0, {1, 9, 81, 1458}, {1, 9, 81, 1458}, {1, 9, 89, 801}});
+}
+
+// every entry of an n^3 slab lands on its own word inside RS
+constexpr bool slab_fits(int n, SlabLayout L)
+{
+  bool seen[4096] = {};
+  if (L.RS > 4096) return false;
+  for (int z = 0; z < n; ++z)
+    for (int y = 0; y < n; ++y)
+      for (int x = 0; x < n; ++x) {
+        const int i = L.SX * x + L.SY * y + L.SZ * z;
+        if (i < 0 || i >= L.RS || seen[i]) return false;
+        seen[i] = true;
+      }
+  return true;
 }
 
 template <int N, typename T>
 struct LineCfg {
   static constexpr PackParams PP = pack_params(N, (int)sizeof(T));
-  static constexpr int W = PP.W, K = PP.K, GROUPS = PP.GROUPS, P1 = PP.P1, P2 = PP.P2;
+  static constexpr int W = PP.W, K = PP.K, GROUPS = PP.GROUPS;
   static constexpr int N2 = N * N, N3 = N * N * N;
-  static constexpr int Q1 = PP.Q1, Q2 = PP.Q2;
-  static constexpr int SLAB = P2 * N;              // elements per slab B0, B1
-  static constexpr int RS = 2 * SLAB + PP.SKEW;    // B0 + B1 region per cell
-  static constexpr int RS2 = Q2 * N + PP.SKEW2;    // B2 region per cell
+  static constexpr SlabLayout L0 = PP.B0, L1 = PP.B1, L2 = PP.B2;
+  static constexpr int RS = L0.RS + L1.RS + L2.RS; // slab words per cell
   static constexpr int AL = 16 / (int)sizeof(T);   // elements per 16 bytes
   static constexpr int KN2 = K * N2;               // lanes that own a line
   static constexpr int GB = (6 * N * KN2 + AL - 1) / AL * AL; // geometry block of K cells
   static constexpr int GT = 32 * W;                // threads per group
   static constexpr long long GROUP_BYTES =
-      ((long long)(GB + K * (RS + RS2)) * (long long)sizeof(T) + 127) / 128 * 128;
+      ((long long)(GB + K * RS) * (long long)sizeof(T) + 127) / 128 * 128;
   static_assert(KN2 <= GT, "cells do not fit the group");
-  static_assert((P1 + 1) * (N - 1) < P2, "slab padding overlaps");
-  static_assert((Q1 + 1) * (N - 1) < Q2 && Q1 >= N, "B2 slab padding overlaps");
+  static_assert(slab_fits(N, L0) && slab_fits(N, L1) && slab_fits(N, L2), "slab entries overlap");
   static_assert(GB * sizeof(T) < (1u << 20), "geometry block exceeds the mbarrier transaction count");
 };
 
@@ -131,7 +151,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
 {
   using Cfg = LineCfg<N, T>;
   constexpr int N2 = Cfg::N2, N3 = Cfg::N3, K = Cfg::K, W = Cfg::W, GT = Cfg::GT;
-  constexpr int P1 = Cfg::P1, P2 = Cfg::P2, SLAB = Cfg::SLAB, Q1 = Cfg::Q1, Q2 = Cfg::Q2;
+  constexpr SlabLayout L0 = Cfg::L0, L1 = Cfg::L1, L2 = Cfg::L2;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw);
   const int grp = threadIdx.x / GT, t = threadIdx.x % GT;
@@ -144,17 +164,18 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
   // broadcast, no extra bank conflict).
   const bool used = t < K * N2;
   const int tt = used ? t : K * N2 - 1;
-  const int k = tt / N2, l = tt % N2;
-  const int a = l % N, b = l / N; // z column (a,b) / y line (a,c=b) / x line (b'=a, c'=b)
+  const int k = Cfg::PP.INTER ? tt % K : tt / N2, l = Cfg::PP.INTER ? tt / K : tt % N2;
+  const int a = l % N, b = l / N; // z column (a, b)
+  const int xy = Cfg::PP.XS ? b : a, xz = Cfg::PP.XS ? a : b; // x line (y, z)
+  const int yx = Cfg::PP.YS ? b : a, yz = Cfg::PP.YS ? a : b; // y line (x, z)
   T *geo_s = reinterpret_cast<T *>(gbase);
-  T *B0 = reinterpret_cast<T *>(gbase) + Cfg::GB + k * Cfg::RS;
-  T *B1 = B0 + SLAB;
-  T *B2 = reinterpret_cast<T *>(gbase) + Cfg::GB + K * Cfg::RS + k * Cfg::RS2;
-  const int zc = a + P1 * b;      // z column base
-  const int xl = P1 * a + P2 * b; // x line (b'=a, c'=b) base, stride 1
-  const int yl = a + P2 * b;      // y line (a, c=b) base, stride P1
-  const int zc2 = a + Q1 * b;     // the same z column in B2, stride Q2
-  const int yl2 = a + Q2 * b;     // the same y line in B2, stride Q1
+  T *B0 = reinterpret_cast<T *>(gbase) + Cfg::GB + k * L0.RS;
+  T *B1 = reinterpret_cast<T *>(gbase) + Cfg::GB + K * L0.RS + k * L1.RS;
+  T *B2 = reinterpret_cast<T *>(gbase) + Cfg::GB + K * (L0.RS + L1.RS) + k * L2.RS;
+  // line bases in each slab (z column stride SZ, x line stride SX, y line stride SY)
+  const int zc0 = L0.SX * a + L0.SY * b, xl0 = L0.SY * xy + L0.SZ * xz, yl0 = L0.SX * yx + L0.SZ * yz;
+  const int zc1 = L1.SX * a + L1.SY * b, xl1 = L1.SY * xy + L1.SZ * xz, yl1 = L1.SX * yx + L1.SZ * yz;
+  const int zc2 = L2.SX * a + L2.SY * b, yl2 = L2.SX * yx + L2.SZ * yz;
   const int plane = A.plane;
   const int toff = b * A.Nx + a;  // node (a, b, 0) relative to the cell's node (0, 0, 0)
 
@@ -218,34 +239,34 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
     eo_apply<N, 1>(A.S, xv, v);
 #pragma unroll
     for (int c = 0; c < N; ++c)
-      if (used) B0[zc + P2 * c] = v[c];
+      if (used) B0[zc0 + L0.SZ * c] = v[c];
     cell_group_sync<W>(grp);
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = B0[xl + m];
+    for (int m = 0; m < N; ++m) v[m] = B0[xl0 + L0.SX * m];
     eo_apply<N, 1>(A.S, v, v);
 #pragma unroll
     for (int m = 0; m < N; ++m)
-      if (used) B0[xl + m] = v[m];
+      if (used) B0[xl0 + L0.SX * m] = v[m];
     cell_group_sync<W>(grp);
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = B0[yl + P1 * m];
+    for (int m = 0; m < N; ++m) v[m] = B0[yl0 + L0.SY * m];
     eo_apply<N, 1>(A.S, v, v);
     eo_apply<N, -1>(A.D, v, g);
 #pragma unroll
     for (int m = 0; m < N; ++m) {
-      if (used) B1[yl + P1 * m] = v[m];
-      if (used) B2[yl2 + Q1 * m] = g[m];
+      if (used) B1[yl1 + L1.SY * m] = v[m];
+      if (used) B2[yl2 + L2.SY * m] = g[m];
     }
     cell_group_sync<W>(grp);
     // ---- D_x into B0; D_z stays in registers (same thread, same column) ----
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = B1[xl + m];
+    for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
     eo_apply<N, -1>(A.D, v, g);
 #pragma unroll
     for (int m = 0; m < N; ++m)
-      if (used) B0[xl + m] = g[m];
+      if (used) B0[xl0 + L0.SX * m] = g[m];
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = B1[zc + P2 * m];
+    for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
     eo_apply<N, -1>(A.D, v, gz);
     cell_group_sync<W>(grp);
     // ---- quadrature points of column (a,b) ----
@@ -262,8 +283,8 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
       const T wab = A.w[a] * A.w[b];
 #pragma unroll
       for (int c = 0; c < N; ++c) {
-        const int s = zc + P2 * c;
-        const T gx = B0[s], gy = B2[zc2 + Q2 * c];
+        const int s = zc0 + L0.SZ * c;
+        const T gx = B0[s], gy = B2[zc2 + L2.SZ * c];
         T tx, ty, tzc;
         if (DEFORMED) {
           constexpr int GC = N * Cfg::KN2; // component stride of the block
@@ -286,13 +307,13 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
           tzc *= kq;
         }
         if (used) B0[s] = tx;
-        if (used) B2[zc2 + Q2 * c] = ty;
+        if (used) B2[zc2 + L2.SZ * c] = ty;
         tz[c] = tzc;
       }
       eo_apply<N, -1>(A.DT, tz, g);
 #pragma unroll
       for (int c = 0; c < N; ++c)
-        if (used) B1[zc + P2 * c] = g[c];
+        if (used) B1[zc1 + L1.SZ * c] = g[c];
     }
     if (DEFORMED) fence_proxy_async_smem();
     cell_group_sync<W>(grp);
@@ -313,33 +334,33 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
     const long long nnb = cell_node_base<N>(2 * ni + A.cx, 2 * nj + A.cy, 2 * nk + A.cz, A.Nx, plane) + toff;
     gather_column<N, T>(A.x + nnb, plane, nmsk.keep, xv);
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = B0[xl + m];
+    for (int m = 0; m < N; ++m) v[m] = B0[xl0 + L0.SX * m];
     eo_apply<N, -1>(A.DT, v, g);
 #pragma unroll
     for (int m = 0; m < N; ++m) {
-      const T s = B1[xl + m] + g[m];
-      if (used) B1[xl + m] = s;
+      const T s = B1[xl1 + L1.SX * m] + g[m];
+      if (used) B1[xl1 + L1.SX * m] = s;
     }
     cell_group_sync<W>(grp);
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = B2[yl2 + Q1 * m];
+    for (int m = 0; m < N; ++m) v[m] = B2[yl2 + L2.SY * m];
     eo_apply<N, -1>(A.DT, v, g);
 #pragma unroll
-    for (int m = 0; m < N; ++m) g[m] += B1[yl + P1 * m];
+    for (int m = 0; m < N; ++m) g[m] += B1[yl1 + L1.SY * m];
     eo_apply<N, 1>(A.ST, g, v);
 #pragma unroll
     for (int m = 0; m < N; ++m)
-      if (used) B1[yl + P1 * m] = v[m];
+      if (used) B1[yl1 + L1.SY * m] = v[m];
     cell_group_sync<W>(grp);
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = B1[xl + m];
+    for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
     eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
     for (int m = 0; m < N; ++m)
-      if (used) B1[xl + m] = v[m];
+      if (used) B1[xl1 + L1.SX * m] = v[m];
     cell_group_sync<W>(grp);
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = B1[zc + P2 * m];
+    for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
     eo_apply<N, 1>(A.ST, v, v);
     // ---- scatter the z column: first colour stores, later ones add ----
     if (valid) store_column<N, T>(A.y + nb, A.x + nb, plane, msk.keep, v, yo);
@@ -353,9 +374,10 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
   if (!y_ready) pdl_wait();
 }
 
-// walk-ordered copy of one colour's geometry: entry (blk, e, c, k n^2 + l) =
-// component e at point (l, c) of the colour's cell with ordinal blk K + k;
-// zero past the colour's last cell and in the block padding
+// walk-ordered copy of one colour's geometry: entry (blk, e, c, t) =
+// component e at point (l, c) of the colour's cell with ordinal blk K + k,
+// (k, l) the cell and line of lane t; zero past the colour's last cell and
+// in the block padding
 template <int N, typename T>
 __global__ void line_pack_geometry_kernel(const double *__restrict__ G, long long gstride, T *__restrict__ out,
                                           long long total, long long count, int nc0, int nc1, int cx, int cy,
@@ -371,7 +393,7 @@ __global__ void line_pack_geometry_kernel(const double *__restrict__ G, long lon
     if (r < 6 * N * KN2) {
       const int ec = r / KN2, tl = r - ec * KN2;
       const int e = ec / N, c = ec - e * N;
-      const int k = tl / N2, l = tl - k * N2;
+      const int k = Cfg::PP.INTER ? tl % Cfg::K : tl / N2, l = Cfg::PP.INTER ? tl / Cfg::K : tl % N2;
       const long long o = blk * Cfg::K + k;
       if (o < count) {
         const long long q = o / mx, mk = q / my;
