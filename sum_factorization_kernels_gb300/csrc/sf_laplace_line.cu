@@ -61,9 +61,9 @@ constexpr PackParams pack_params(int n, int elem)
                       : n == 4 ? PackParams{1, 2, 4, 1, 0, 0, 0, {1, 4, 19, 176}, {1, 4, 19, 176}, {1, 4, 20, 80}}
                       : n == 5 ? PackParams{4, 5, 2, 4, 1, 1, 0, {1, 5, 33, 173}, {1, 5, 33, 173}, {1, 5, 37, 173}}
                       : n == 6 ? PackParams{7, 6, 1, 1, 0, 0, 0, {1, 7, 42, 508}, {1, 7, 42, 508}, {1, 6, 38, 228}}
-                      : n == 7 ? PackParams{5, 3, 1, 1, 0, 0, 0, {1, 7, 56, 785}, {1, 7, 56, 785}, {1, 7, 52, 369}}
-                      : n == 8 ? PackParams{2, 1, 2, 1, 0, 0, 0, {1, 9, 72, 1152}, {1, 9, 72, 1152}, {1, 8, 72, 576}}
-                               : PackParams{8, 3, 1, 1, 0, 0, 0, {1, 9, 81, 1465}, {1, 9, 81, 1465}, {1, 9, 85, 785}})
+                      : n == 7 ? PackParams{5, 3, 1, 1, 1, 1, 0, {1, 7, 65, 459}, {1, 7, 65, 459}, {1, 7, 49, 363}}
+                      : n == 8 ? PackParams{2, 1, 2, 1, 0, 1, 0, {67, 8, 1, 533}, {67, 8, 1, 533}, {1, 8, 72, 568}}
+                               : PackParams{8, 3, 1, 1, 1, 1, 0, {1, 9, 97, 875}, {1, 9, 97, 875}, {1, 9, 105, 939}})
                    : (n == 2   ? PackParams{1, 8, 4, 1, 0, 0, 0, {1, 2, 5, 20}, {1, 2, 5, 20}, {1, 2, 6, 12}}
                       : n == 3 ? PackParams{2, 7, 2, 1, 0, 0, 0, {1, 3, 18, 121}, {1, 3, 18, 121}, {1, 3, 19, 57}}
                       : n == 4 ? PackParams{1, 2, 4, 1, 0, 0, 0, {1, 4, 19, 152}, {1, 4, 19, 152}, {1, 4, 20, 80}}
