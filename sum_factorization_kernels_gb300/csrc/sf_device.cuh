@@ -79,15 +79,18 @@ __device__ __forceinline__ T dot_row(const T (&row)[N], const T (&v)[N])
   return s;
 }
 
-// Synchronise the threads of one cell group.  A one-warp group uses
-// __syncwarp (no hardware barrier); larger groups use named barriers 1..3
-// with compile-time ids, so a block reserves only GROUPS + 1 of the SM's
-// barriers (a register id would reserve all 16 and cap residency).
-template <int G>
+// Synchronise the threads of one cell group of G warps (NGROUPS groups per
+// block).  A one-warp group uses __syncwarp (no hardware barrier); larger
+// groups use named barriers 1..4 with compile-time ids, so a block reserves
+// only NGROUPS + 1 of the SM's barriers (a register id would reserve all 16
+// and cap residency); a block of one group needs no branch on the group.
+template <int G, int NGROUPS = 4>
 __device__ __forceinline__ void cell_group_sync(int grp)
 {
   if (G == 1) {
     __syncwarp();
+  } else if (NGROUPS == 1) {
+    asm volatile("bar.sync 1, %0;" ::"n"(32 * G) : "memory");
   } else {
     constexpr int NT = 32 * G;
     if (grp == 0) asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");

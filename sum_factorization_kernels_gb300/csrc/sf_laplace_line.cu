@@ -59,7 +59,7 @@ constexpr PackParams pack_params(int n, int elem)
   return elem == 4 ? (n == 2   ? PackParams{1, 8, 4, 1, 0, 0, 0, {1, 2, 5, 20}, {1, 2, 5, 20}, {1, 2, 6, 12}}
                       : n == 3 ? PackParams{2, 7, 2, 1, 0, 0, 0, {1, 3, 9, 59}, {1, 3, 9, 59}, {1, 3, 11, 41}}
                       : n == 4 ? PackParams{1, 2, 4, 1, 0, 0, 0, {1, 4, 19, 176}, {1, 4, 19, 176}, {1, 4, 20, 80}}
-                      : n == 5 ? PackParams{4, 5, 2, 4, 1, 1, 0, {1, 5, 33, 173}, {1, 5, 33, 173}, {1, 5, 37, 173}}
+                      : n == 5 ? PackParams{4, 5, 1, 7, 1, 1, 0, {1, 5, 33, 173}, {1, 5, 33, 173}, {1, 5, 37, 173}}
                       : n == 6 ? PackParams{7, 6, 1, 1, 0, 0, 0, {1, 7, 42, 508}, {1, 7, 42, 508}, {1, 6, 38, 228}}
                       : n == 7 ? PackParams{5, 3, 1, 1, 1, 1, 0, {1, 7, 65, 459}, {1, 7, 65, 459}, {1, 7, 49, 363}}
                       : n == 8 ? PackParams{2, 1, 2, 1, 0, 1, 0, {67, 8, 1, 533}, {67, 8, 1, 533}, {1, 8, 72, 568}}
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
         tma_load_1d_hint(geo_s, A.geo + blk * Cfg::GB, geo_bytes, bar, pol);
       }
     }
-    cell_group_sync<W>(grp);
+    cell_group_sync<W, Cfg::GROUPS>(grp);
   }
   pdl_trigger();
   uint32_t parity = 0;
@@ -240,14 +240,14 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
 #pragma unroll
     for (int c = 0; c < N; ++c)
       if (used) B0[zc0 + L0.SZ * c] = v[c];
-    cell_group_sync<W>(grp);
+    cell_group_sync<W, Cfg::GROUPS>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B0[xl0 + L0.SX * m];
     eo_apply<N, 1>(A.S, v, v);
 #pragma unroll
     for (int m = 0; m < N; ++m)
       if (used) B0[xl0 + L0.SX * m] = v[m];
-    cell_group_sync<W>(grp);
+    cell_group_sync<W, Cfg::GROUPS>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B0[yl0 + L0.SY * m];
     eo_apply<N, 1>(A.S, v, v);
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
       if (used) B1[yl1 + L1.SY * m] = v[m];
       if (used) B2[yl2 + L2.SY * m] = g[m];
     }
-    cell_group_sync<W>(grp);
+    cell_group_sync<W, Cfg::GROUPS>(grp);
     // ---- D_x into B0; D_z stays in registers (same thread, same column) ----
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
     eo_apply<N, -1>(A.D, v, gz);
-    cell_group_sync<W>(grp);
+    cell_group_sync<W, Cfg::GROUPS>(grp);
     // ---- quadrature points of column (a,b) ----
     const bool more = o0 + step < A.count;
     if (DEFORMED) {
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
         if (used) B1[zc1 + L1.SZ * c] = g[c];
     }
     if (DEFORMED) fence_proxy_async_smem();
-    cell_group_sync<W>(grp);
+    cell_group_sync<W, Cfg::GROUPS>(grp);
     // geometry buffers free: fetch the next step's blocks
     const bool nvalid = used && o + step < A.count;
     blk += ng;
@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
       const T s = B1[xl1 + L1.SX * m] + g[m];
       if (used) B1[xl1 + L1.SX * m] = s;
     }
-    cell_group_sync<W>(grp);
+    cell_group_sync<W, Cfg::GROUPS>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B2[yl2 + L2.SY * m];
     eo_apply<N, -1>(A.DT, v, g);
@@ -351,14 +351,14 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
 #pragma unroll
     for (int m = 0; m < N; ++m)
       if (used) B1[yl1 + L1.SY * m] = v[m];
-    cell_group_sync<W>(grp);
+    cell_group_sync<W, Cfg::GROUPS>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
     eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
     for (int m = 0; m < N; ++m)
       if (used) B1[xl1 + L1.SX * m] = v[m];
-    cell_group_sync<W>(grp);
+    cell_group_sync<W, Cfg::GROUPS>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
     eo_apply<N, 1>(A.ST, v, v);
