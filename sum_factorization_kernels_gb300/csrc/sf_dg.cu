@@ -188,14 +188,65 @@ __device__ __forceinline__ void line_residual(const DGArgs<N, T> &A, int d, cons
   }
 }
 
+// Shared-memory layout of one of the three slabs of dg_kernel: entry
+// (x, y, z) of the block's cell cs at BASE + cs RS + SX x + SY y + SZ z.
+struct DGSlab {
+  int SX, SY, SZ, RS, BASE;
+};
+
+// The slabs and the lines the threads own in the x and y sweeps: the thread
+// of z column (a, b) owns the x line (y, z) = (a, b), or (b, a) with XS, and
+// the y line (x, z) = (a, b), or (b, a) with YS.  Either the padded layout
+// of dg_layout with the three slabs of a cell side by side, or (degree 4,
+// FP32) three regions with strides from a bank-conflict model of the
+// kernel's access patterns over the lanes of each warp.
+struct DGSlabs {
+  int XS, YS;
+  DGSlab B0, B1, B2;
+};
+
+constexpr DGSlabs dg_slabs(int n, int elem)
+{
+  if (elem == 4 && n == 5)
+    return DGSlabs{0, 0, {26, 1, 5, 153, 0}, {26, 1, 5, 153, 5 * 153}, {1, 5, 37, 185, 10 * 153}};
+  const DGLayout L = dg_layout(n, elem);
+  const int slab = L.P2 * n, rs = 3 * slab + L.SKEW;
+  return DGSlabs{0, 0, {1, L.P1, L.P2, rs, 0}, {1, L.P1, L.P2, rs, slab}, {1, L.P1, L.P2, rs, 2 * slab}};
+}
+
+// words from the start of the slabs to the end of slab S of the last cell
+constexpr int dg_slab_end(int n, int cpb, DGSlab S)
+{
+  return S.BASE + (cpb - 1) * S.RS + (n - 1) * (S.SX + S.SY + S.SZ) + 1;
+}
+
+constexpr int imax3(int a, int b, int c) { return a > b ? (a > c ? a : c) : (b > c ? b : c); }
+
+// every entry of an n^3 slab has its own word and the slabs of the block's
+// cells do not overlap
+constexpr bool dg_slabs_fit(int n, int cpb, DGSlabs S)
+{
+  bool seen[8192] = {};
+  const DGSlab L[3] = {S.B0, S.B1, S.B2};
+  for (int s = 0; s < 3; ++s)
+    for (int c = 0; c < cpb; ++c)
+      for (int z = 0; z < n; ++z)
+        for (int y = 0; y < n; ++y)
+          for (int x = 0; x < n; ++x) {
+            const int i = L[s].BASE + c * L[s].RS + L[s].SX * x + L[s].SY * y + L[s].SZ * z;
+            if (i < 0 || i >= 8192 || seen[i]) return false;
+            seen[i] = true;
+          }
+  return true;
+}
+
 template <int N, typename T>
 struct DGCfg {
   static constexpr int CPB = DGCells<N>::value;
-  static constexpr DGLayout L = dg_layout(N, (int)sizeof(T));
-  static constexpr int P1 = L.P1, P2 = L.P2;
-  static constexpr int SLAB = P2 * N;            // elements per slab
-  static constexpr int RS = 3 * SLAB + L.SKEW;   // slab region per cell
-  static_assert((P1 + 1) * (N - 1) < P2, "slab padding overlaps");
+  static constexpr DGSlabs S = dg_slabs(N, (int)sizeof(T));
+  // slab words of a block
+  static constexpr int SLABS = imax3(dg_slab_end(N, CPB, S.B0), dg_slab_end(N, CPB, S.B1), dg_slab_end(N, CPB, S.B2));
+  static_assert(SLABS > 8192 || dg_slabs_fit(N, CPB, S), "slab entries overlap");
   // face region per cell of an operator kind
   static constexpr int face_stride(bool sipg)
   {
@@ -203,7 +254,7 @@ struct DGCfg {
   }
   static constexpr size_t smem(bool sipg)
   {
-    return (size_t(CPB) * RS + size_t(CPB) * face_stride(sipg)) * sizeof(T);
+    return (size_t(SLABS) + size_t(CPB) * face_stride(sipg)) * sizeof(T);
   }
 };
 
@@ -213,7 +264,8 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
 {
   using Cfg = DGCfg<N, T>;
   constexpr int N2 = N * N, N3 = N * N * N;
-  constexpr int CPB = Cfg::CPB, P1 = Cfg::P1, P2 = Cfg::P2;
+  constexpr int CPB = Cfg::CPB;
+  constexpr DGSlab L0 = Cfg::S.B0, L1 = Cfg::S.B1, L2 = Cfg::S.B2;
   constexpr int NF = face_arrays<KIND>(); // face arrays per cell
   constexpr DGFaceLayout FL = dg_face_layout(N, KIND == K_SIPG);
   constexpr int FA = FL.FA;
@@ -228,13 +280,20 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   const bool valid = cell < A.n_cells;
   const long long roff = (long long)blockIdx.y * A.n_dofs; // right-hand side offset
   const T *__restrict__ x = A.x + roff;
-  T *B0 = smem + cs * Cfg::RS;
-  T *B1 = B0 + Cfg::SLAB, *B2 = B1 + Cfg::SLAB;
+  T *B0 = smem + L0.BASE + cs * L0.RS;
+  T *B1 = smem + L1.BASE + cs * L1.RS;
+  T *B2 = smem + L2.BASE + cs * L2.RS;
   // face arrays: [dir][side][value, derivative][n^2]  (SIPG), values only (advection)
-  T *F = smem + CPB * Cfg::RS + cs * Cfg::face_stride(KIND == K_SIPG);
-  const int zc = a + P1 * b;      // z column (a, b)
-  const int xl = P1 * a + P2 * b; // x line (y=a, z=b), stride 1
-  const int yl = a + P2 * b;      // y line (x=a, z=b), stride P1
+  T *F = smem + Cfg::SLABS + cs * Cfg::face_stride(KIND == K_SIPG);
+  // the lines of this thread: z column (a, b), x line (y, z) = (xy, xz),
+  // y line (x, z) = (yx, yz); their bases in each slab
+  const int xy = Cfg::S.XS ? b : a, xz = Cfg::S.XS ? a : b;
+  const int yx = Cfg::S.YS ? b : a, yz = Cfg::S.YS ? a : b;
+  const int zc0 = L0.SX * a + L0.SY * b, xl0 = L0.SY * xy + L0.SZ * xz, yl0 = L0.SX * yx + L0.SZ * yz;
+  const int zc1 = L1.SX * a + L1.SY * b, xl1 = L1.SY * xy + L1.SZ * xz, yl1 = L1.SX * yx + L1.SZ * yz;
+  const int zc2 = L2.SX * a + L2.SY * b, yl2 = L2.SX * yx + L2.SZ * yz;
+  // face point index of the x line on the x faces, of the y line on the y faces
+  const int fx = xy + N * xz, fy = yx + N * yz;
   // this thread's z column in the cell-major vector: runs of n^2 consecutive
   // entries per warp instruction (coalesced)
   const long long col = cell * N3 + t;
@@ -245,7 +304,7 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   for (int m = 0; m < N; ++m) v[m] = valid ? __ldg(x + col + N2 * m) : T(0);
   eo_apply<N, 1>(A.S, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B0[zc + P2 * m] = v[m];
+  for (int m = 0; m < N; ++m) B0[zc0 + L0.SZ * m] = v[m];
   // ---- neighbour face layers ----
   if (valid) {
     const unsigned uc = (unsigned)cell;
@@ -292,10 +351,10 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   __syncthreads();
   // ---- x sweep, second tangential direction of the faces ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B0[xl + m];
+  for (int m = 0; m < N; ++m) v[m] = B0[xl0 + L0.SX * m];
   eo_apply<N, 1>(A.S, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B0[xl + m] = v[m];
+  for (int m = 0; m < N; ++m) B0[xl0 + L0.SX * m] = v[m];
   for (int task = t; task < NF * N; task += N2) {
     const int arr = FL.LINE_MAJOR ? task % NF : task / N, line = FL.LINE_MAJOR ? task / NF : task % N;
     T *Fa = F + arr * FA + line;
@@ -308,54 +367,54 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   __syncthreads();
   // ---- y lines: Gauss-point values, y residual ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B0[yl + P1 * m];
+  for (int m = 0; m < N; ++m) v[m] = B0[yl0 + L0.SY * m];
   eo_apply<N, 1>(A.S, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B1[yl + P1 * m] = v[m];
-  // y line t = (a, c=b): face point (a, c) has weight w_a w_c
-  line_residual<KIND, TRANSPOSE, N, T>(A, 1, v, A.w[a] * A.w[b], F, t, r);
+  for (int m = 0; m < N; ++m) B1[yl1 + L1.SY * m] = v[m];
+  // y line (x, z): face point (x, z) has weight w_x w_z
+  line_residual<KIND, TRANSPOSE, N, T>(A, 1, v, A.w[a] * A.w[b], F, fy, r);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B2[yl + P1 * m] = r[m];
+  for (int m = 0; m < N; ++m) B2[yl2 + L2.SY * m] = r[m];
   __syncthreads();
   // ---- x lines and z lines ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B1[xl + m];
-  // x line t = (b, c) = (t%N, t/N)
-  line_residual<KIND, TRANSPOSE, N, T>(A, 0, v, A.w[a] * A.w[b], F, t, r);
+  for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
+  // x line (y, z)
+  line_residual<KIND, TRANSPOSE, N, T>(A, 0, v, A.w[a] * A.w[b], F, fx, r);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B0[xl + m] = r[m];
+  for (int m = 0; m < N; ++m) B0[xl0 + L0.SX * m] = r[m];
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B1[zc + P2 * m];
+  for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
   T rz[N];
   line_residual<KIND, TRANSPOSE, N, T>(A, 2, v, A.w[a] * A.w[b], F, t, rz);
   __syncthreads();
   // ---- sum; integrate / apply the inverse mass along x, y, then z ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = rz[m] + B0[zc + P2 * m] + B2[zc + P2 * m];
+  for (int m = 0; m < N; ++m) v[m] = rz[m] + B0[zc0 + L0.SZ * m] + B2[zc2 + L2.SZ * m];
   if (INVMASS) {
     const T iwab = A.ijxw * A.iw[a] * A.iw[b];
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] *= iwab * A.iw[m];
   }
 #pragma unroll
-  for (int m = 0; m < N; ++m) B1[zc + P2 * m] = v[m];
+  for (int m = 0; m < N; ++m) B1[zc1 + L1.SZ * m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B1[xl + m];
+  for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
   if (INVMASS) eo_apply<N, 1>(A.P, v, v);
   else eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B1[xl + m] = v[m];
+  for (int m = 0; m < N; ++m) B1[xl1 + L1.SX * m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B1[yl + P1 * m];
+  for (int m = 0; m < N; ++m) v[m] = B1[yl1 + L1.SY * m];
   if (INVMASS) eo_apply<N, 1>(A.P, v, v);
   else eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B1[yl + P1 * m] = v[m];
+  for (int m = 0; m < N; ++m) B1[yl1 + L1.SY * m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B1[zc + P2 * m];
+  for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
   if (INVMASS) eo_apply<N, 1>(A.P, v, v);
   else eo_apply<N, 1>(A.ST, v, v);
   // ---- store the z column (plain, fused Chebyshev or Runge-Kutta update) ----
