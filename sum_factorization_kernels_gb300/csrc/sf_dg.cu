@@ -197,9 +197,9 @@ struct DGSlab {
 // The slabs and the lines the threads own in the x and y sweeps: the thread
 // of z column (a, b) owns the x line (y, z) = (a, b), or (b, a) with XS, and
 // the y line (x, z) = (a, b), or (b, a) with YS.  Either the padded layout
-// of dg_layout with the three slabs of a cell side by side, or (degree 4,
-// FP32) three regions with strides from a bank-conflict model of the
-// kernel's access patterns over the lanes of each warp.
+// of dg_layout with the three slabs of a cell side by side, or (FP32) three
+// regions with strides from a bank-conflict model of the kernel's access
+// patterns over the lanes of each warp.
 struct DGSlabs {
   int XS, YS;
   DGSlab B0, B1, B2;
@@ -209,6 +209,18 @@ constexpr DGSlabs dg_slabs(int n, int elem)
 {
   if (elem == 4 && n == 5)
     return DGSlabs{0, 0, {26, 1, 5, 153, 0}, {26, 1, 5, 153, 5 * 153}, {1, 5, 37, 185, 10 * 153}};
+  if (elem == 4 && n == 6)
+    return DGSlabs{1, 0, {1, 6, 49, 292, 0}, {37, 6, 1, 228, 7 * 292}, {1, 6, 38, 228, 7 * 292 + 7 * 228}};
+  if (elem == 4 && n == 2)
+    return DGSlabs{0, 0, {1, 2, 5, 12, 0}, {1, 2, 5, 12, 32 * 12}, {1, 2, 6, 12, 64 * 12}};
+  if (elem == 4 && n == 4)
+    return DGSlabs{0, 0, {1, 4, 19, 80, 0}, {1, 4, 19, 80, 8 * 80}, {1, 4, 20, 80, 16 * 80}};
+  if (elem == 4 && n == 7)
+    return DGSlabs{1, 1, {52, 7, 1, 369, 0}, {1, 7, 52, 369, 5 * 369}, {7, 49, 1, 343, 10 * 369}};
+  if (elem == 4 && n == 8)
+    return DGSlabs{1, 0, {67, 8, 1, 533, 0}, {67, 8, 1, 533, 2 * 533}, {1, 8, 72, 568, 4 * 533}};
+  if (elem == 4 && n == 9)
+    return DGSlabs{0, 0, {1, 9, 81, 729, 0}, {1, 9, 81, 729, 3 * 729}, {1, 9, 105, 945, 6 * 729}};
   const DGLayout L = dg_layout(n, elem);
   const int slab = L.P2 * n, rs = 3 * slab + L.SKEW;
   return DGSlabs{0, 0, {1, L.P1, L.P2, rs, 0}, {1, L.P1, L.P2, rs, slab}, {1, L.P1, L.P2, rs, 2 * slab}};
