@@ -234,13 +234,13 @@ constexpr int dg_slab_end(int n, int cpb, DGSlab S)
 
 constexpr int imax3(int a, int b, int c) { return a > b ? (a > c ? a : c) : (b > c ? b : c); }
 
-// every entry of an n^3 slab has its own word and the slabs of the block's
-// cells do not overlap
-constexpr bool dg_slabs_fit(int n, int cpb, DGSlabs S)
+// every entry of the first ns slabs has its own word and the slabs of the
+// block's cells do not overlap
+constexpr bool dg_slabs_fit(int n, int cpb, DGSlabs S, int ns = 3)
 {
   bool seen[8192] = {};
   const DGSlab L[3] = {S.B0, S.B1, S.B2};
-  for (int s = 0; s < 3; ++s)
+  for (int s = 0; s < ns; ++s)
     for (int c = 0; c < cpb; ++c)
       for (int z = 0; z < n; ++z)
         for (int y = 0; y < n; ++y)
@@ -458,61 +458,93 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   }
 }
 
+// Slabs of the inverse mass kernel: region ZX (written along z columns, read
+// along x lines and the reverse) and region XY (x and y lines), x lines
+// (y, z) = (b, a) with XS, y lines (x, z) = (b, a) with YS.  FP32 degree 4:
+// both regions conflict-free for their two patterns (bank-conflict model);
+// otherwise the padded layout of dg_layout in both regions.
+struct DGInvLayout {
+  int XS, YS;
+  DGSlab ZX, XY;
+};
+
+constexpr DGInvLayout dg_inv_layout(int n, int elem, int cpb)
+{
+  if (elem == 4 && n == 5) return DGInvLayout{1, 1, {1, 5, 33, 185, 0}, {5, 37, 1, 185, 5 * 185}};
+  const DGLayout L = dg_layout(n, elem);
+  const int rs = L.P2 * n + L.SKEW;
+  return DGInvLayout{0, 0, {1, L.P1, L.P2, rs, 0}, {1, L.P1, L.P2, rs, cpb * rs}};
+}
+
+template <int N, typename T>
+struct DGInvCfg {
+  static constexpr int CPB = DGCells<N>::value;
+  static constexpr DGInvLayout L = dg_inv_layout(N, (int)sizeof(T), CPB);
+  static constexpr int WORDS = dg_slab_end(N, CPB, L.ZX) > dg_slab_end(N, CPB, L.XY) ? dg_slab_end(N, CPB, L.ZX)
+                                                                                       : dg_slab_end(N, CPB, L.XY);
+  static_assert(WORDS > 8192 || dg_slabs_fit(N, CPB, DGSlabs{0, 0, L.ZX, L.XY, L.XY}, 2), "slab entries overlap");
+};
+
 // cell-local inverse mass matrix M^-1 = P W^-1 P^T (GLL basis, Gauss points)
 template <int N, typename T>
 __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     dg_inverse_mass_kernel(const __grid_constant__ DGArgs<N, T> A)
 {
-  // one padded slab per cell; z columns read and written straight from the
-  // cell-major vectors: P^T along z (registers), x, y; scale by 1/(JxW w) at
-  // the Gauss points; P along y, x, z (registers)
+  // z columns read and written straight from the cell-major vectors: P^T
+  // along z (registers), x, y; scale by 1/(JxW w) at the Gauss points (the
+  // 1/w of the y direction sits in the table, slot D = W^-1 P^T); P along y,
+  // x, z (registers).  Slot ST holds P^T.
+  using Cfg = DGInvCfg<N, T>;
   constexpr int N2 = N * N, N3 = N * N * N;
-  constexpr int CPB = DGCells<N>::value;
-  constexpr DGLayout L = dg_layout(N, (int)sizeof(T));
-  constexpr int P1 = L.P1, P2 = L.P2, RS1 = P2 * N + L.SKEW;
+  constexpr int CPB = Cfg::CPB;
+  constexpr DGSlab ZX = Cfg::L.ZX, XY = Cfg::L.XY;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
   const int tid = threadIdx.x;
   const int cs = tid / N2;
   const int t = tid - cs * N2;
   const int a = t % N, b = t / N;
+  const int xy = Cfg::L.XS ? b : a, xz = Cfg::L.XS ? a : b; // x line (y, z)
+  const int yx = Cfg::L.YS ? b : a, yz = Cfg::L.YS ? a : b; // y line (x, z)
   const long long cell = (long long)blockIdx.x * CPB + cs;
   const bool valid = cell < A.n_cells;
   const long long col = (long long)blockIdx.y * A.n_dofs + cell * N3 + t;
-  T *B = smem + cs * RS1;
-  const int zc = a + P1 * b, xl = P1 * a + P2 * b, yl = a + P2 * b;
+  T *Z = smem + ZX.BASE + cs * ZX.RS;
+  T *X = smem + XY.BASE + cs * XY.RS;
+  const int zc = ZX.SX * a + ZX.SY * b, xlz = ZX.SY * xy + ZX.SZ * xz;
+  const int xlx = XY.SY * xy + XY.SZ * xz, ylx = XY.SX * yx + XY.SZ * yz;
   T v[N];
 #pragma unroll
   for (int m = 0; m < N; ++m) v[m] = valid ? __ldg(A.x + col + N2 * m) : T(0);
   eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[zc + P2 * m] = v[m];
+  for (int m = 0; m < N; ++m) Z[zc + ZX.SZ * m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[xl + m];
+  for (int m = 0; m < N; ++m) v[m] = Z[xlz + ZX.SX * m];
   eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[xl + m] = v[m];
+  for (int m = 0; m < N; ++m) X[xlx + XY.SX * m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[yl + P1 * m];
-  eo_apply<N, 1>(A.ST, v, v);
-  // now at Gauss point (a, m, c=b): divide by JxW w
-  const T iwab = A.ijxw * A.iw[a] * A.iw[b];
+  for (int m = 0; m < N; ++m) v[m] = X[ylx + XY.SY * m];
+  eo_apply<N, 1>(A.D, v, v);
+  // Gauss point (yx, m, yz): the remaining 1 / (JxW w_x w_z)
+  const T iwab = A.ijxw * A.iw[yx] * A.iw[yz];
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] *= iwab * A.iw[m];
+  for (int m = 0; m < N; ++m) v[m] *= iwab;
   eo_apply<N, 1>(A.P, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[yl + P1 * m] = v[m];
+  for (int m = 0; m < N; ++m) X[ylx + XY.SY * m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[xl + m];
+  for (int m = 0; m < N; ++m) v[m] = X[xlx + XY.SX * m];
   eo_apply<N, 1>(A.P, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[xl + m] = v[m];
+  for (int m = 0; m < N; ++m) Z[xlz + ZX.SX * m] = v[m];
   __syncthreads();
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[zc + P2 * m];
+  for (int m = 0; m < N; ++m) v[m] = Z[zc + ZX.SZ * m];
   eo_apply<N, 1>(A.P, v, v);
   if (valid) {
 #pragma unroll
@@ -613,13 +645,14 @@ template <int N, typename T>
 int dg_invmass_impl(const sf_op *op, int nrhs, const T *x, T *y, cudaStream_t st)
 {
   constexpr int CPB = DGCells<N>::value;
-  constexpr DGLayout L = dg_layout(N, (int)sizeof(T));
   DGArgs<N, T> A = make_dg_args<N, T>(op);
-  // the transposed tables of P go into the ST slot
-  A.ST = eo_of<N, T>(op->shape.Sinv, true);
+  // P^T in the ST slot, W^-1 P^T (Gauss weights along the row) in the D slot
+  const Shape1D &sh = op->shape;
+  A.ST = eo_of<N, T>(sh.Sinv, true);
+  A.D = make_eo<N, T>([&](int i, int j) { return sh.Sinv[j][i] / sh.wq[i]; });
   A.x = x;
   A.y = y;
-  const size_t smem = size_t(CPB) * (L.P2 * N + L.SKEW) * sizeof(T);
+  const size_t smem = size_t(DGInvCfg<N, T>::WORDS) * sizeof(T);
   SF_CUDA_TRY(cudaFuncSetAttribute(dg_inverse_mass_kernel<N, T>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long blocks = (op->n_cells + CPB - 1) / CPB;
