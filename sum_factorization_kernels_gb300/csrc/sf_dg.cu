@@ -460,9 +460,10 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
 
 // Slabs of the inverse mass kernel: region ZX (written along z columns, read
 // along x lines and the reverse) and region XY (x and y lines), x lines
-// (y, z) = (b, a) with XS, y lines (x, z) = (b, a) with YS.  FP32 degree 4:
-// both regions conflict-free for their two patterns (bank-conflict model);
-// otherwise the padded layout of dg_layout in both regions.
+// (y, z) = (b, a) with XS, y lines (x, z) = (b, a) with YS.  FP32: layouts
+// from the bank-conflict model (both regions conflict-free for their two
+// patterns at degrees 1 and 3-5, 7, 8); FP64: the padded layout of
+// dg_layout in both regions.
 struct DGInvLayout {
   int XS, YS;
   DGSlab ZX, XY;
@@ -470,7 +471,19 @@ struct DGInvLayout {
 
 constexpr DGInvLayout dg_inv_layout(int n, int elem, int cpb)
 {
-  if (elem == 4 && n == 5) return DGInvLayout{1, 1, {1, 5, 33, 185, 0}, {5, 37, 1, 185, 5 * 185}};
+  if (elem == 4) {
+    switch (n) {
+    case 2: return DGInvLayout{0, 0, {1, 2, 5, 12, 0}, {1, 3, 6, 12, 32 * 12}};
+    case 3: return DGInvLayout{1, 1, {3, 9, 1, 27, 0}, {1, 33, 11, 99, 14 * 27}};
+    case 4: return DGInvLayout{0, 0, {1, 4, 17, 80, 0}, {1, 5, 20, 80, 8 * 80}};
+    case 5: return DGInvLayout{1, 1, {1, 5, 33, 185, 0}, {5, 37, 1, 185, 5 * 185}};
+    case 6: return DGInvLayout{1, 1, {1, 6, 49, 292, 0}, {6, 38, 1, 228, 7 * 292}};
+    case 7: return DGInvLayout{0, 0, {1, 7, 49, 343, 0}, {1, 65, 7, 465, 5 * 343}};
+    case 8: return DGInvLayout{0, 0, {68, 1, 8, 540, 0}, {1, 65, 8, 519, 2 * 540}};
+    case 9: return DGInvLayout{1, 1, {1, 9, 97, 881, 0}, {9, 105, 1, 945, 3 * 881}};
+    default: break;
+    }
+  }
   const DGLayout L = dg_layout(n, elem);
   const int rs = L.P2 * n + L.SKEW;
   return DGInvLayout{0, 0, {1, L.P1, L.P2, rs, 0}, {1, L.P1, L.P2, rs, cpb * rs}};
