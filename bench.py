@@ -37,6 +37,7 @@ MEASURED_TRAFFIC = {(4, 64): 985032704}
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the 8 colour launches "
                   "of one apply, caches warm (--cache-control none)")
 UNIT = "GDoF/s"
+REF_BUDGET_S = 120.0  # CPU seconds of the --impl reference run's timed steps
 DEFORM = 0.05
 
 
@@ -178,10 +179,13 @@ def run_reference(args):
     p = args.degree
     per_step = []
     base = None
+    # each step is a bounded sample: the whole run stays within about
+    # REF_BUDGET_S seconds of CPU time whatever --steps is
+    step_s = max(0.05, min(args.ref_seconds, REF_BUDGET_S / max(1, args.steps)))
     for _ in range(args.warmup):
-        cpu_reference(p, seconds=1.0)
+        cpu_reference(p, seconds=min(1.0, step_s))
     for _ in range(args.steps):
-        r = cpu_reference(p, seconds=args.ref_seconds)
+        r = cpu_reference(p, seconds=step_s)
         per_step.append(r["value"])
         base = r
     value = statistics.median(per_step)
