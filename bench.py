@@ -10,7 +10,8 @@ FP64 with the relative error of every FP32 apply against the FP64 apply.
 One step = one operator apply y = A x with x and the geometry resident in
 HBM (the working set, 0.9 GB at p=4 FP32, exceeds the 129 MB L2, so no
 explicit flush).  e2e = the same apply through the C ABI with the input
-copied from pinned host memory and the result copied back every step.
+copied from pinned host memory and the result copied back every step (steps
+pipelined on three streams with double-buffered device vectors).
 
 ``--impl reference`` times the reference's CPU algorithm for the same apply
 on the host cores (the FP64 oracle port, OpenMP over all host threads) on a
@@ -421,28 +422,61 @@ def run_ours(args):
     op.set_kernel_variant(sfgpu.KERNEL_AUTO)
 
     # ---- e2e: pinned host input -> device -> apply -> host, every step ----
+    # Steps are pipelined on three streams with two device buffer pairs:
+    # step k+1's host-to-device copy and step k-1's device-to-host copy run
+    # while step k's apply runs.  Every step copies its whole input in and
+    # its whole result out inside the timed region.
     xh = torch.empty(N, dtype=torch.float32, pin_memory=True)
     xh.copy_(x32.cpu())
-    yh = torch.empty(N, dtype=torch.float32, pin_memory=True)
-    xd = torch.empty_like(x32)
-    yd = torch.empty_like(x32)
-    for _ in range(args.warmup):
-        with torch.cuda.stream(stream):
-            xd.copy_(xh, non_blocking=True)
-            op.vmult(xd, yd, stream=stream)
-            yh.copy_(yd, non_blocking=True)
+    yh = [torch.empty(N, dtype=torch.float32, pin_memory=True) for _ in range(2)]
+    xd = [torch.empty_like(x32) for _ in range(2)]
+    yd = [torch.empty_like(x32) for _ in range(2)]
+    # each copy is split into E2E_CHUNKS pieces on as many streams (several
+    # copy engines); one cudaMemcpyAsync per piece
+    nch = max(1, args.e2e_chunks)
+    bounds = [N * i // nch for i in range(nch + 1)]
+    s_in = [torch.cuda.Stream() for _ in range(nch)]
+    s_out = [torch.cuda.Stream() for _ in range(nch)]
+    ev_in = [[torch.cuda.Event() for _ in range(nch)] for _ in range(2)]
+    ev_apply = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [[torch.cuda.Event() for _ in range(nch)] for _ in range(2)]
+    for e in ev_apply + [e for row in ev_out for e in row]:
+        e.record(stream)
+    torch.cuda.synchronize()
+
+    def e2e_steps(k_steps):
+        for k in range(k_steps):
+            b = k & 1
+            for c in range(nch):
+                lo, hi = bounds[c], bounds[c + 1]
+                s_in[c].wait_event(ev_apply[b])   # xd[b] no longer read
+                with torch.cuda.stream(s_in[c]):
+                    xd[b][lo:hi].copy_(xh[lo:hi], non_blocking=True)
+                ev_in[b][c].record(s_in[c])
+                stream.wait_event(ev_in[b][c])
+                stream.wait_event(ev_out[b][c])   # yd[b] already copied out
+            op.vmult(xd[b], yd[b], stream=stream)
+            ev_apply[b].record(stream)
+            for c in range(nch):
+                lo, hi = bounds[c], bounds[c + 1]
+                s_out[c].wait_event(ev_apply[b])
+                with torch.cuda.stream(s_out[c]):
+                    yh[b][lo:hi].copy_(yd[b][lo:hi], non_blocking=True)
+                ev_out[b][c].record(s_out[c])
+
+    e2e_steps(args.warmup)
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        with torch.cuda.stream(stream):
-            xd.copy_(xh, non_blocking=True)
-            op.vmult(xd, yd, stream=stream)
-            yh.copy_(yd, non_blocking=True)
-        stream.synchronize()
+    e2e_steps(args.steps)
+    torch.cuda.synchronize()
     t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
     e2e = {"value": N * world / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": 4 * N,
-           "d2h_bytes_per_step": 4 * N}
+           "d2h_bytes_per_step": 4 * N,
+           "pipelined": "2 device buffer pairs: H2D of step k+1 and D2H of step k-1 overlap the apply of step k; "
+                        "each copy in %d pieces on %d streams" % (nch, nch)}
+    if not torch.equal(yh[(args.steps - 1) & 1], yd[(args.steps - 1) & 1].cpu()):
+        raise SystemExit("e2e: the result read back differs from the device result")
 
     # ---- FP64 at the headline degree and the degree sweep ----
     sweep = []
@@ -532,6 +566,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip configs 1, 3, 4, 5")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--e2e-chunks", type=int, default=1, help="pieces per host-device copy in the e2e leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
