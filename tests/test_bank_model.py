@@ -1,0 +1,68 @@
+"""The shared-memory bank model behind the line kernel's slab tables: it
+reproduces the ncu wavefront count of the p=4 FP32 kernel, and the committed
+tables (parsed from the CUDA source) cost no more than the single padded
+layout each degree started from."""
+import numpy as np
+
+from sum_factorization_kernels_gb300 import bank_model as B
+
+# the line kernel's layouts before the search: (W, K) and one padded layout
+# (1, P1, P2) shared by B0 and B1 (per-cell stride 2 n P2 + skew) and B2
+# (1, Q1, Q2), cell-major lanes, no line swaps
+PADDED_F32 = {
+    2: (1, 8, (1, 2, 5, 20), (1, 2, 6, 12)),
+    3: (2, 7, (1, 3, 9, 59), (1, 3, 11, 41)),
+    4: (1, 2, (1, 4, 19, 176), (1, 4, 20, 80)),
+    5: (4, 5, (1, 5, 25, 253), (1, 5, 37, 185)),
+    6: (7, 6, (1, 7, 42, 508), (1, 6, 38, 228)),
+    7: (5, 3, (1, 7, 56, 785), (1, 7, 52, 369)),
+    8: (2, 1, (1, 9, 72, 1152), (1, 8, 72, 576)),
+    9: (8, 3, (1, 9, 81, 1465), (1, 9, 85, 785)),
+}
+
+
+def test_wavefront_rules():
+    lanes = np.arange(32)[None, :]
+    assert B.wavefronts(lanes, 4) == 1                 # 32 consecutive words
+    assert B.wavefronts(lanes * 2, 4) == 2             # stride 2: two words per bank
+    assert B.wavefronts(np.zeros((1, 32), int), 4) == 1  # one word: broadcast
+    assert B.wavefronts(lanes * 32, 4) == 32           # one bank
+    assert B.wavefronts(lanes, 8) == 2                 # 8-byte words: two half-warps
+
+
+def test_source_tables_parse_and_fit():
+    t = B.pack_params_from_source()
+    assert sorted(t) == [(e, n) for e in (4, 8) for n in range(2, 10)]
+    for (elem, n), pp in t.items():
+        for sx, sy, sz, rs in pp[7:]:
+            g = np.arange(n)
+            v = (sx * g[:, None, None] + sy * g[None, :, None] + sz * g[None, None, :]).ravel()
+            assert len(np.unique(v)) == v.size and v.max() < rs, (elem, n)
+
+
+def test_model_reproduces_ncu_p4():
+    """ncu on the 64^3 p=4 FP32 apply (one colour launch, 32,768 cells):
+    5,089,427 shared wavefronts = 155.3 per cell.  Model: slabs + the six
+    walk-ordered geometry reads + the geometry block written by the bulk copy
+    (15,000 bytes per step in 128-byte wavefronts), per cell of the 5-cell
+    step."""
+    pp = B.pack_params_from_source()[(4, 5)]
+    slabs = B.line_cost(5, 4, pp)
+    geo = B.line_geometry_cost(5, 4, 4, 5)
+    tma = 15000 / 128
+    per_cell = (slabs + geo + tma) / 5
+    assert slabs == 540 and geo == B.ideal(5, 4, 4, 6)
+    assert abs(per_cell - 5089427 / 32768) < 0.02 * per_cell
+
+
+def test_tables_no_worse_than_padded_layout():
+    t = B.pack_params_from_source()
+    for n, (w, k, b01, b2) in PADDED_F32.items():
+        lanes = B.lane_map(n, w, k, False)
+        old = (B.slab_cost(n, 4, lanes, b01, (6, 9, 4)) + B.slab_cost(n, 4, lanes, b2, (2, 0, 2)))
+        new = B.line_cost(n, 4, t[(4, n)])
+        assert new <= old, (n, new, old)
+    # p=4: 540 weighted wavefronts per step against 660 and the ideal 460
+    lanes = B.lane_map(5, 4, 5, False)
+    old5 = B.slab_cost(5, 4, lanes, (1, 5, 25, 253), (6, 9, 4)) + B.slab_cost(5, 4, lanes, (1, 5, 37, 185), (2, 0, 2))
+    assert (B.line_cost(5, 4, t[(4, 5)]), old5, B.ideal(5, 4, 4, 23)) == (540, 660, 460)
