@@ -20,6 +20,8 @@
 // slabs per cell; each thread also owns one point of each face pair of its
 // line, so the face fluxes are computed in the thread that holds the
 // matching line.
+#include <cmath>
+
 #include "sf_device.cuh"
 #include "sf_dg_common.cuh"
 #include "sf_internal.h"
@@ -38,6 +40,7 @@ enum { EPI_STORE = 0, EPI_CHEB = 1, EPI_RK = 2 };
 template <int N, typename T>
 struct DGArgs {
   EOMat<N, T> S, ST, D, DT, P;   // P = Sinv (Gauss values -> GLL nodes)
+  EOMat<N, T> PW, PWJ;           // P W^-1 and P W^-1 / JxW (inverse mass sweeps)
   T fv0[N], fv1[N], fd0[N], fd1[N];
   T w[N];
   T iw[N];        // 1 / w
@@ -47,6 +50,11 @@ struct DGArgs {
   T jface[3];     // face area elements jxw * ij_d
   T tau[3];       // SIPG penalty per direction
   T cdir[3];      // SIPG: ij_d^2 jxw ; advection: a_d ij_d jxw
+  T cw[3][N];     // cdir[d] w_m
+  // advection flux coefficients per direction and side: fa, fb =
+  // -(a.n) jface / 2, -|a.n| jface / 2 (forward), fa = -((a.n) + |a.n|)
+  // jface / 2 (transpose)
+  T fa[3][2], fb[3][2];
   T an[3];        // advection velocity a_d
   T hd0;          // derivative of the first Hermite-like function at 0
   const T *__restrict__ x;
@@ -79,19 +87,20 @@ template <int KIND, bool TRANSPOSE, int N, typename T>
 __device__ __forceinline__ void face_flux(const DGArgs<N, T> &A, int d, int side, T um, T dm, T up,
                                           T dp, T wf, T &fv, T &fd)
 {
+  const T jump = um - up;
   if (KIND == K_SIPG) {
+    // (-{du/dn} + tau [u]) jface w and -[u] {dv/dn} jface w (the same
+    // arithmetic with precomputed coefficients takes 8 more registers)
     const T sgn = side ? T(-1) : T(1);
-    const T jump = um - up;
     const T avg = sgn * T(0.5) * A.ij[d] * (dm + dp);
     fv = (avg + jump * A.tau[d]) * A.jface[d] * wf;
     fd = sgn * (T(0.5) * A.ij[d] * A.jface[d]) * jump * wf;
   } else {
-    const T an = side ? A.an[d] : -A.an[d];
-    const T aa = an < T(0) ? -an : an;
+    // fv = -(a.n) u_upwind jface w with (a.n) u_upwind = (a.n) {u} + |a.n| [u] / 2
     if (TRANSPOSE)
-      fv = T(-0.5) * (an + aa) * (um - up) * A.jface[d] * wf;
+      fv = jump * A.fa[d][side] * wf;
     else
-      fv = T(-0.5) * ((um + up) * an + aa * (um - up)) * A.jface[d] * wf;
+      fv = fma(um + up, A.fa[d][side], jump * A.fb[d][side]) * wf;
     fd = T(0);
   }
 }
@@ -166,16 +175,16 @@ __device__ __forceinline__ void line_residual(const DGArgs<N, T> &A, int d, cons
   if (KIND == K_SIPG) {
     eo_apply<N, -1>(A.D, u, g);
 #pragma unroll
-    for (int m = 0; m < N; ++m) g[m] *= A.cdir[d] * A.w[m] * wt;
+    for (int m = 0; m < N; ++m) g[m] *= A.cw[d][m] * wt;
     eo_apply<N, -1>(A.DT, g, r);
   } else if (!TRANSPOSE) {
 #pragma unroll
-    for (int m = 0; m < N; ++m) g[m] = A.cdir[d] * A.w[m] * wt * u[m];
+    for (int m = 0; m < N; ++m) g[m] = A.cw[d][m] * wt * u[m];
     eo_apply<N, -1>(A.DT, g, r);
   } else {
     eo_apply<N, -1>(A.D, u, g);
 #pragma unroll
-    for (int m = 0; m < N; ++m) r[m] = A.cdir[d] * A.w[m] * wt * g[m];
+    for (int m = 0; m < N; ++m) r[m] = A.cw[d][m] * wt * g[m];
   }
 #pragma unroll
   for (int m = 0; m < N; ++m) {
@@ -403,31 +412,28 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   // ---- sum; integrate / apply the inverse mass along x, y, then z ----
 #pragma unroll
   for (int m = 0; m < N; ++m) v[m] = rz[m] + B0[zc0 + L0.SZ * m] + B2[zc2 + L2.SZ * m];
-  if (INVMASS) {
-    const T iwab = A.ijxw * A.iw[a] * A.iw[b];
-#pragma unroll
-    for (int m = 0; m < N; ++m) v[m] *= iwab * A.iw[m];
-  }
+  // with the inverse mass, the scaling 1 / (JxW w_x w_y w_z) at the Gauss
+  // points sits in the tables of the three P sweeps (PW, PW, PWJ)
 #pragma unroll
   for (int m = 0; m < N; ++m) B1[zc1 + L1.SZ * m] = v[m];
   __syncthreads();
 #pragma unroll
   for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
-  if (INVMASS) eo_apply<N, 1>(A.P, v, v);
+  if (INVMASS) eo_apply<N, 1>(A.PW, v, v);
   else eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
   for (int m = 0; m < N; ++m) B1[xl1 + L1.SX * m] = v[m];
   __syncthreads();
 #pragma unroll
   for (int m = 0; m < N; ++m) v[m] = B1[yl1 + L1.SY * m];
-  if (INVMASS) eo_apply<N, 1>(A.P, v, v);
+  if (INVMASS) eo_apply<N, 1>(A.PW, v, v);
   else eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
   for (int m = 0; m < N; ++m) B1[yl1 + L1.SY * m] = v[m];
   __syncthreads();
 #pragma unroll
   for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
-  if (INVMASS) eo_apply<N, 1>(A.P, v, v);
+  if (INVMASS) eo_apply<N, 1>(A.PWJ, v, v);
   else eo_apply<N, 1>(A.ST, v, v);
   // ---- store the z column (plain, fused Chebyshev or Runge-Kutta update) ----
   if (valid) {
@@ -575,7 +581,7 @@ __global__ void pattern_kernel(long long n, int n3, const T *__restrict__ pat, T
 }
 
 template <int N, typename T>
-DGArgs<N, T> make_dg_args(const sf_op *op)
+DGArgs<N, T> make_dg_args(const sf_op *op, bool transpose = false)
 {
   DGArgs<N, T> A{};
   const Shape1D &s = op->shape;
@@ -584,6 +590,9 @@ DGArgs<N, T> make_dg_args(const sf_op *op)
   A.D = eo_of<N, T>(s.D, false);
   A.DT = eo_of<N, T>(s.D, true);
   A.P = eo_of<N, T>(s.Sinv, false);
+  const double jxw = op->h[0] * op->h[1] * op->h[2];
+  A.PW = make_eo<N, T>([&](int i, int j) { return s.Sinv[i][j] / s.wq[j]; });
+  A.PWJ = make_eo<N, T>([&](int i, int j) { return s.Sinv[i][j] / (s.wq[j] * jxw); });
   for (int i = 0; i < N; ++i) {
     A.fv0[i] = T(s.fv[0][i]);
     A.fv1[i] = T(s.fv[1][i]);
@@ -592,7 +601,6 @@ DGArgs<N, T> make_dg_args(const sf_op *op)
     A.w[i] = T(s.wq[i]);
     A.iw[i] = T(1.0 / s.wq[i]);
   }
-  const double jxw = op->h[0] * op->h[1] * op->h[2];
   A.jxw = T(jxw);
   A.ijxw = T(1.0 / jxw);
   for (int d = 0; d < 3; ++d) {
@@ -601,7 +609,15 @@ DGArgs<N, T> make_dg_args(const sf_op *op)
     A.jface[d] = T(jxw * ij);
     A.tau[d] = T((N) * (N) * op->desc.penalty * ij);
     A.an[d] = T(op->desc.velocity[d]);
-    A.cdir[d] = op->desc.kind == SF_OP_DG_SIPG ? T(ij * ij * jxw) : T(op->desc.velocity[d] * ij * jxw);
+    const double cdir = op->desc.kind == SF_OP_DG_SIPG ? ij * ij * jxw : op->desc.velocity[d] * ij * jxw;
+    A.cdir[d] = T(cdir);
+    for (int m = 0; m < N; ++m) A.cw[d][m] = T(cdir * s.wq[m]);
+    const double jf = jxw * ij;
+    for (int side = 0; side < 2; ++side) {
+      const double an = side ? op->desc.velocity[d] : -op->desc.velocity[d];
+      A.fa[d][side] = T(-0.5 * (transpose ? an + std::fabs(an) : an) * jf);
+      A.fb[d][side] = T(-0.5 * std::fabs(an) * jf);
+    }
     A.nc[d] = op->desc.n_cells[d];
   }
   A.div_nx = make_fast_div((unsigned)A.nc[0]);
@@ -618,7 +634,7 @@ int dg_vmult_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T *y, c
                   cudaStream_t st)
 {
   constexpr int CPB = DGCells<N>::value;
-  DGArgs<N, T> A = make_dg_args<N, T>(op);
+  DGArgs<N, T> A = make_dg_args<N, T>(op, transpose);
   A.x = x;
   A.y = y;
   A.cb = cb;
