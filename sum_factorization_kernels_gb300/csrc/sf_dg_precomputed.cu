@@ -47,14 +47,43 @@ struct PDGArgs {
   long long n_cells, n_dofs;
 };
 
+// Slabs X, Az, B of a block's cells: entry (x, y, z) of cell cs at
+// BASE + cs RS + SX x + SY y + SZ z.  FP32 degrees 3 and 5: three regions
+// with strides from the bank-conflict model (X: 1 z, 2 x, 2 y accesses per
+// step; Az: 2, 2, 2; B: 1, 3, 2); otherwise dg_layout's padded layout with
+// the three slabs of a cell side by side.
+struct PDGSlab {
+  int SX, SY, SZ, RS, BASE;
+};
+struct PDGSlabs {
+  PDGSlab X, Az, B;
+};
+
+constexpr PDGSlabs pdg_slabs(int n, int elem, int cpb)
+{
+  if (elem == 4 && n == 4)
+    return PDGSlabs{{1, 5, 20, 80, 0}, {1, 4, 19, 80, 8 * 80}, {1, 5, 20, 80, 16 * 80}};
+  if (elem == 4 && n == 6)
+    return PDGSlabs{{1, 49, 6, 292, 0}, {37, 1, 6, 228, 7 * 292}, {1, 49, 6, 292, 7 * (292 + 228)}};
+  const DGLayout L = dg_layout(n, elem);
+  const int slab = L.P2 * n, rs = 3 * slab + L.SKEW;
+  (void)cpb;
+  return PDGSlabs{{1, L.P1, L.P2, rs, 0}, {1, L.P1, L.P2, rs, slab}, {1, L.P1, L.P2, rs, 2 * slab}};
+}
+
+constexpr int pdg_slab_end(int n, int cpb, PDGSlab S)
+{
+  return S.BASE + (cpb - 1) * S.RS + (n - 1) * (S.SX + S.SY + S.SZ) + 1;
+}
+
 template <int N, typename T>
 struct PDGCfg {
   static constexpr int CPB = DGCells<N>::value;
-  static constexpr DGLayout L = dg_layout(N, (int)sizeof(T));
-  static constexpr int P1 = L.P1, P2 = L.P2;
-  static constexpr int SLAB = P2 * N;
-  static constexpr int RS = 3 * SLAB + L.SKEW;
-  static constexpr size_t SMEM = size_t(CPB) * RS * sizeof(T);
+  static constexpr PDGSlabs S = pdg_slabs(N, (int)sizeof(T), CPB);
+  static constexpr int E0 = pdg_slab_end(N, CPB, S.X), E1 = pdg_slab_end(N, CPB, S.Az),
+                       E2 = pdg_slab_end(N, CPB, S.B);
+  static constexpr int WORDS = E0 > E1 ? (E0 > E2 ? E0 : E2) : (E1 > E2 ? E1 : E2);
+  static constexpr size_t SMEM = size_t(WORDS) * sizeof(T);
 };
 
 // line residual of the 1D operator L plus the couplings with the two
@@ -79,7 +108,8 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
 {
   using Cfg = PDGCfg<N, T>;
   constexpr int N2 = N * N, N3 = N * N * N;
-  constexpr int CPB = Cfg::CPB, P1 = Cfg::P1, P2 = Cfg::P2;
+  constexpr int CPB = Cfg::CPB;
+  constexpr PDGSlab LX = Cfg::S.X, LA = Cfg::S.Az, LB = Cfg::S.B;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
   const int tid = threadIdx.x;
@@ -88,11 +118,13 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   const int a = t % N, b = t / N;
   const long long cell = (long long)blockIdx.x * CPB + cs;
   const bool valid = cell < A.n_cells;
-  T *X = smem + cs * Cfg::RS;
-  T *Az = X + Cfg::SLAB, *B = Az + Cfg::SLAB;
-  const int zc = a + P1 * b;      // z column (a, b)
-  const int xl = P1 * a + P2 * b; // x line (y=a, z=b), stride 1
-  const int yl = a + P2 * b;      // y line (x=a, z=b), stride P1
+  T *X = smem + LX.BASE + cs * LX.RS;
+  T *Az = smem + LA.BASE + cs * LA.RS;
+  T *B = smem + LB.BASE + cs * LB.RS;
+  // z column (a, b), x line (y=a, z=b), y line (x=a, z=b) in each slab
+  const int zcX = LX.SX * a + LX.SY * b, xlX = LX.SY * a + LX.SZ * b, ylX = LX.SX * a + LX.SZ * b;
+  const int zcA = LA.SX * a + LA.SY * b, xlA = LA.SY * a + LA.SZ * b, ylA = LA.SX * a + LA.SZ * b;
+  const int zcB = LB.SX * a + LB.SY * b, xlB = LB.SY * a + LB.SZ * b, ylB = LB.SX * a + LB.SZ * b;
   const long long col = cell * N3 + t;
   const long long roff = (long long)blockIdx.y * A.n_dofs; // right-hand side offset
   const T *__restrict__ x = A.x + roff;
@@ -115,7 +147,7 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
 #pragma unroll
   for (int m = 0; m < N; ++m) v[m] = valid ? __ldg(x + col + N2 * m) : T(0);
 #pragma unroll
-  for (int m = 0; m < N; ++m) X[zc + P2 * m] = v[m];
+  for (int m = 0; m < N; ++m) X[zcX + LX.SZ * m] = v[m];
   {
     T lo1 = T(0), lo2 = T(0), hi1 = T(0), hi2 = T(0);
     if (valid) {
@@ -128,11 +160,11 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     stiffness_line<N, T>(A, v, lo1, lo2, hi1, hi2, A.c[2], r);
   }
 #pragma unroll
-  for (int m = 0; m < N; ++m) Az[zc + P2 * m] = r[m];
+  for (int m = 0; m < N; ++m) Az[zcA + LA.SZ * m] = r[m];
   __syncthreads();
   // ---- x: x stiffness with couplings into B; mass along x of Az ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = X[xl + m];
+  for (int m = 0; m < N; ++m) v[m] = X[xlX + LX.SX * m];
   {
     // x line (y=a, z=b): node (m, a, b) at m + N a + N2 b
     T lo1 = T(0), lo2 = T(0), hi1 = T(0), hi2 = T(0);
@@ -146,26 +178,26 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     stiffness_line<N, T>(A, v, lo1, lo2, hi1, hi2, A.c[0], r);
   }
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[xl + m] = r[m];
+  for (int m = 0; m < N; ++m) B[xlB + LB.SX * m] = r[m];
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = Az[xl + m];
+  for (int m = 0; m < N; ++m) v[m] = Az[xlA + LA.SX * m];
   eo_apply<N, 1>(A.M, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) Az[xl + m] = v[m];
+  for (int m = 0; m < N; ++m) Az[xlA + LA.SX * m] = v[m];
   __syncthreads();
   // ---- y: mass along y of B and Az; y stiffness with couplings into X ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[yl + P1 * m];
+  for (int m = 0; m < N; ++m) v[m] = B[ylB + LB.SY * m];
   eo_apply<N, 1>(A.M, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[yl + P1 * m] = v[m];
+  for (int m = 0; m < N; ++m) B[ylB + LB.SY * m] = v[m];
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = Az[yl + P1 * m];
+  for (int m = 0; m < N; ++m) v[m] = Az[ylA + LA.SY * m];
   eo_apply<N, 1>(A.M, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) Az[yl + P1 * m] = v[m];
+  for (int m = 0; m < N; ++m) Az[ylA + LA.SY * m] = v[m];
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = X[yl + P1 * m];
+  for (int m = 0; m < N; ++m) v[m] = X[ylX + LX.SY * m];
   {
     // y line (x=a, z=b): node (a, m, b) at a + N m + N2 b
     T lo1 = T(0), lo2 = T(0), hi1 = T(0), hi2 = T(0);
@@ -179,21 +211,21 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     stiffness_line<N, T>(A, v, lo1, lo2, hi1, hi2, A.c[1], r);
   }
 #pragma unroll
-  for (int m = 0; m < N; ++m) X[yl + P1 * m] = r[m];
+  for (int m = 0; m < N; ++m) X[ylX + LX.SY * m] = r[m];
   __syncthreads();
   // ---- x: B += M_x X ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = X[xl + m];
+  for (int m = 0; m < N; ++m) v[m] = X[xlX + LX.SX * m];
   eo_apply<N, 1>(A.M, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) B[xl + m] += v[m];
+  for (int m = 0; m < N; ++m) B[xlB + LB.SX * m] += v[m];
   __syncthreads();
   // ---- z: y = M_z B + Az ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = B[zc + P2 * m];
+  for (int m = 0; m < N; ++m) v[m] = B[zcB + LB.SZ * m];
   eo_apply<N, 1>(A.M, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] += Az[zc + P2 * m];
+  for (int m = 0; m < N; ++m) v[m] += Az[zcA + LA.SZ * m];
   if (valid) {
     T *dst = A.y + roff + col;
     if (CHEB) {
