@@ -223,7 +223,8 @@ def secondary_configs(stream, peak):
     same problem with the precomputed tensor-product SIPG operator),
     config 4 (variable kappa p=4 32^3: forward and adjoint), config 5 (DG
     advection p=4 48^3, 8 right-hand sides: forward / transpose, LSRK(5,4)
-    time steps, dot test)"""
+    time steps, dot test), and the mass / convection variants of the cell
+    operator (p=4 affine 64^3 FP32)"""
     import numpy as np
     import torch
 
@@ -367,6 +368,18 @@ def secondary_configs(stream, peak):
     out["dg_advect_p4_48c_8rhs"] = res
     del op
     torch.cuda.empty_cache()
+    # ---- the cell operator's DO_MASS_MATRIX / DO_CONVECTION variants:
+    # continuous mass matrix and convection form, p=4, affine 64^3, FP32
+    # (vectors only: 2 s N algorithmic bytes) ----
+    res = {}
+    for name, kind in (("mass", sfgpu.OP_MASS), ("convection", sfgpu.OP_CONVECTION)):
+        op = sfgpu.Operator(kind, degree=4, n_cells=(64, 64, 64), velocity=(1.0, 2.0, 3.0))
+        x = torch.rand(op.n_dofs, device="cuda", dtype=torch.float32) * 2 - 1
+        y = torch.empty_like(x)
+        t = time_apply(op, x, y, 30, 5, stream)
+        res[name] = {"gdofs": round(op.n_dofs / t / 1e9, 3), "hbm_frac": round(8 * op.n_dofs / t / 1e9 / peak, 4)}
+        del op, x, y
+    out["cell_variants_p4_64c_affine_fp32"] = res
     return out
 
 

@@ -22,7 +22,8 @@
  *  - Precision: SF_FP64 vectors are double, SF_FP32 vectors are float.
  *
  * Vector layouts
- *  - continuous (SF_OP_LAPLACE): global lexicographic nodes of the
+ *  - continuous (SF_OP_LAPLACE, SF_OP_MASS, SF_OP_CONVECTION): global
+ *    lexicographic nodes of the
  *    (p*nx+1) x (p*ny+1) x (p*nz+1) grid, x fastest; cell (i,j,k) local node
  *    (a,b,c) is global ((k*p+c)*(p*ny+1) + (j*p+b))*(p*nx+1) + (i*p+a).
  *    Restricted to one cell this is the reference's cell-local order
@@ -62,11 +63,18 @@ typedef enum {
   SF_OP_LAPLACE = 0,   /* continuous FE Laplacian -div(kappa grad u)           */
   SF_OP_DG_SIPG = 1,   /* DG symmetric interior penalty Laplacian, periodic     */
   SF_OP_DG_ADVECT = 2, /* DG upwind advection, periodic                        */
-  SF_OP_DG_PRECOMPUTED = 3 /* DG SIPG Laplacian in tensor-product form with
+  SF_OP_DG_PRECOMPUTED = 3, /* DG SIPG Laplacian in tensor-product form with
                           precomputed 1D mass and stiffness matrices, Hermite-
                           like basis, penalty p(p+1), periodic; replaces
                           PrecomputedDGLaplacian (precomputed_dg_laplacian.h:
                           44-377): sf_vmult = matrix_vector_product() */
+  SF_OP_MASS = 4,      /* continuous mass matrix (u, v), affine meshes; the
+                          DO_MASS_MATRIX variant of the cell Laplacian
+                          (evaluation_cell_laplacian.h:299-326)              */
+  SF_OP_CONVECTION = 5 /* continuous convection form (u, b . grad v) with a
+                          constant b = desc.velocity, affine meshes; the
+                          DO_CONVECTION variant (evaluation_cell_laplacian.h:
+                          328-354), there with b = (1, 2, 3)                 */
 } sf_op_kind;
 
 typedef enum { SF_BASIS_GLL = 0, SF_BASIS_HERMITE = 1 } sf_basis;
@@ -76,14 +84,14 @@ typedef struct {
   int degree;          /* 1..8                                                  */
   int n_cells[3];      /* hexahedral cells per direction                        */
   double length[3];    /* domain [0,Lx]x[0,Ly]x[0,Lz]                           */
-  int basis;           /* SF_OP_LAPLACE only (DG SIPG and precomputed:
+  int basis;           /* continuous operators (DG SIPG and precomputed:
                           Hermite-like, DG advect: GLL)                         */
   double deform;       /* SF_OP_LAPLACE: amplitude a of the mapping
                           x_i <- x_i + a sin(2 pi x_j) sin(2 pi x_k), (i,j,k)
                           cyclic; 0 = affine (geometry not stored)            */
-  int dirichlet;       /* SF_OP_LAPLACE: 1 = homogeneous Dirichlet boundary    */
+  int dirichlet;       /* continuous: 1 = homogeneous Dirichlet boundary       */
   double penalty;      /* SF_OP_DG_SIPG: tau = penalty (p+1)^2 / h_d (ref: 1)  */
-  double velocity[3];  /* SF_OP_DG_ADVECT                                      */
+  double velocity[3];  /* SF_OP_DG_ADVECT, SF_OP_CONVECTION                     */
   int inverse_mass;    /* SF_OP_DG_ADVECT: 1 = apply M^-1 (reference do_matvec) */
   int precisions;      /* bit 0: prepare FP64, bit 1: prepare FP32             */
 } sf_desc;

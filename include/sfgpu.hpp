@@ -143,10 +143,18 @@ public:
   static constexpr unsigned int dimension = 3;
   static constexpr unsigned int dofs_per_cell = (degree + 1) * (degree + 1) * (degree + 1);
 
+  // the reference's compile-time variants of this class, DO_MASS_MATRIX and
+  // DO_CONVECTION (evaluation_cell_laplacian.h:22-24, :299-354): set to
+  // SF_OP_MASS or SF_OP_CONVECTION before initialize() (affine meshes);
+  // the convection velocity defaults to the reference's b_d = d + 1
+  int cell_operator = SF_OP_LAPLACE;
+  double convection[3] = {1.0, 2.0, 3.0};
+
   void initialize(const unsigned *n_cells, const double *length = nullptr, double deform = 0.0,
                   int basis = SF_BASIS_GLL, bool dirichlet = true)
   {
-    sf_desc d = make_desc(SF_OP_LAPLACE, degree, n_cells, length);
+    sf_desc d = make_desc(cell_operator, degree, n_cells, length);
+    for (int k = 0; k < 3; ++k) d.velocity[k] = convection[k];
     d.deform = deform;
     d.basis = basis;
     d.dirichlet = dirichlet ? 1 : 0;

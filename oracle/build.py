@@ -121,15 +121,21 @@ def build_ref() -> list[str]:
     outs = []
     # the DG headers put an OpenMP 'private' clause that the access macro of
     # ref_shim.h would rewrite, so they are built without OpenMP (serial)
-    for name, extra, omp in [("ref_kernel", [REF_INC], False),
-                             ("ref_cell_gll", [REF_INC, REF_SRC], True),
-                             ("ref_cell_hermite", [REF_INC], False),
-                             ("ref_dg", [pdir, REF_INC], False)]:
+    # the cell Laplacian's mass-matrix and convection variants are the same
+    # adapter compiled with the reference's DO_MASS_MATRIX / DO_CONVECTION
+    for name, src, extra, omp, defs in [("ref_kernel", "ref_kernel", [REF_INC], False, []),
+                                        ("ref_cell_gll", "ref_cell_gll", [REF_INC, REF_SRC], True, []),
+                                        ("ref_cell_hermite", "ref_cell_hermite", [REF_INC], False, []),
+                                        ("ref_cell_mass", "ref_cell_hermite", [REF_INC], False,
+                                         ["-DDO_MASS_MATRIX"]),
+                                        ("ref_cell_convection", "ref_cell_hermite", [REF_INC], False,
+                                         ["-DDO_CONVECTION"]),
+                                        ("ref_dg", "ref_dg", [pdir, REF_INC], False, [])]:
         inc = ["-fopenmp"] if omp else []
         for d in extra:
             inc += ["-I", d]
         out = os.path.join(OUT_REF, "lib%s.so" % name)
-        _run(flags + inc + ["-o", out, os.path.join(shim, name + ".cc")])
+        _run(flags + inc + defs + ["-o", out, os.path.join(shim, src + ".cc")])
         outs.append(out)
     return outs
 

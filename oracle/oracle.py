@@ -66,6 +66,8 @@ def lib():
         L.sfo_cont_kappa_grad.argtypes = [C.POINTER(Mesh), _dp, _dp, _dp, _dp]
         L.sfo_cont_diagonal.argtypes = [C.POINTER(Mesh), _dp, C.c_void_p, _dp]
         L.sfo_cell_apply.argtypes = [C.POINTER(Shape), _dp, C.c_int, _dp, _dp]
+        L.sfo_cell_op.argtypes = [C.POINTER(Shape), C.c_int, _dp, C.c_double, _dp, _dp, _dp]
+        L.sfo_cont_apply_op.argtypes = [C.POINTER(Mesh), C.c_int, _dp, _dp, _dp]
         L.sfo_dg_n_dofs.argtypes = [C.POINTER(DG)]
         L.sfo_dg_n_dofs.restype = C.c_longlong
         for f in ("sfo_dg_sipg_apply", "sfo_dg_advect_apply", "sfo_dg_advect_apply_transpose"):
@@ -174,6 +176,26 @@ def cell_apply(degree, basis, G, x, geo_stride):
     lib().sfo_cell_apply(C.byref(s), np.ascontiguousarray(G, dtype=np.float64), geo_stride,
                          np.ascontiguousarray(x, dtype=np.float64), out)
     return out
+
+
+OP_MASS, OP_CONVECTION = 1, 2
+
+
+def cell_op(degree, basis, kind, ij, jxw, b, x):
+    """mass (kind 1) or convection (kind 2) operator of one Cartesian cell"""
+    s = shape(degree, basis)
+    out = np.zeros((degree + 1) ** 3)
+    lib().sfo_cell_op(C.byref(s), kind, np.ascontiguousarray(ij, dtype=np.float64), jxw,
+                      np.ascontiguousarray(b, dtype=np.float64), np.ascontiguousarray(x, dtype=np.float64), out)
+    return out
+
+
+def cont_apply_op(m: Mesh, kind, x, b=(0.0, 0.0, 0.0)):
+    """mass (kind 1) or convection (kind 2) operator on the affine continuous mesh"""
+    y = np.zeros(cont_n_dofs(m))
+    lib().sfo_cont_apply_op(C.byref(m), kind, np.ascontiguousarray(b, dtype=np.float64),
+                            np.ascontiguousarray(x, dtype=np.float64), y)
+    return y
 
 
 def dg(degree, n_cells, h, penalty=1.0, velocity=(1.0, 0.5, 0.25), inverse_mass=1):

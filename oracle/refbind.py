@@ -101,8 +101,11 @@ def herm_tables(degree):
     return s, d, w, h[0]
 
 
-def herm_cell(degree, ij, jxw, x):
-    L = _lib("ref_cell_hermite")
+def herm_cell(degree, ij, jxw, x, variant=None):
+    """the reference's Cartesian cell operator (Hermite-like basis): the
+    Laplacian, or with variant "mass" / "convection" its DO_MASS_MATRIX /
+    DO_CONVECTION build (convection velocity (1, 2, 3))"""
+    L = _lib("ref_cell_hermite" if variant is None else "ref_cell_" + variant)
     L.sfref_herm_cell.argtypes = [C.c_int, _dp, C.c_double, _dp, _dp]
     out = np.zeros((degree + 1) ** 3)
     L.sfref_herm_cell(degree, np.ascontiguousarray(ij, dtype=np.float64), jxw,

@@ -597,6 +597,44 @@ void sfo_cell_apply(const sfo_shape *s, const double *Gcell, int geo_stride,
   cell_apply_k(s, Gcell, geo_stride, NULL, in, out);
 }
 
+/* mass matrix and convection form of one Cartesian cell
+ * (evaluation_cell_laplacian.h:299-326 and :328-354): u_q = S x at the Gauss
+ * points, r_q = u_q JxW w_q; mass: S^T r; convection: t_d = ij_d b_d r,
+ * integrated with D^T and S^T as the Laplacian's second half */
+SFO_INLINE void cell_op_n(int n, const sfo_shape *s, int kind, const double *ij, double jxw,
+                          const double *b, const double *in, double *out)
+{
+  double t[SFO_MAX_NQ], uq[SFO_MAX_NQ];
+  sweep(n, 0, 0, 1, 0, s->S_eo, in, t);
+  sweep(n, 1, 0, 1, 0, s->S_eo, t, uq);
+  sweep(n, 2, 0, 1, 0, s->S_eo, uq, t);
+  for (int qz = 0; qz < n; ++qz)
+    for (int qy = 0; qy < n; ++qy)
+      for (int qx = 0; qx < n; ++qx) {
+        const int q = (qz * n + qy) * n + qx;
+        t[q] *= jxw * ((s->wq[qz] * s->wq[qy]) * s->wq[qx]);
+      }
+  if (kind == 1) {
+    sweep(n, 2, 0, 0, 0, s->S_eo, t, uq);
+    sweep(n, 1, 0, 0, 0, s->S_eo, uq, t);
+    sweep(n, 0, 0, 0, 0, s->S_eo, t, out);
+    return;
+  }
+  double tx[SFO_MAX_NQ], ty[SFO_MAX_NQ], tz[SFO_MAX_NQ];
+  for (int q = 0; q < n * n * n; ++q) {
+    tx[q] = t[q] * (ij[0] * b[0]);
+    ty[q] = t[q] * (ij[1] * b[1]);
+    tz[q] = t[q] * (ij[2] * b[2]);
+  }
+  cell_integrate_n(n, s, tx, ty, tz, out);
+}
+
+void sfo_cell_op(const sfo_shape *s, int kind, const double *ij, double jxw,
+                 const double *b, const double *in, double *out)
+{
+  cell_op_n(s->n, s, kind, ij, jxw, b, in, out);
+}
+
 /* ------------------------------------------------------------------------ */
 /* continuous numbering (no counterpart in the reference; the cell-local     */
 /* order restricts to the reference's lexicographic cell order,              */
@@ -743,6 +781,51 @@ void sfo_cont_apply(const sfo_mesh *m, const double *G, const double *kappa,
       free(u);
     }
   }
+  if (m->dirichlet) {
+    const int p = m->degree;
+    const long long Nx = (long long)p * nx + 1, Ny = (long long)p * ny + 1,
+                    Nz = (long long)p * nz + 1;
+    for (long long Z = 0; Z < Nz; ++Z)
+      for (long long Y = 0; Y < Ny; ++Y)
+        for (long long X = 0; X < Nx; ++X)
+          if (X == 0 || Y == 0 || Z == 0 || X == Nx - 1 || Y == Ny - 1 || Z == Nz - 1) {
+            const long long g = (Z * Ny + Y) * Nx + X;
+            y[g] = x[g];
+          }
+  }
+}
+
+void sfo_cont_apply_op(const sfo_mesh *m, int kind, const double *b,
+                       const double *x, double *y)
+{
+  sfo_shape s;
+  sfo_shape_init(m->degree, m->basis, &s);
+  const int n = s.n, nq = n * n * n;
+  const long long N = sfo_cont_n_dofs(m);
+  memset(y, 0, sizeof(double) * N);
+  const int nx = m->n_cells[0], ny = m->n_cells[1], nz = m->n_cells[2];
+  double ij[3], jxw = 1.;
+  for (int d = 0; d < 3; ++d) {
+    const double h = m->length[d] / m->n_cells[d];
+    ij[d] = 1. / h;
+    jxw *= h;
+  }
+  double *u = (double *)malloc(sizeof(double) * nq * 2);
+  double *v = u + nq;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        cont_gather(m, i, j, k, x, u);
+        cell_op_n(n, &s, kind, ij, jxw, b, u, v);
+        for (int c = 0; c < n; ++c)
+          for (int bb = 0; bb < n; ++bb)
+            for (int a = 0; a < n; ++a) {
+              int bd;
+              const long long g = cont_index(m, i, j, k, a, bb, c, &bd);
+              if (!bd) y[g] += v[(c * n + bb) * n + a];
+            }
+      }
+  free(u);
   if (m->dirichlet) {
     const int p = m->degree;
     const long long Nx = (long long)p * nx + 1, Ny = (long long)p * ny + 1,

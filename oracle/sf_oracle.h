@@ -97,6 +97,17 @@ void sfo_cont_diagonal(const sfo_mesh *m, const double *G, const double *kappa,
 void sfo_cell_apply(const sfo_shape *s, const double *Gcell, int geo_stride,
                     const double *in, double *out);
 
+/* mass matrix (kind 1) and convection form (u, b . grad v) (kind 2) of one
+ * cell with inverse Jacobian diag(ij) and volume jxw: the DO_MASS_MATRIX and
+ * DO_CONVECTION variants of evaluation_cell_laplacian.h (:299-326,
+ * :328-354) */
+void sfo_cell_op(const sfo_shape *s, int kind, const double *ij, double jxw,
+                 const double *b, const double *in, double *out);
+/* y = A x on the affine continuous mesh (m->deform ignored) for those two
+ * operators; Dirichlet rows as in sfo_cont_apply */
+void sfo_cont_apply_op(const sfo_mesh *m, int kind, const double *b,
+                       const double *x, double *y);
+
 /* ---------------- DG operators (cell-major layout, periodic) ------------- */
 typedef struct {
   int degree;

@@ -59,6 +59,8 @@ int check_prec(const sf_op *op, int prec)
   return SF_OK;
 }
 
+bool is_continuous(int kind) { return kind == SF_OP_LAPLACE || kind == SF_OP_MASS || kind == SF_OP_CONVECTION; }
+
 int check_ptr(const void *p, int prec, const char *name)
 {
   if (!p) return fail(SF_ERR_NULL, std::string(name) + " is NULL");
@@ -133,23 +135,24 @@ int sf_create(const sf_desc *desc, sf_op **out)
   if (!desc || !out) return fail(SF_ERR_NULL, "desc/op is NULL");
   *out = nullptr;
   const sf_desc &d = *desc;
-  if (d.kind < SF_OP_LAPLACE || d.kind > SF_OP_DG_PRECOMPUTED) return fail(SF_ERR_INVALID, "unknown operator kind");
+  if (d.kind < SF_OP_LAPLACE || d.kind > SF_OP_CONVECTION) return fail(SF_ERR_INVALID, "unknown operator kind");
+  const bool cont = is_continuous(d.kind);
   if (d.degree < 1 || d.degree > kMaxDegree) return fail(SF_ERR_UNSUPPORTED, "degree must be 1..8");
   for (int k = 0; k < 3; ++k) {
     if (d.n_cells[k] < 1 || d.n_cells[k] > (1 << 20)) return fail(SF_ERR_INVALID, "n_cells out of range");
     if (!(d.length[k] > 0.0)) return fail(SF_ERR_INVALID, "length must be positive");
   }
   if ((d.precisions & 3) == 0) return fail(SF_ERR_INVALID, "precisions must select FP64 and/or FP32");
-  if (d.kind == SF_OP_LAPLACE && d.basis != SF_BASIS_GLL && d.basis != SF_BASIS_HERMITE)
-    return fail(SF_ERR_INVALID, "unknown basis");
+  if (cont && d.basis != SF_BASIS_GLL && d.basis != SF_BASIS_HERMITE) return fail(SF_ERR_INVALID, "unknown basis");
+  if ((d.kind == SF_OP_MASS || d.kind == SF_OP_CONVECTION) && d.deform != 0.0)
+    return fail(SF_ERR_UNSUPPORTED, "mass and convection operators: affine meshes only (deform = 0)");
   if (d.kind == SF_OP_DG_SIPG && !(d.penalty > 0.0)) return fail(SF_ERR_INVALID, "penalty must be positive");
   if (d.kind == SF_OP_LAPLACE && !(d.deform >= 0.0 && d.deform < 0.15))
     return fail(SF_ERR_INVALID, "deform amplitude must be in [0, 0.15) to keep the mapping invertible");
   sf_op *op = new (std::nothrow) sf_op();
   if (!op) return fail(SF_ERR_OOM, "host allocation failed");
   op->desc = d;
-  const int basis = d.kind == SF_OP_LAPLACE ? d.basis
-                    : (d.kind == SF_OP_DG_ADVECT ? SF_BASIS_GLL : SF_BASIS_HERMITE);
+  const int basis = cont ? d.basis : (d.kind == SF_OP_DG_ADVECT ? SF_BASIS_GLL : SF_BASIS_HERMITE);
   op->desc.basis = basis;
   fill_shape(d.degree, basis, op->shape);
   op->n = d.degree + 1;
@@ -160,7 +163,7 @@ int sf_create(const sf_desc *desc, sf_op **out)
     return fail(SF_ERR_INVALID, "more than 2^31 - 1 cells");
   }
   const long long n3 = (long long)op->n * op->n * op->n;
-  if (d.kind == SF_OP_LAPLACE)
+  if (cont)
     op->n_dofs = ((long long)d.degree * d.n_cells[0] + 1) * ((long long)d.degree * d.n_cells[1] + 1) *
                  ((long long)d.degree * d.n_cells[2] + 1);
   else
@@ -171,7 +174,7 @@ int sf_create(const sf_desc *desc, sf_op **out)
   }
   // the Laplacian kernels address the nodes of a cell by 32-bit offsets
   // within the degree + 1 node planes that the cell spans
-  if (d.kind == SF_OP_LAPLACE &&
+  if (cont &&
       ((long long)d.degree * d.n_cells[0] + 1) * ((long long)d.degree * d.n_cells[1] + 1) * (d.degree + 1) >=
           (1LL << 31)) {
     delete op;
@@ -279,7 +282,7 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
   SF_RET(check_ptr(y, prec, "y"));
   if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
-  if (op->desc.kind == SF_OP_LAPLACE) return launch_cont_vmult(op, prec, x, y, st);
+  if (is_continuous(op->desc.kind)) return launch_cont_vmult(op, prec, x, y, st);
   if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
     return launch_dg_precomputed(op, prec, 1, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
   return launch_dg_vmult(op, prec, 1, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
@@ -288,6 +291,7 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
 int sf_vmult_transpose(sf_op *op, int prec, const void *x, void *y, void *stream)
 {
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (op->desc.kind == SF_OP_CONVECTION) return fail(SF_ERR_UNSUPPORTED, "no transpose of the convection form");
   if (op->desc.kind != SF_OP_DG_ADVECT) return sf_vmult(op, prec, x, y, stream);
   return sf_vmult_transpose_batched(op, prec, 1, x, y, stream);
 }
@@ -301,7 +305,7 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
   if (nrhs < 1 || nrhs > 64) return fail(SF_ERR_INVALID, "nrhs must be 1..64");
   if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
-  if (op->desc.kind == SF_OP_LAPLACE) {
+  if (is_continuous(op->desc.kind)) {
     const size_t es = elem_size(prec);
     for (int r = 0; r < nrhs; ++r)
       SF_RET(launch_cont_vmult(op, prec, (const char *)x + r * op->n_dofs * es,
@@ -316,6 +320,7 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
 int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void *stream)
 {
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
+  if (op->desc.kind == SF_OP_CONVECTION) return fail(SF_ERR_UNSUPPORTED, "no transpose of the convection form");
   if (op->desc.kind != SF_OP_DG_ADVECT) return sf_vmult_batched(op, prec, nrhs, x, y, stream);
   SF_RET(check_prec(op, prec));
   SF_RET(check_ptr(x, prec, "x"));
@@ -418,6 +423,8 @@ int sf_diagonal(sf_op *op, int prec, void *diag, void *stream)
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
   SF_RET(check_prec(op, prec));
   SF_RET(check_ptr(diag, prec, "diag"));
+  if (op->desc.kind == SF_OP_MASS || op->desc.kind == SF_OP_CONVECTION)
+    return fail(SF_ERR_UNSUPPORTED, "diagonal: Laplacian and DG operators only");
   if (op->desc.kind == SF_OP_LAPLACE) return launch_cont_diagonal(op, prec, diag, (cudaStream_t)stream);
   if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
     return launch_dg_precomputed_diagonal(op, prec, diag, (cudaStream_t)stream);

@@ -136,6 +136,8 @@ struct LineArgs {
   int nc[3];
   int Nx, plane;                // nodes per x line, per z plane
   T aff[3];
+  T jxw;                        // mass / convection: cell volume (affine)
+  T conv[3];                    // convection: b_d / h_d
   int dirichlet;
   int color, cx, cy, cz, mx, my;
   long long count;              // cells of this colour
@@ -145,7 +147,13 @@ struct LineArgs {
   int step_i, step_j, step_k;
 };
 
-template <int N, typename T, bool DEFORMED, bool KAPPA>
+// cell operator of the apply: the Laplacian (div(kappa grad)), the mass
+// matrix or the convection form (u, b . grad v); the last two on affine
+// meshes (the reference's DO_MASS_MATRIX / DO_CONVECTION variants of the
+// cell Laplacian, evaluation_cell_laplacian.h:299-354)
+enum { OP_LAPLACE = 0, OP_MASS = 1, OP_CONVECTION = 2 };
+
+template <int N, typename T, bool DEFORMED, bool KAPPA, int OPK = OP_LAPLACE>
 __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, LineCfg<N, T>::PP.MINB)
     line_vmult_kernel(const __grid_constant__ LineArgs<N, T> A)
 {
@@ -248,6 +256,96 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
     for (int m = 0; m < N; ++m)
       if (used) B0[xl0 + L0.SX * m] = v[m];
     cell_group_sync<W, Cfg::GROUPS>(grp);
+    if constexpr (OPK != OP_LAPLACE) {
+      // ---- y lines: S_y, the weights JxW w at the Gauss points ----
+#pragma unroll
+      for (int m = 0; m < N; ++m) v[m] = B0[yl0 + L0.SY * m];
+      eo_apply<N, 1>(A.S, v, v);
+      const T wxz = A.jxw * A.w[yx] * A.w[yz];
+#pragma unroll
+      for (int m = 0; m < N; ++m) v[m] *= wxz * A.w[m];
+      if constexpr (OPK == OP_MASS) {
+        eo_apply<N, 1>(A.ST, v, v);
+#pragma unroll
+        for (int m = 0; m < N; ++m)
+          if (used) B1[yl1 + L1.SY * m] = v[m];
+      } else {
+        // convection: r = u JxW w stays in B0 for the x and z lines; the y
+        // term b_y / h_y D^T r goes to B1
+        eo_apply<N, -1>(A.DT, v, g);
+#pragma unroll
+        for (int m = 0; m < N; ++m) {
+          if (used) B0[yl0 + L0.SY * m] = v[m];
+          if (used) B1[yl1 + L1.SY * m] = A.conv[1] * g[m];
+        }
+      }
+      cell_group_sync<W, Cfg::GROUPS>(grp);
+      if constexpr (OPK == OP_CONVECTION) {
+        // ---- x lines: + b_x / h_x D^T r ----
+#pragma unroll
+        for (int m = 0; m < N; ++m) v[m] = B0[xl0 + L0.SX * m];
+        eo_apply<N, -1>(A.DT, v, g);
+#pragma unroll
+        for (int m = 0; m < N; ++m) {
+          const T s = fma(A.conv[0], g[m], B1[xl1 + L1.SX * m]);
+          if (used) B1[xl1 + L1.SX * m] = s;
+        }
+        cell_group_sync<W, Cfg::GROUPS>(grp);
+      }
+      // loads overlapped with the remaining sweeps: the y values this column
+      // adds to, and the next cell's x column
+      const bool nvalid = used && o + step < A.count;
+      if (!y_ready) {
+        pdl_wait();
+        y_ready = true;
+      }
+      T yo[N];
+      load_column_sums<N, T>(A.y + nb, plane, msk.add, yo);
+      const ColumnMask nmsk =
+          column_mask<N>(a, b, 2 * ni + A.cx, 2 * nj + A.cy, 2 * nk + A.cz, A.nc, A.color, dir, nvalid);
+      const long long nnb = cell_node_base<N>(2 * ni + A.cx, 2 * nj + A.cy, 2 * nk + A.cz, A.Nx, plane) + toff;
+      gather_column<N, T>(A.x + nnb, plane, nmsk.keep, xv);
+      if constexpr (OPK == OP_CONVECTION) {
+        // ---- z columns: + b_z / h_z D^T r, then S_z^T ----
+#pragma unroll
+        for (int m = 0; m < N; ++m) v[m] = B0[zc0 + L0.SZ * m];
+        eo_apply<N, -1>(A.DT, v, g);
+#pragma unroll
+        for (int m = 0; m < N; ++m) v[m] = fma(A.conv[2], g[m], B1[zc1 + L1.SZ * m]);
+        eo_apply<N, 1>(A.ST, v, v);
+#pragma unroll
+        for (int m = 0; m < N; ++m)
+          if (used) B1[zc1 + L1.SZ * m] = v[m];
+        cell_group_sync<W, Cfg::GROUPS>(grp);
+#pragma unroll
+        for (int m = 0; m < N; ++m) v[m] = B1[yl1 + L1.SY * m];
+        eo_apply<N, 1>(A.ST, v, v);
+#pragma unroll
+        for (int m = 0; m < N; ++m)
+          if (used) B1[yl1 + L1.SY * m] = v[m];
+        cell_group_sync<W, Cfg::GROUPS>(grp);
+      }
+      // ---- x lines: S_x^T ----
+#pragma unroll
+      for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
+      eo_apply<N, 1>(A.ST, v, v);
+#pragma unroll
+      for (int m = 0; m < N; ++m)
+        if (used) B1[xl1 + L1.SX * m] = v[m];
+      cell_group_sync<W, Cfg::GROUPS>(grp);
+      // ---- z column: S_z^T (mass), scatter ----
+#pragma unroll
+      for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
+      if constexpr (OPK == OP_MASS) eo_apply<N, 1>(A.ST, v, v);
+      if (valid) store_column<N, T>(A.y + nb, A.x + nb, plane, msk.keep, v, yo);
+      msk = nmsk;
+      nb = nnb;
+      valid = nvalid;
+      mi = ni;
+      mj = nj;
+      mk = nk;
+      continue;
+    } else {
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B0[yl0 + L0.SY * m];
     eo_apply<N, 1>(A.S, v, v);
@@ -370,6 +468,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
     mi = ni;
     mj = nj;
     mk = nk;
+    }
   }
   if (!y_ready) pdl_wait();
 }
@@ -451,6 +550,8 @@ int line_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
   A.plane = A.Nx * ((N - 1) * A.nc[1] + 1);
   const double jxw = op->h[0] * op->h[1] * op->h[2];
   for (int d = 0; d < 3; ++d) A.aff[d] = T(jxw / (op->h[d] * op->h[d]));
+  A.jxw = T(jxw);
+  for (int d = 0; d < 3; ++d) A.conv[d] = T(op->desc.velocity[d] / op->h[d]);
   A.dirichlet = op->desc.dirichlet;
   A.x = x;
   A.y = y;
@@ -466,9 +567,16 @@ int line_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
     set_error("line kernel: coefficient missing");
     return SF_ERR_STATE;
   }
+  const int kind = op->desc.kind;
+  if ((kind == SF_OP_MASS || kind == SF_OP_CONVECTION) && (deformed || kap)) {
+    set_error("mass and convection operators: affine meshes without a coefficient only");
+    return SF_ERR_UNSUPPORTED;
+  }
   void (*kern)(const LineArgs<N, T>) =
-      deformed ? (kap ? line_vmult_kernel<N, T, true, true> : line_vmult_kernel<N, T, true, false>)
-               : (kap ? line_vmult_kernel<N, T, false, true> : line_vmult_kernel<N, T, false, false>);
+      kind == SF_OP_MASS         ? line_vmult_kernel<N, T, false, false, OP_MASS>
+      : kind == SF_OP_CONVECTION ? line_vmult_kernel<N, T, false, false, OP_CONVECTION>
+      : deformed ? (kap ? line_vmult_kernel<N, T, true, true> : line_vmult_kernel<N, T, true, false>)
+                 : (kap ? line_vmult_kernel<N, T, false, true> : line_vmult_kernel<N, T, false, false>);
   const size_t smem = 128 + size_t(Cfg::GROUPS) * Cfg::GROUP_BYTES;
   const int threads = Cfg::GT * Cfg::GROUPS;
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

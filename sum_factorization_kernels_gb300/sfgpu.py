@@ -17,8 +17,10 @@ SF_OK = 0
 STATUS = {0: "SF_OK", -1: "SF_ERR_INVALID", -2: "SF_ERR_NULL", -3: "SF_ERR_UNSUPPORTED",
           -4: "SF_ERR_CUDA", -5: "SF_ERR_OOM", -6: "SF_ERR_NOT_CONVERGED",
           -7: "SF_ERR_BREAKDOWN", -8: "SF_ERR_ALIGN", -9: "SF_ERR_STATE"}
+(SF_ERR_INVALID, SF_ERR_NULL, SF_ERR_UNSUPPORTED, SF_ERR_CUDA, SF_ERR_OOM, SF_ERR_NOT_CONVERGED,
+ SF_ERR_BREAKDOWN, SF_ERR_ALIGN, SF_ERR_STATE) = range(-1, -10, -1)
 FP64, FP32 = 0, 1
-OP_LAPLACE, OP_DG_SIPG, OP_DG_ADVECT, OP_DG_PRECOMPUTED = 0, 1, 2, 3
+OP_LAPLACE, OP_DG_SIPG, OP_DG_ADVECT, OP_DG_PRECOMPUTED, OP_MASS, OP_CONVECTION = 0, 1, 2, 3, 4, 5
 BASIS_GLL, BASIS_HERMITE = 0, 1
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2

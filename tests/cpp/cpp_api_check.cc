@@ -45,6 +45,28 @@ int main()
     std::printf("EvaluationCellLaplacian<4,double>::matrix_vector_product rel err %.3e\n", e);
     fails += !(e < 1e-12);
   }
+  // the DO_MASS_MATRIX / DO_CONVECTION variants of the cell evaluator, p = 3
+  for (int kind : {SF_OP_MASS, SF_OP_CONVECTION}) {
+    const unsigned nc[3] = {5, 4, 3};
+    const double L[3] = {1.0, 0.8, 0.6};
+    sfgpu::EvaluationCellLaplacian<3, double> ev;
+    ev.cell_operator = kind;
+    ev.initialize(nc, L);
+    std::vector<double> x(ev.n_dofs());
+    for (auto &v : x) v = U(gen);
+    ev.input_array.upload(x);
+    ev.matrix_vector_product();
+    cudaDeviceSynchronize();
+    const std::vector<double> y = ev.output_array.download();
+    sfo_mesh m{3, SFO_BASIS_GLL, {5, 4, 3}, {1.0, 0.8, 0.6}, 0.0, 1};
+    std::vector<double> yr(y.size());
+    const double b[3] = {1.0, 2.0, 3.0};
+    sfo_cont_apply_op(&m, kind == SF_OP_MASS ? 1 : 2, b, x.data(), yr.data());
+    const double e = rel(y, yr);
+    std::printf("EvaluationCellLaplacian<3,double> (%s) rel err %.3e\n",
+                kind == SF_OP_MASS ? "DO_MASS_MATRIX" : "DO_CONVECTION", e);
+    fails += !(e < 1e-12);
+  }
   // DG SIPG, p = 5: do_matvec, do_chebyshev, emulate_cheby_vector_updates
   {
     const unsigned nc[3] = {4, 3, 3};

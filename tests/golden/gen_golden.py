@@ -213,16 +213,66 @@ def precomputed_fixtures():
     np.savez(os.path.join(HERE, "dg_precomputed.npz"), **out)
 
 
+def ref_cont_apply_variant(degree, nc, length, x, variant):
+    """gather -> the reference's Hermite-like Cartesian cell operator built
+    with DO_MASS_MATRIX / DO_CONVECTION -> scatter, Dirichlet rows identity"""
+    idx, bnd, N = cont_index_arrays(degree, nc)
+    h = np.array(length, dtype=np.float64) / np.array(nc)
+    ij, jxw = 1.0 / h, float(np.prod(h))
+    y = np.zeros(N)
+    for c in range(idx.shape[0]):
+        u = np.where(bnd[c], 0.0, x[idx[c]])
+        v = R.herm_cell(degree, ij, jxw, u, variant)
+        np.add.at(y, idx[c][~bnd[c]], v[~bnd[c]])
+    allb = np.zeros(N, dtype=bool)
+    allb[idx[bnd]] = True
+    y[allb] = x[allb]
+    return y, allb
+
+
+def cellop_fixtures():
+    """the reference's DO_MASS_MATRIX and DO_CONVECTION builds of the
+    Hermite-like cell operator (velocity (1, 2, 3)): single Cartesian cells
+    with inverse Jacobian diag(4, 2, 4/3) and small affine boxes with
+    homogeneous Dirichlet conditions.  Degree 2 is stored too, but the
+    reference's degree-2 variants are not symmetric (its mass matrix differs
+    from S^T W S by 32 %), so the tests pin degree 2 by the tensor-product
+    identity instead."""
+    rng = np.random.default_rng(20241209)
+    out = {}
+    ij = np.array([4.0, 2.0, 4.0 / 3.0])
+    jxw = 1.0 / np.prod(ij)
+    for p in range(1, 9):
+        x = rng.uniform(-1, 1, (p + 1) ** 3)
+        out["cell_x_%d" % p] = x
+        out["cell_mass_%d" % p] = R.herm_cell(p, ij, jxw, x, "mass")
+        out["cell_conv_%d" % p] = R.herm_cell(p, ij, jxw, x, "convection")
+        nc = (3, 2, 2) if p <= 4 else (2, 2, 2)
+        length = (1.0, 0.8, 1.2)
+        _, _, N = cont_index_arrays(p, nc)
+        xc = rng.uniform(-1, 1, N)
+        for name, variant in (("mass", "mass"), ("conv", "convection")):
+            y, bnd = ref_cont_apply_variant(p, nc, length, xc, variant)
+            out["cont_%s_%d" % (name, p)] = np.where(bnd, 0.0, y)
+        xc[bnd] = 0.0
+        out["cont_x_%d" % p] = xc
+        out["nc_%d" % p], out["len_%d" % p] = np.array(nc), np.array(length)
+    np.savez(os.path.join(HERE, "cell_ops.npz"), **out)
+
+
 if __name__ == "__main__":
     import sys
     if sys.argv[1:] == ["rk"]:
         rk_fixtures()
     elif sys.argv[1:] == ["precomputed"]:
         precomputed_fixtures()
+    elif sys.argv[1:] == ["cellops"]:
+        cellop_fixtures()
     else:
         main()
         rk_fixtures()
         precomputed_fixtures()
+        cellop_fixtures()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

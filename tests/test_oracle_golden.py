@@ -175,3 +175,54 @@ def test_dg_precomputed(golden, p):
     d = O.dg(p, tuple(int(v) for v in g["nc_%d" % p]), (1.0, 1.0, 1.0))
     y = O.dg_precomputed_apply(d, g["x_%d" % p].astype(np.float64))
     assert rel(y, g["y_%d" % p]) < 1e-14
+
+
+# mass matrix and convection form (the reference's DO_MASS_MATRIX and
+# DO_CONVECTION builds of the cell operator, velocity (1, 2, 3)); the
+# reference's degree-2 variants are not symmetric, so degree 2 is pinned by
+# the tensor-product identity M = JxW (S^T W S) x (S^T W S) x (S^T W S)
+CELL_IJ = np.array([4.0, 2.0, 4.0 / 3.0])
+
+
+@pytest.mark.parametrize("p", [1, 3, 4, 5, 6, 7, 8])
+def test_cell_mass_convection(golden, p):
+    g = golden("cell_ops.npz")
+    jxw = 1.0 / np.prod(CELL_IJ)
+    x = g["cell_x_%d" % p]
+    assert rel(O.cell_op(p, O.BASIS_HERMITE, O.OP_MASS, CELL_IJ, jxw, (0, 0, 0), x), g["cell_mass_%d" % p]) < 1e-13
+    assert rel(O.cell_op(p, O.BASIS_HERMITE, O.OP_CONVECTION, CELL_IJ, jxw, (1, 2, 3), x),
+               g["cell_conv_%d" % p]) < 1e-13
+
+
+@pytest.mark.parametrize("basis", [O.BASIS_GLL, O.BASIS_HERMITE])
+@pytest.mark.parametrize("p", [2, 4])
+def test_cell_mass_convection_tensor_identity(p, basis):
+    """the oracle's sum-factorised variants equal the dense Kronecker forms
+    built from its 1D tables: M = JxW M1 x M1 x M1 with M1 = S^T W S, and the
+    convection form sum_d (ij_d b_d) JxW (S^T W D S in direction d)"""
+    n = p + 1
+    a = O.shape_arrays(p, basis)
+    S = np.array(a["S"])[: n * n].reshape(n, n)
+    D = np.array(a["D"])[: n * n].reshape(n, n)
+    W = np.diag(np.array(a["wq"])[:n])
+    jxw = 1.0 / np.prod(CELL_IJ)
+    M1, C1 = S.T @ W @ S, (D @ S).T @ W @ S
+    k = np.kron
+    M = jxw * k(k(M1, M1), M1)
+    b = np.array([1.0, 2.0, 3.0])
+    Cv = jxw * (CELL_IJ[0] * b[0] * k(k(M1, M1), C1) + CELL_IJ[1] * b[1] * k(k(M1, C1), M1)
+                + CELL_IJ[2] * b[2] * k(k(C1, M1), M1))
+    x = np.random.default_rng(p).uniform(-1, 1, n ** 3)
+    assert rel(O.cell_op(p, basis, O.OP_MASS, CELL_IJ, jxw, (0, 0, 0), x), M @ x) < 1e-14
+    assert rel(O.cell_op(p, basis, O.OP_CONVECTION, CELL_IJ, jxw, b, x), Cv @ x) < 1e-14
+    assert np.abs(M - M.T).max() < 1e-15
+
+
+@pytest.mark.parametrize("p", [1, 3, 4, 5, 6, 7, 8])
+def test_continuous_mass_convection(golden, p):
+    g = golden("cell_ops.npz")
+    nc = tuple(int(v) for v in g["nc_%d" % p])
+    m = O.mesh(p, nc, basis=O.BASIS_HERMITE, length=tuple(g["len_%d" % p]))
+    x = g["cont_x_%d" % p]
+    assert rel(O.cont_apply_op(m, O.OP_MASS, x), g["cont_mass_%d" % p]) < 1e-13
+    assert rel(O.cont_apply_op(m, O.OP_CONVECTION, x, (1, 2, 3)), g["cont_conv_%d" % p]) < 1e-13
