@@ -235,9 +235,10 @@ def cellop_fixtures():
     Hermite-like cell operator (velocity (1, 2, 3)): single Cartesian cells
     with inverse Jacobian diag(4, 2, 4/3) and small affine boxes with
     homogeneous Dirichlet conditions.  Degree 2 is stored too, but the
-    reference's degree-2 variants are not symmetric (its mass matrix differs
-    from S^T W S by 32 %), so the tests pin degree 2 by the tensor-product
-    identity instead."""
+    reference's transposed values kernel drops the middle point for odd n
+    (matrix_vector_kernel.h:130-131), which is wrong for the Hermite-like
+    degree-2 basis (the reference's degree-2 mass matrix is not symmetric),
+    so the tests pin degree 2 by the tensor-product identity instead."""
     rng = np.random.default_rng(20241209)
     out = {}
     ij = np.array([4.0, 2.0, 4.0 / 3.0])

@@ -179,8 +179,10 @@ def test_dg_precomputed(golden, p):
 
 # mass matrix and convection form (the reference's DO_MASS_MATRIX and
 # DO_CONVECTION builds of the cell operator, velocity (1, 2, 3)); the
-# reference's degree-2 variants are not symmetric, so degree 2 is pinned by
-# the tensor-product identity M = JxW (S^T W S) x (S^T W S) x (S^T W S)
+# reference's transposed values kernel drops the middle point for odd n
+# (matrix_vector_kernel.h:130-131), wrong for the Hermite-like degree-2
+# basis, so degree 2 is pinned by the tensor-product identity
+# M = JxW (S^T W S) x (S^T W S) x (S^T W S)
 CELL_IJ = np.array([4.0, 2.0, 4.0 / 3.0])
 
 
