@@ -56,9 +56,9 @@ def test_cellops_vs_oracle(p, dirichlet):
 
 def test_mass_identities_48():
     """48^3 cells, p=4 (12.2 M DoF), no Dirichlet: the mass matrix is
-    symmetric positive definite and integrates constants to the volume;
-    the convection form of a constant vanishes (grad 1 = 0 on the test side
-    is not implied, but sum_i (u, b.grad phi_i) = (u, b.grad 1) = 0)"""
+    symmetric positive definite and integrates constants to the volume; the
+    convection form sums to zero over all test functions,
+    sum_i (u, b . grad phi_i) = (u, b . grad 1) = 0"""
     torch = torch_cuda()
     sf = _sf()
     nc, length = (48, 48, 48), (1.0, 2.0, 0.5)
@@ -99,3 +99,20 @@ def test_cellops_unsupported():
     with pytest.raises(sf.SFError) as e:
         op.diagonal(y)
     assert e.value.code == sf.SF_ERR_UNSUPPORTED
+
+
+def test_mass_cg_unpreconditioned():
+    """CG on the mass matrix (SPD) without a preconditioner, FP64 and
+    FP32-inner/FP64-refined"""
+    torch = torch_cuda()
+    sf = _sf()
+    op = sf.Operator(sf.OP_MASS, degree=3, n_cells=(6, 5, 4), length=(1.0, 0.8, 0.7))
+    b = torch.tensor(np.random.default_rng(5).standard_normal(op.n_dofs), device="cuda:0")
+    for mode in (0, 1):
+        x = torch.zeros_like(b)
+        opts = sf.default_solve_opts(mode=mode, precond=0, rtol=1e-10)
+        code, st = op.cg_solve(b, x, opts)
+        assert code == 0, sf.lib().sf_last_error()
+        r = torch.empty_like(x)
+        op.vmult(x, r)
+        assert float((r - b).norm() / b.norm()) < 1e-9
