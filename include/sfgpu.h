@@ -71,10 +71,13 @@ typedef enum {
   SF_OP_MASS = 4,      /* continuous mass matrix (u, v), affine meshes; the
                           DO_MASS_MATRIX variant of the cell Laplacian
                           (evaluation_cell_laplacian.h:299-326)              */
-  SF_OP_CONVECTION = 5 /* continuous convection form (u, b . grad v) with a
+  SF_OP_CONVECTION = 5, /* continuous convection form (u, b . grad v) with a
                           constant b = desc.velocity, affine meshes; the
                           DO_CONVECTION variant (evaluation_cell_laplacian.h:
                           328-354), there with b = (1, 2, 3)                 */
+  SF_OP_LAPLACE_UNSTRUCTURED = 6 /* continuous Laplacian on an unstructured
+                          hexahedral mesh (sf_create_unstructured; the
+                          reference has no mesh input at all)                */
 } sf_op_kind;
 
 typedef enum { SF_BASIS_GLL = 0, SF_BASIS_HERMITE = 1 } sf_basis;
@@ -108,6 +111,27 @@ const char *sf_version(void);
  * on the device (FP64, plus an FP32 copy).  Synchronous. */
 int sf_create(const sf_desc *desc, sf_op **op);
 int sf_destroy(sf_op *op);
+
+/* The continuous Laplacian on an unstructured hexahedral mesh of degree
+ * 1..8 (no counterpart in the reference, whose evaluators take structured
+ * meshes only).  Host arrays, copied:
+ *  - cell_nodes[e (p+1)^3 + (z (p+1) + y)(p+1) + x]: global index in
+ *    [0, n_nodes) of node (x, y, z) of cell e, in the cell-local order of the
+ *    structured layout (x fastest).  Each cell's orientation is the caller's:
+ *    a rotated or reflected cell lists its nodes in its own local frame.
+ *  - merged6[e][6][(p+1)^3]: JxW J^-1 J^-T at the Gauss points of cell e in
+ *    that local frame (order xx, yy, zz, xy, xz, yz; quadrature weight
+ *    included), as sf_set_geometry.
+ *  - dirichlet[node] != 0: homogeneous Dirichlet node (row y = x); may be
+ *    NULL.
+ * Cells are coloured greedily on the host (cells of one colour share no
+ * node) and summed colour by colour without atomics.  The handle takes
+ * sf_vmult, sf_vmult_batched, sf_chebyshev_step, and sf_cg_solve without a
+ * preconditioner; n_dofs = n_nodes.  basis: sf_basis; precisions as in
+ * sf_desc. */
+int sf_create_unstructured(int degree, int basis, long long n_cells, long long n_nodes,
+                           const int *cell_nodes, const double *merged6,
+                           const unsigned char *dirichlet, int precisions, sf_op **op);
 /* number of vector entries, number of cells */
 int sf_sizes(const sf_op *op, long long *n_dofs, long long *n_cells);
 

@@ -68,6 +68,8 @@ def lib():
         L.sfo_cell_apply.argtypes = [C.POINTER(Shape), _dp, C.c_int, _dp, _dp]
         L.sfo_cell_op.argtypes = [C.POINTER(Shape), C.c_int, _dp, C.c_double, _dp, _dp, _dp]
         L.sfo_cont_apply_op.argtypes = [C.POINTER(Mesh), C.c_int, _dp, _dp, _dp]
+        L.sfo_unstructured_apply.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_void_p,
+                                             _dp, C.c_void_p, _dp, _dp]
         L.sfo_dg_n_dofs.argtypes = [C.POINTER(DG)]
         L.sfo_dg_n_dofs.restype = C.c_longlong
         for f in ("sfo_dg_sipg_apply", "sfo_dg_advect_apply", "sfo_dg_advect_apply_transpose"):
@@ -196,6 +198,72 @@ def cont_apply_op(m: Mesh, kind, x, b=(0.0, 0.0, 0.0)):
     lib().sfo_cont_apply_op(C.byref(m), kind, np.ascontiguousarray(b, dtype=np.float64),
                             np.ascontiguousarray(x, dtype=np.float64), y)
     return y
+
+
+def unstructured_apply(degree, basis, idx, G, n_nodes, x, dirichlet=None):
+    """Laplacian on an unstructured hexahedral mesh (idx int32 [cell][nq])"""
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    nq = (degree + 1) ** 3
+    d = None if dirichlet is None else np.ascontiguousarray(dirichlet, dtype=np.uint8)
+    y = np.zeros(n_nodes)
+    lib().sfo_unstructured_apply(degree, basis, idx.size // nq, n_nodes, idx.ctypes.data,
+                                 np.ascontiguousarray(G, dtype=np.float64),
+                                 None if d is None else d.ctypes.data,
+                                 np.ascontiguousarray(x, dtype=np.float64), y)
+    return y
+
+
+def structured_as_unstructured(m: Mesh):
+    """index array [cell][nq] and Dirichlet mask of a structured mesh in the
+    global lexicographic numbering (cells x fastest)"""
+    p, n = m.degree, m.degree + 1
+    nc = [m.n_cells[d] for d in range(3)]
+    Nx, Ny, Nz = p * nc[0] + 1, p * nc[1] + 1, p * nc[2] + 1
+    c, b, a = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    k, j, i = np.meshgrid(np.arange(nc[2]), np.arange(nc[1]), np.arange(nc[0]), indexing="ij")
+    X = (i.ravel()[:, None] * p + a.ravel()[None, :])
+    Y = (j.ravel()[:, None] * p + b.ravel()[None, :])
+    Z = (k.ravel()[:, None] * p + c.ravel()[None, :])
+    idx = ((Z * Ny + Y) * Nx + X).astype(np.int32)
+    N = Nx * Ny * Nz
+    dmask = np.zeros(N, dtype=np.uint8)
+    if m.dirichlet:
+        g = np.arange(N)
+        Xg, Yg, Zg = g % Nx, (g // Nx) % Ny, g // (Nx * Ny)
+        dmask[(Xg == 0) | (Yg == 0) | (Zg == 0) | (Xg == Nx - 1) | (Yg == Ny - 1) | (Zg == Nz - 1)] = 1
+    return idx, dmask
+
+
+def reorient_cell(idx_e, G_e, n, perm, flips):
+    """the same cell described in another local frame: new axis d is old
+    axis perm[d], reflected when flips[d]; returns the node indices and the
+    merged tensor (P^T G P per point) in the new frame"""
+    Gm = np.zeros((n, n, n, 3, 3))
+    g = G_e.reshape(6, n, n, n)
+    pairs = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
+    for e, (r, s) in enumerate(pairs):
+        Gm[..., r, s] = g[e]
+        Gm[..., s, r] = g[e]
+    P = np.zeros((3, 3))
+    for d in range(3):
+        P[perm[d], d] = -1.0 if flips[d] else 1.0
+    old = idx_e.reshape(n, n, n)
+    new_idx = np.zeros_like(old)
+    new_G = np.zeros((6, n, n, n))
+    for cz in range(n):
+        for cy in range(n):
+            for cx in range(n):
+                newc = (cx, cy, cz)
+                oldc = [0, 0, 0]
+                for d in range(3):
+                    v = newc[d]
+                    oldc[perm[d]] = n - 1 - v if flips[d] else v
+                ox, oy, oz = oldc
+                new_idx[cz, cy, cx] = old[oz, oy, ox]
+                Gn = P.T @ Gm[oz, oy, ox] @ P
+                for e, (r, s) in enumerate(pairs):
+                    new_G[e, cz, cy, cx] = Gn[r, s]
+    return new_idx.ravel(), new_G.ravel()
 
 
 def dg(degree, n_cells, h, penalty=1.0, velocity=(1.0, 0.5, 0.25), inverse_mass=1):

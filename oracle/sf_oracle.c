@@ -840,6 +840,31 @@ void sfo_cont_apply_op(const sfo_mesh *m, int kind, const double *b,
   }
 }
 
+/* unstructured meshes: no counterpart in the reference (its evaluators take
+ * structured meshes); the cell operator is cell_apply_k */
+void sfo_unstructured_apply(int degree, int basis, long long n_cells, long long n_nodes,
+                            const int *idx, const double *G, const unsigned char *dirichlet,
+                            const double *x, double *y)
+{
+  sfo_shape s;
+  sfo_shape_init(degree, basis, &s);
+  const int nq = s.n * s.n * s.n;
+  memset(y, 0, sizeof(double) * n_nodes);
+  double *u = (double *)malloc(sizeof(double) * nq * 2);
+  double *v = u + nq;
+  for (long long e = 0; e < n_cells; ++e) {
+    const int *id = idx + e * nq;
+    for (int q = 0; q < nq; ++q) u[q] = (dirichlet && dirichlet[id[q]]) ? 0. : x[id[q]];
+    cell_apply_k(&s, G + e * 6 * nq, nq, NULL, u, v);
+    for (int q = 0; q < nq; ++q)
+      if (!(dirichlet && dirichlet[id[q]])) y[id[q]] += v[q];
+  }
+  free(u);
+  if (dirichlet)
+    for (long long i = 0; i < n_nodes; ++i)
+      if (dirichlet[i]) y[i] = x[i];
+}
+
 void sfo_cont_kappa_grad(const sfo_mesh *m, const double *G, const double *u,
                          const double *lam, double *dk)
 {

@@ -108,6 +108,13 @@ void sfo_cell_op(const sfo_shape *s, int kind, const double *ij, double jxw,
 void sfo_cont_apply_op(const sfo_mesh *m, int kind, const double *b,
                        const double *x, double *y);
 
+/* y = A x for the Laplacian on an unstructured hexahedral mesh: cell e's
+ * local node q (x fastest) is idx[e nq + q], G[e][6][nq] its merged tensor,
+ * dirichlet[node] != 0 (or NULL) homogeneous Dirichlet rows y = x */
+void sfo_unstructured_apply(int degree, int basis, long long n_cells, long long n_nodes,
+                            const int *idx, const double *G, const unsigned char *dirichlet,
+                            const double *x, double *y);
+
 /* ---------------- DG operators (cell-major layout, periodic) ------------- */
 typedef struct {
   int degree;

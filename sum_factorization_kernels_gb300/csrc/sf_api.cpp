@@ -5,6 +5,10 @@
 #include <new>
 #include <string>
 
+#include <algorithm>
+#include <memory>
+#include <vector>
+
 #include "sf_internal.h"
 #include "sf_launch.h"
 
@@ -59,7 +63,11 @@ int check_prec(const sf_op *op, int prec)
   return SF_OK;
 }
 
-bool is_continuous(int kind) { return kind == SF_OP_LAPLACE || kind == SF_OP_MASS || kind == SF_OP_CONVECTION; }
+bool is_continuous(int kind)
+{
+  return kind == SF_OP_LAPLACE || kind == SF_OP_MASS || kind == SF_OP_CONVECTION ||
+         kind == SF_OP_LAPLACE_UNSTRUCTURED;
+}
 
 int check_ptr(const void *p, int prec, const char *name)
 {
@@ -135,7 +143,10 @@ int sf_create(const sf_desc *desc, sf_op **out)
   if (!desc || !out) return fail(SF_ERR_NULL, "desc/op is NULL");
   *out = nullptr;
   const sf_desc &d = *desc;
-  if (d.kind < SF_OP_LAPLACE || d.kind > SF_OP_CONVECTION) return fail(SF_ERR_INVALID, "unknown operator kind");
+  if (d.kind < SF_OP_LAPLACE || d.kind > SF_OP_CONVECTION) {
+    if (d.kind == SF_OP_LAPLACE_UNSTRUCTURED) return fail(SF_ERR_INVALID, "unstructured meshes: sf_create_unstructured");
+    return fail(SF_ERR_INVALID, "unknown operator kind");
+  }
   const bool cont = is_continuous(d.kind);
   if (d.degree < 1 || d.degree > kMaxDegree) return fail(SF_ERR_UNSUPPORTED, "degree must be 1..8");
   for (int k = 0; k < 3; ++k) {
@@ -197,6 +208,118 @@ int sf_create(const sf_desc *desc, sf_op **out)
     }
   }
   *out = op;
+  return SF_OK;
+}
+
+int sf_create_unstructured(int degree, int basis, long long n_cells, long long n_nodes, const int *cell_nodes,
+                           const double *merged6, const unsigned char *dirichlet, int precisions, sf_op **out)
+{
+  if (!out || !cell_nodes || !merged6) return fail(SF_ERR_NULL, "op/cell_nodes/merged6 is NULL");
+  *out = nullptr;
+  if (degree < 1 || degree > kMaxDegree) return fail(SF_ERR_UNSUPPORTED, "degree must be 1..8");
+  if (basis != SF_BASIS_GLL && basis != SF_BASIS_HERMITE) return fail(SF_ERR_INVALID, "unknown basis");
+  if (n_cells < 1 || n_cells >= (1LL << 31) || n_nodes < 1 || n_nodes >= (1LL << 31))
+    return fail(SF_ERR_INVALID, "n_cells and n_nodes must be in [1, 2^31)");
+  if ((precisions & 3) == 0) return fail(SF_ERR_INVALID, "precisions must select FP64 and/or FP32");
+  const int n = degree + 1, n2 = n * n, n3 = n * n * n;
+  const long long ne = n_cells * n3;
+  for (long long i = 0; i < ne; ++i)
+    if (cell_nodes[i] < 0 || cell_nodes[i] >= n_nodes) return fail(SF_ERR_INVALID, "cell_nodes entry out of range");
+  // greedy colouring: a cell takes the smallest colour no cell sharing one of
+  // its nodes has; node -> cells in compressed rows
+  std::vector<long long> start((size_t)n_nodes + 1, 0);
+  for (long long i = 0; i < ne; ++i) ++start[(size_t)cell_nodes[i] + 1];
+  for (long long v = 0; v < n_nodes; ++v) start[(size_t)v + 1] += start[(size_t)v];
+  std::vector<int> node_cells((size_t)ne);
+  {
+    std::vector<long long> fill(start.begin(), start.end() - 1);
+    for (long long e = 0; e < n_cells; ++e)
+      for (int q = 0; q < n3; ++q) node_cells[(size_t)fill[(size_t)cell_nodes[e * n3 + q]]++] = (int)e;
+  }
+  std::vector<int> color((size_t)n_cells, -1), stamp(1024, -1);
+  int n_colors = 0;
+  for (long long e = 0; e < n_cells; ++e) {
+    for (int q = 0; q < n3; ++q) {
+      const int v = cell_nodes[e * n3 + q];
+      for (long long k = start[(size_t)v]; k < start[(size_t)v + 1]; ++k) {
+        const int c = color[(size_t)node_cells[(size_t)k]];
+        if (c >= 0) stamp[(size_t)c] = (int)e;
+      }
+    }
+    int c = 0;
+    while (stamp[(size_t)c] == (int)e) ++c;
+    if (c >= 1023) return fail(SF_ERR_UNSUPPORTED, "mesh needs more than 1023 colours");
+    color[(size_t)e] = c;
+    n_colors = std::max(n_colors, c + 1);
+  }
+  // first colour to touch each node; keep / add bits per cell column
+  std::vector<int> first((size_t)n_nodes, 1 << 30);
+  for (long long e = 0; e < n_cells; ++e)
+    for (int q = 0; q < n3; ++q) {
+      int &f = first[(size_t)cell_nodes[e * n3 + q]];
+      f = std::min(f, color[(size_t)e]);
+    }
+  std::vector<unsigned> masks((size_t)(n_cells * n2), 0u);
+  for (long long e = 0; e < n_cells; ++e)
+    for (int t = 0; t < n2; ++t) {
+      unsigned m = 0;
+      for (int z = 0; z < n; ++z) {
+        const int v = cell_nodes[e * n3 + z * n2 + t];
+        if (!(dirichlet && dirichlet[v])) m |= 1u << z;
+        if (first[(size_t)v] < color[(size_t)e]) m |= 1u << (16 + z);
+      }
+      masks[(size_t)(e * n2 + t)] = m;
+    }
+  std::vector<long long> cstart((size_t)n_colors + 1, 0);
+  for (long long e = 0; e < n_cells; ++e) ++cstart[(size_t)color[(size_t)e] + 1];
+  for (int c = 0; c < n_colors; ++c) cstart[(size_t)c + 1] += cstart[(size_t)c];
+  std::vector<int> cells((size_t)n_cells);
+  {
+    std::vector<long long> fill(cstart.begin(), cstart.end() - 1);
+    for (long long e = 0; e < n_cells; ++e) cells[(size_t)fill[(size_t)color[(size_t)e]]++] = (int)e;
+  }
+
+  sf_op *op = new (std::nothrow) sf_op();
+  if (!op) return fail(SF_ERR_OOM, "host allocation failed");
+  std::unique_ptr<sf_op> guard(op);
+  op->desc = sf_desc{};
+  op->desc.kind = SF_OP_LAPLACE_UNSTRUCTURED;
+  op->desc.degree = degree;
+  op->desc.basis = basis;
+  op->desc.dirichlet = dirichlet ? 1 : 0;
+  op->desc.precisions = precisions;
+  for (int k = 0; k < 3; ++k) {
+    op->desc.n_cells[k] = 1;
+    op->desc.length[k] = 1.0;
+    op->h[k] = 1.0;
+  }
+  fill_shape(degree, basis, op->shape);
+  op->n = n;
+  op->n_cells = n_cells;
+  op->n_dofs = n_nodes;
+  op->unstr.reset(new (std::nothrow) sf_unstructured());
+  if (!op->unstr) return fail(SF_ERR_OOM, "host allocation failed");
+  sf_unstructured &M = *op->unstr;
+  M.n_nodes = n_nodes;
+  M.color_start = cstart;
+  SF_RET(op->dev_err.alloc(sizeof(int)));
+  SF_CUDA_TRY(cudaMemset(op->dev_err.ptr, 0, sizeof(int)));
+  SF_RET(M.idx.alloc(sizeof(int) * (size_t)ne));
+  SF_CUDA_TRY(cudaMemcpy(M.idx.ptr, cell_nodes, sizeof(int) * (size_t)ne, cudaMemcpyHostToDevice));
+  SF_RET(M.masks.alloc(sizeof(unsigned) * masks.size()));
+  SF_CUDA_TRY(cudaMemcpy(M.masks.ptr, masks.data(), sizeof(unsigned) * masks.size(), cudaMemcpyHostToDevice));
+  SF_RET(M.cells.alloc(sizeof(int) * cells.size()));
+  SF_CUDA_TRY(cudaMemcpy(M.cells.ptr, cells.data(), sizeof(int) * cells.size(), cudaMemcpyHostToDevice));
+  op->geo_stride = 6LL * n3;
+  const size_t entries = (size_t)(n_cells * op->geo_stride);
+  SF_RET(op->geo64.alloc(entries * sizeof(double)));
+  SF_CUDA_TRY(cudaMemcpy(op->geo64.ptr, merged6, entries * sizeof(double), cudaMemcpyHostToDevice));
+  if (precisions & 2) {
+    SF_RET(op->geo32.alloc(entries * sizeof(float)));
+    SF_RET(launch_convert((long long)entries, SF_FP64, op->geo64.ptr, SF_FP32, op->geo32.ptr, 0));
+  }
+  SF_CUDA_TRY(cudaDeviceSynchronize());
+  *out = guard.release();
   return SF_OK;
 }
 
@@ -423,8 +546,9 @@ int sf_diagonal(sf_op *op, int prec, void *diag, void *stream)
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
   SF_RET(check_prec(op, prec));
   SF_RET(check_ptr(diag, prec, "diag"));
-  if (op->desc.kind == SF_OP_MASS || op->desc.kind == SF_OP_CONVECTION)
-    return fail(SF_ERR_UNSUPPORTED, "diagonal: Laplacian and DG operators only");
+  if (op->desc.kind == SF_OP_MASS || op->desc.kind == SF_OP_CONVECTION ||
+      op->desc.kind == SF_OP_LAPLACE_UNSTRUCTURED)
+    return fail(SF_ERR_UNSUPPORTED, "diagonal: structured Laplacian and DG operators only");
   if (op->desc.kind == SF_OP_LAPLACE) return launch_cont_diagonal(op, prec, diag, (cudaStream_t)stream);
   if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
     return launch_dg_precomputed_diagonal(op, prec, diag, (cudaStream_t)stream);

@@ -3,7 +3,9 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <memory>
 #include <string>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -49,6 +51,15 @@ struct DevBuf {
 
 } // namespace sf
 
+// unstructured-mesh data of a SF_OP_LAPLACE_UNSTRUCTURED handle
+struct sf_unstructured {
+  sf::DevBuf idx;                     // [cell][n^3] node indices (int32)
+  sf::DevBuf masks;                   // [cell][n^2] keep / add bits (uint32)
+  sf::DevBuf cells;                   // cells grouped by colour (int32)
+  std::vector<long long> color_start; // colour c: cells[color_start[c] .. color_start[c+1])
+  long long n_nodes = 0;
+};
+
 // the opaque handle
 struct sf_op {
   sf_desc desc;
@@ -63,6 +74,7 @@ struct sf_op {
   sf::DevBuf scratch;           // operator-private scratch (transpose, M^-1)
   sf::DevBuf geoPair;           // FP32 geometry for the pair kernel (pair-interleaved)
   sf::DevBuf geoLine64, geoLine32; // geometry in the line kernel's walk order
+  std::unique_ptr<sf_unstructured> unstr; // SF_OP_LAPLACE_UNSTRUCTURED only
   long long geoPair_stride = 0;
   sf::DevBuf dev_err;           // device error flags (bounded waits)
   int kernel_variant = 0;       // sf_kernel_variant

@@ -9,6 +9,7 @@ namespace sf {
 
 // sf_laplace.cu
 int launch_cont_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st);
+int launch_unstructured_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st);
 int launch_cont_kappa_grad(const sf_op *op, int prec, const void *u, const void *lam, void *dk,
                            cudaStream_t st);
 int launch_geometry(const sf_op *op, double *G, cudaStream_t st);

@@ -21,6 +21,7 @@ STATUS = {0: "SF_OK", -1: "SF_ERR_INVALID", -2: "SF_ERR_NULL", -3: "SF_ERR_UNSUP
  SF_ERR_BREAKDOWN, SF_ERR_ALIGN, SF_ERR_STATE) = range(-1, -10, -1)
 FP64, FP32 = 0, 1
 OP_LAPLACE, OP_DG_SIPG, OP_DG_ADVECT, OP_DG_PRECOMPUTED, OP_MASS, OP_CONVECTION = 0, 1, 2, 3, 4, 5
+OP_LAPLACE_UNSTRUCTURED = 6
 BASIS_GLL, BASIS_HERMITE = 0, 1
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2
@@ -32,7 +33,7 @@ EXPORTS = [
     "sf_vmult_transpose_batched", "sf_chebyshev_step", "sf_vector_update", "sf_diagonal",
     "sf_kappa_gradient", "sf_solve_opts_default", "sf_cg_solve", "sf_convert", "sf_dot",
     "sf_shape_tables", "sf_set_kernel_variant", "sf_device_status", "sf_vmult_transpose_static",
-    "sf_rk_stage", "sf_lsrk_step",
+    "sf_rk_stage", "sf_lsrk_step", "sf_create_unstructured",
 ]
 
 
@@ -76,6 +77,7 @@ def lib():
         L.sf_last_error.restype = C.c_char_p
         L.sf_version.restype = C.c_char_p
         L.sf_create.argtypes = [C.POINTER(Desc), C.POINTER(vp)]
+        L.sf_create_unstructured.argtypes = [C.c_int, C.c_int, ll, ll, vp, vp, vp, C.c_int, C.POINTER(vp)]
         L.sf_destroy.argtypes = [vp]
         L.sf_sizes.argtypes = [vp, C.POINTER(ll), C.POINTER(ll)]
         L.sf_set_geometry.argtypes = [vp, vp]
@@ -160,6 +162,29 @@ class Operator:
         self.n_dofs, self.n_cells = nd.value, nc.value
         self.degree = degree
         self.kind = kind
+
+    @classmethod
+    def unstructured(cls, degree, cell_nodes, merged6, n_nodes, dirichlet=None, basis=BASIS_GLL, precisions=3):
+        """continuous Laplacian on an unstructured hexahedral mesh
+        (sf_create_unstructured): cell_nodes int32 [cell][(p+1)^3], merged6
+        float64 [cell][6][(p+1)^3], dirichlet uint8 [n_nodes] or None"""
+        import numpy as np
+        idx = np.ascontiguousarray(cell_nodes, dtype=np.int32).ravel()
+        geo = np.ascontiguousarray(merged6, dtype=np.float64).ravel()
+        n3 = (degree + 1) ** 3
+        n_cells = idx.size // n3
+        dmask = None if dirichlet is None else np.ascontiguousarray(dirichlet, dtype=np.uint8)
+        self = cls.__new__(cls)
+        h = C.c_void_p()
+        check(lib().sf_create_unstructured(degree, basis, n_cells, int(n_nodes), idx.ctypes.data, geo.ctypes.data,
+                                           None if dmask is None else dmask.ctypes.data, precisions,
+                                           C.byref(h)))
+        self._h = h
+        self.desc = None
+        self.n_dofs, self.n_cells = int(n_nodes), n_cells
+        self.degree = degree
+        self.kind = OP_LAPLACE_UNSTRUCTURED
+        return self
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

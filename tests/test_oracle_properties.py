@@ -140,3 +140,34 @@ def test_precomputed_sipg_matrix_properties(p):
     d2 = O.dg(p, (3, 2, 2), (1.5, 2.4, 0.9))
     x = np.random.default_rng(p).uniform(-1, 1, n)
     assert np.abs(O.dg_precomputed_apply(d2, x) - 3.0 * A @ x).max() < 1e-12 * np.abs(A @ x).max() * 3
+
+
+# unstructured hexahedral meshes (no counterpart in the reference): the
+# structured mesh written as index arrays, renumbered, and with every cell
+# described in a random local frame (axis permutation and reflections) gives
+# the structured operator
+@pytest.mark.parametrize("basis", [O.BASIS_GLL, O.BASIS_HERMITE])
+@pytest.mark.parametrize("p", [1, 3, 4])
+def test_unstructured_equals_structured(p, basis):
+    m = O.mesh(p, (3, 2, 2), basis=basis, length=(1.0, 0.7, 0.9), deform=0.05)
+    G = O.cont_geometry(m)
+    N = O.cont_n_dofs(m)
+    idx, dmask = O.structured_as_unstructured(m)
+    x = np.random.default_rng(p).uniform(-1, 1, N)
+    y = O.cont_apply(m, G, x)
+    n, nc = p + 1, idx.shape[0]
+    rng = np.random.default_rng(10 + p)
+    perm_nodes = rng.permutation(N)             # new number of old node i
+    perm_cells = rng.permutation(nc)
+    Gc = G.reshape(nc, -1)
+    idx2 = np.empty_like(idx)
+    G2 = np.empty_like(Gc)
+    for new_e, e in enumerate(perm_cells):
+        a, g = O.reorient_cell(perm_nodes[idx[e]], Gc[e], n, rng.permutation(3), rng.integers(0, 2, 3))
+        idx2[new_e], G2[new_e] = a, g
+    x2 = np.empty(N)
+    x2[perm_nodes] = x
+    d2 = np.empty(N, dtype=np.uint8)
+    d2[perm_nodes] = dmask
+    y2 = O.unstructured_apply(p, basis, idx2, G2, N, x2, d2)
+    assert np.abs(y2[perm_nodes] - y).max() < 1e-13 * np.abs(y).max()
