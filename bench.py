@@ -223,8 +223,9 @@ def secondary_configs(stream, peak):
     same problem with the precomputed tensor-product SIPG operator),
     config 4 (variable kappa p=4 32^3: forward and adjoint), config 5 (DG
     advection p=4 48^3, 8 right-hand sides: forward / transpose, LSRK(5,4)
-    time steps, dot test), and the mass / convection variants of the cell
-    operator (p=4 affine 64^3 FP32)"""
+    time steps, dot test), the mass / convection variants of the cell
+    operator (p=4 affine 64^3 FP32) and the unstructured-mesh input
+    (p=4 48^3 FP32)"""
     import numpy as np
     import torch
 
@@ -380,6 +381,36 @@ def secondary_configs(stream, peak):
         res[name] = {"gdofs": round(op.n_dofs / t / 1e9, 3), "hbm_frac": round(8 * op.n_dofs / t / 1e9 / peak, 4)}
         del op, x, y
     out["cell_variants_p4_64c_affine_fp32"] = res
+    # ---- unstructured hexahedral input: the 48^3 p=4 box given as cell-node
+    # index arrays (lexicographic numbering) and per-cell merged geometry
+    # (affine tensor times Gauss weights); bytes: vectors, geometry, indices
+    # and the per-column masks ----
+    p_, nc_ = 4, 48
+    n_ = p_ + 1
+    S_, D_, xq_, wq_ = sfgpu.shape_tables(p_)
+    Nx = p_ * nc_ + 1
+    cz, cy, cx = np.meshgrid(np.arange(n_), np.arange(n_), np.arange(n_), indexing="ij")
+    kk, jj, ii = np.meshgrid(np.arange(nc_), np.arange(nc_), np.arange(nc_), indexing="ij")
+    idx = (((kk.ravel()[:, None] * p_ + cz.ravel()[None, :]) * Nx + (jj.ravel()[:, None] * p_ + cy.ravel()[None, :]))
+           * Nx + (ii.ravel()[:, None] * p_ + cx.ravel()[None, :])).astype(np.int32)
+    w3 = (wq_[:, None, None] * wq_[None, :, None] * wq_[None, None, :]).ravel()
+    h = 1.0 / nc_
+    g1 = np.zeros((6, n_ ** 3))
+    g1[:3] = h * w3                             # JxW / h_d^2 = h
+    geo = np.broadcast_to(g1, (nc_ ** 3, 6, n_ ** 3))
+    N = Nx ** 3
+    op = sfgpu.Operator.unstructured(p_, idx, geo, N, dirichlet=None, precisions=2)
+    del geo, idx
+    x = torch.rand(N, device="cuda", dtype=torch.float32) * 2 - 1
+    y = torch.empty_like(x)
+    t = time_apply(op, x, y, 30, 5, stream)
+    C = nc_ ** 3
+    bytes_apply = 8 * N + C * (6 * n_ ** 3 * 4 + n_ ** 3 * 4 + n_ ** 2 * 4)
+    out["unstructured_p4_48c_fp32"] = {"n_dofs": N, "gdofs": round(N / t / 1e9, 3),
+                                       "hbm_frac": round(bytes_apply / t / 1e9 / peak, 4),
+                                       "algorithmic_bytes_per_apply": bytes_apply}
+    del op, x, y
+    torch.cuda.empty_cache()
     return out
 
 
