@@ -49,13 +49,11 @@ struct DGArgs {
   T ijxw;         // 1 / jxw
   T jface[3];     // face area elements jxw * ij_d
   T tau[3];       // SIPG penalty per direction
-  T cdir[3];      // SIPG: ij_d^2 jxw ; advection: a_d ij_d jxw
-  T cw[3][N];     // cdir[d] w_m
+  T cw[3][N];     // c_d w_m, c_d = ij_d^2 jxw (SIPG), a_d ij_d jxw (advection)
   // advection flux coefficients per direction and side: fa, fb =
   // -(a.n) jface / 2, -|a.n| jface / 2 (forward), fa = -((a.n) + |a.n|)
   // jface / 2 (transpose)
   T fa[3][2], fb[3][2];
-  T an[3];        // advection velocity a_d
   T hd0;          // derivative of the first Hermite-like function at 0
   const T *__restrict__ x;
   T *__restrict__ y;
@@ -608,9 +606,7 @@ DGArgs<N, T> make_dg_args(const sf_op *op, bool transpose = false)
     A.ij[d] = T(ij);
     A.jface[d] = T(jxw * ij);
     A.tau[d] = T((N) * (N) * op->desc.penalty * ij);
-    A.an[d] = T(op->desc.velocity[d]);
     const double cdir = op->desc.kind == SF_OP_DG_SIPG ? ij * ij * jxw : op->desc.velocity[d] * ij * jxw;
-    A.cdir[d] = T(cdir);
     for (int m = 0; m < N; ++m) A.cw[d][m] = T(cdir * s.wq[m]);
     const double jf = jxw * ij;
     for (int side = 0; side < 2; ++side) {
