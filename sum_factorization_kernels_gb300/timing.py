@@ -2,8 +2,10 @@
 device memory): ``python -m sum_factorization_kernels_gb300.timing KIND ...``.
 
 KIND is ``laplace`` (continuous, deformed mesh), ``sipg`` (DG SIPG),
-``advect`` (DG upwind advection with inverse mass) or ``precomputed`` (DG
-SIPG in tensor-product form with precomputed 1D matrices).  Prints one line with the
+``advect`` (DG upwind advection with inverse mass), ``precomputed`` (DG
+SIPG in tensor-product form with precomputed 1D matrices), ``mass`` /
+``convection`` (continuous, affine) or ``unstructured`` (the affine box given
+as cell-node index arrays and per-cell geometry).  Prints one line with the
 apply rate summed over the right-hand sides and the vector traffic it implies.
 Used to drive profiler captures of one kernel on a small case.
 """
@@ -16,8 +18,34 @@ import torch
 from . import sfgpu as sf
 
 
+def unstructured_box(degree: int, ncells: int):
+    """the unit box of ncells^3 affine cells as an unstructured mesh: cell-node
+    indices in the lexicographic numbering and the merged tensor h w_q on the
+    diagonal"""
+    import numpy as np
+    p, n = degree, degree + 1
+    Nx = p * ncells + 1
+    cz, cy, cx = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    kk, jj, ii = np.meshgrid(np.arange(ncells), np.arange(ncells), np.arange(ncells), indexing="ij")
+    idx = (((kk.ravel()[:, None] * p + cz.ravel()[None, :]) * Nx + (jj.ravel()[:, None] * p + cy.ravel()[None, :]))
+           * Nx + (ii.ravel()[:, None] * p + cx.ravel()[None, :])).astype(np.int32)
+    _, _, _, wq = sf.shape_tables(degree)
+    w3 = (wq[:, None, None] * wq[None, :, None] * wq[None, None, :]).ravel()
+    g1 = np.zeros((6, n ** 3))
+    g1[:3] = w3 / ncells
+    geo = np.broadcast_to(g1, (ncells ** 3, 6, n ** 3))
+    return idx, geo, Nx ** 3
+
+
 def make_operator(kind: str, degree: int, ncells: int):
     n = (ncells,) * 3
+    if kind == "mass":
+        return sf.Operator(sf.OP_MASS, degree=degree, n_cells=n)
+    if kind == "convection":
+        return sf.Operator(sf.OP_CONVECTION, degree=degree, n_cells=n, velocity=(1.0, 2.0, 3.0))
+    if kind == "unstructured":
+        idx, geo, nn = unstructured_box(degree, ncells)
+        return sf.Operator.unstructured(degree, idx, geo, nn)
     if kind == "laplace":
         return sf.Operator(sf.OP_LAPLACE, degree=degree, n_cells=n, deform=0.05)
     if kind == "sipg":
@@ -31,7 +59,8 @@ def make_operator(kind: str, degree: int, ncells: int):
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("kind", choices=["laplace", "sipg", "advect", "precomputed"])
+    ap.add_argument("kind", choices=["laplace", "sipg", "advect", "precomputed", "mass", "convection",
+                                     "unstructured"])
     ap.add_argument("--degree", type=int, default=4)
     ap.add_argument("--ncells", type=int, default=32, help="cells per direction")
     ap.add_argument("--prec", choices=["fp32", "fp64"], default="fp32")
