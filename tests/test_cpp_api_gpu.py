@@ -1,5 +1,5 @@
 """Builds the C++ driver of include/sfgpu.hpp against libsfgpu.so and the
-oracle, runs it on the GPU and checks its verdict."""
+oracle, runs it on the GPU and checks its exit status."""
 import os
 import subprocess
 
