@@ -220,11 +220,18 @@ int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void 
 
 /* Kernel selection for the continuous Laplacian apply.  SF_KERNEL_AUTO and
  * SF_KERNEL_GENERIC: the packed line-ownership kernel (one thread per line
- * of a cell, several cells per warp group) for both precisions.
- * SF_KERNEL_PAIR: the FP32 paired line-ownership kernel (two cells per
- * thread in packed FP32x2 arithmetic).  For comparisons; no reference
- * counterpart. */
-typedef enum { SF_KERNEL_AUTO = 0, SF_KERNEL_GENERIC = 1, SF_KERNEL_PAIR = 2 } sf_kernel_variant;
+ * of a cell, several cells per warp group) for both precisions, structured
+ * or unstructured.  SF_KERNEL_PAIR: the FP32 paired line-ownership kernel
+ * (two cells per thread in packed FP32x2 arithmetic; structured meshes).
+ * SF_KERNEL_CELL: one block of cells per launch with block barriers and
+ * geometry read in the quadrature-point operation (unstructured meshes).
+ * For comparisons; no reference counterpart. */
+typedef enum {
+  SF_KERNEL_AUTO = 0,
+  SF_KERNEL_GENERIC = 1,
+  SF_KERNEL_PAIR = 2,
+  SF_KERNEL_CELL = 3
+} sf_kernel_variant;
 int sf_set_kernel_variant(sf_op *op, int variant);
 /* Device-side error flags of the handle's kernels (bit 0: a bounded wait
  * for an asynchronous copy timed out; the result of that apply is invalid).

@@ -318,6 +318,10 @@ int sf_create_unstructured(int degree, int basis, long long n_cells, long long n
     SF_RET(op->geo32.alloc(entries * sizeof(float)));
     SF_RET(launch_convert((long long)entries, SF_FP64, op->geo64.ptr, SF_FP32, op->geo32.ptr, 0));
   }
+  // the line kernel's walk-ordered geometry, colour by colour
+  op->deformed = true;
+  if (precisions & 1) SF_RET(pack_line_geometry(op, SF_FP64));
+  if (precisions & 2) SF_RET(pack_line_geometry(op, SF_FP32));
   SF_CUDA_TRY(cudaDeviceSynchronize());
   *out = guard.release();
   return SF_OK;
@@ -382,7 +386,7 @@ int sf_set_coefficient(sf_op *op, const double *kappa)
 int sf_set_kernel_variant(sf_op *op, int variant)
 {
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
-  if (variant < SF_KERNEL_AUTO || variant > SF_KERNEL_PAIR)
+  if (variant < SF_KERNEL_AUTO || variant > SF_KERNEL_CELL)
     return fail(SF_ERR_INVALID, "unknown kernel variant");
   op->kernel_variant = variant;
   SF_RET(derive_variant_geometry(op));

@@ -608,7 +608,10 @@ int cont_kgrad_n(const sf_op *op, int prec, const void *u, const void *l, void *
 
 int launch_cont_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
 {
-  if (op->desc.kind == SF_OP_LAPLACE_UNSTRUCTURED) return launch_unstructured_vmult(op, prec, x, y, st);
+  // unstructured meshes: the line kernel with index arrays by default, the
+  // block-barrier cell pipeline as the generic variant
+  if (op->desc.kind == SF_OP_LAPLACE_UNSTRUCTURED && op->kernel_variant == SF_KERNEL_CELL)
+    return launch_unstructured_vmult(op, prec, x, y, st);
   if (pair_path(op, prec)) return launch_cont_vmult_pair(op, (const float *)x, (float *)y, st);
   return launch_cont_vmult_line(op, prec, x, y, st);
 }

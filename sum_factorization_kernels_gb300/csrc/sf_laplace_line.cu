@@ -137,6 +137,12 @@ struct LineArgs {
   int Nx, plane;                // nodes per x line, per z plane
   T aff[3];
   T jxw;                        // mass / convection: cell volume (affine)
+  // unstructured meshes: node (x, y, z) of cell e at idx[e n^3 + (z n + y) n + x],
+  // umask[e n^2 + column]: keep bits 0..n-1, add bits 16..16+n-1, ucells: the
+  // colour's cells in walk order
+  const int *__restrict__ idx;
+  const unsigned *__restrict__ umask;
+  const int *__restrict__ ucells;
   T conv[3];                    // convection: b_d / h_d
   int dirichlet;
   int color, cx, cy, cz, mx, my;
@@ -153,10 +159,34 @@ struct LineArgs {
 // cell Laplacian, evaluation_cell_laplacian.h:299-354)
 enum { OP_LAPLACE = 0, OP_MASS = 1, OP_CONVECTION = 2 };
 
-template <int N, typename T, bool DEFORMED, bool KAPPA, int OPK = OP_LAPLACE>
-__global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, LineCfg<N, T>::PP.MINB)
+// column of an unstructured cell: its node indices and masks
+template <int N, typename T>
+__device__ __forceinline__ void unstr_column(const LineArgs<N, T> &A, bool valid, long long o, int l, int (&nd)[N],
+                                             ColumnMask &m)
+{
+  constexpr int N2 = N * N, N3 = N * N * N;
+  const long long cell = valid ? (long long)__ldg(A.ucells + o) : 0;
+  const unsigned u = valid ? __ldg(A.umask + cell * N2 + l) : 0u;
+  m.keep = u & 0xffffu;
+  m.add = u >> 16;
+#pragma unroll
+  for (int c = 0; c < N; ++c) nd[c] = valid ? __ldg(A.idx + cell * N3 + c * N2 + l) : 0;
+}
+
+template <int N, typename T>
+__device__ __forceinline__ void gather_nodes(const T *__restrict__ x, const int (&nd)[N], unsigned keep, T (&v)[N])
+{
+#pragma unroll
+  for (int c = 0; c < N; ++c) v[c] = ((keep >> c) & 1u) ? __ldg(x + nd[c]) : T(0);
+}
+
+template <int N, typename T, bool DEFORMED, bool KAPPA, int OPK = OP_LAPLACE, bool UNSTR = false>
+__global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
+                                  UNSTR && LineCfg<N, T>::PP.MINB > 1 ? LineCfg<N, T>::PP.MINB - 1
+                                                                     : LineCfg<N, T>::PP.MINB)
     line_vmult_kernel(const __grid_constant__ LineArgs<N, T> A)
 {
+  static_assert(!UNSTR || (DEFORMED && !KAPPA && OPK == OP_LAPLACE), "unstructured: deformed Laplacian only");
   using Cfg = LineCfg<N, T>;
   constexpr int N2 = Cfg::N2, N3 = Cfg::N3, K = Cfg::K, W = Cfg::W, GT = Cfg::GT;
   constexpr SlabLayout L0 = Cfg::L0, L1 = Cfg::L1, L2 = Cfg::L2;
@@ -197,7 +227,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
   // space; later cells follow by a division-free strided walk
   long long o = gid * K + k;
   int mi = 0, mj = 0, mk = 0;
-  if (o < A.count) {
+  if (!UNSTR && o < A.count) {
     const unsigned uo = (unsigned)o, umx = (unsigned)A.mx, umy = (unsigned)A.my;
     const unsigned q = uo / umx;
     mi = int(uo - q * umx);
@@ -225,10 +255,18 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
   // the current cell's column: bookkeeping, node base, gathered x; the next
   // cell's column is fetched during the current cell's integration sweeps
   bool valid = used && o < A.count;
-  ColumnMask msk = column_mask<N>(a, b, 2 * mi + A.cx, 2 * mj + A.cy, 2 * mk + A.cz, A.nc, A.color, dir, valid);
-  long long nb = cell_node_base<N>(2 * mi + A.cx, 2 * mj + A.cy, 2 * mk + A.cz, A.Nx, plane) + toff;
+  ColumnMask msk;
+  long long nb = 0;
+  int cn[N]; // unstructured: the column's node indices
   T xv[N];
-  gather_column<N, T>(A.x + nb, plane, msk.keep, xv);
+  if constexpr (UNSTR) {
+    unstr_column<N, T>(A, valid, o, l, cn, msk);
+    gather_nodes<N, T>(A.x, cn, msk.keep, xv);
+  } else {
+    msk = column_mask<N>(a, b, 2 * mi + A.cx, 2 * mj + A.cy, 2 * mk + A.cz, A.nc, A.color, dir, valid);
+    nb = cell_node_base<N>(2 * mi + A.cx, 2 * mj + A.cy, 2 * mk + A.cz, A.Nx, plane) + toff;
+    gather_column<N, T>(A.x + nb, plane, msk.keep, xv);
+  }
 
   for (long long o0 = gid * K; o0 < A.count; o0 += step, o += step) {
     const int ci = 2 * mi + A.cx, cj = 2 * mj + A.cy, ck = 2 * mk + A.cz;
@@ -426,11 +464,20 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
       y_ready = true;
     }
     T yo[N];
-    load_column_sums<N, T>(A.y + nb, plane, msk.add, yo);
-    const ColumnMask nmsk =
-        column_mask<N>(a, b, 2 * ni + A.cx, 2 * nj + A.cy, 2 * nk + A.cz, A.nc, A.color, dir, nvalid);
-    const long long nnb = cell_node_base<N>(2 * ni + A.cx, 2 * nj + A.cy, 2 * nk + A.cz, A.Nx, plane) + toff;
-    gather_column<N, T>(A.x + nnb, plane, nmsk.keep, xv);
+    ColumnMask nmsk;
+    long long nnb = 0;
+    int nn[N];
+    if constexpr (UNSTR) {
+#pragma unroll
+      for (int c = 0; c < N; ++c) yo[c] = ((msk.add >> c) & 1u) ? A.y[cn[c]] : T(0);
+      unstr_column<N, T>(A, nvalid, o + step, l, nn, nmsk);
+      gather_nodes<N, T>(A.x, nn, nmsk.keep, xv);
+    } else {
+      load_column_sums<N, T>(A.y + nb, plane, msk.add, yo);
+      nmsk = column_mask<N>(a, b, 2 * ni + A.cx, 2 * nj + A.cy, 2 * nk + A.cz, A.nc, A.color, dir, nvalid);
+      nnb = cell_node_base<N>(2 * ni + A.cx, 2 * nj + A.cy, 2 * nk + A.cz, A.Nx, plane) + toff;
+      gather_column<N, T>(A.x + nnb, plane, nmsk.keep, xv);
+    }
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B0[xl0 + L0.SX * m];
     eo_apply<N, -1>(A.DT, v, g);
@@ -461,7 +508,16 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
     for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
     eo_apply<N, 1>(A.ST, v, v);
     // ---- scatter the z column: first colour stores, later ones add ----
-    if (valid) store_column<N, T>(A.y + nb, A.x + nb, plane, msk.keep, v, yo);
+    if constexpr (UNSTR) {
+      if (valid) {
+#pragma unroll
+        for (int c = 0; c < N; ++c) A.y[cn[c]] = ((msk.keep >> c) & 1u) ? v[c] + yo[c] : __ldg(A.x + cn[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < N; ++c) cn[c] = nn[c];
+    } else {
+      if (valid) store_column<N, T>(A.y + nb, A.x + nb, plane, msk.keep, v, yo);
+    }
     msk = nmsk;
     nb = nnb;
     valid = nvalid;
@@ -480,7 +536,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS, Lin
 template <int N, typename T>
 __global__ void line_pack_geometry_kernel(const double *__restrict__ G, long long gstride, T *__restrict__ out,
                                           long long total, long long count, int nc0, int nc1, int cx, int cy,
-                                          int cz, int mx, int my)
+                                          int cz, int mx, int my, const int *__restrict__ cells)
 {
   using Cfg = LineCfg<N, T>;
   constexpr int KN2 = Cfg::KN2, N2 = Cfg::N2;
@@ -495,9 +551,14 @@ __global__ void line_pack_geometry_kernel(const double *__restrict__ G, long lon
       const int k = Cfg::PP.INTER ? tl % Cfg::K : tl / N2, l = Cfg::PP.INTER ? tl / Cfg::K : tl % N2;
       const long long o = blk * Cfg::K + k;
       if (o < count) {
-        const long long q = o / mx, mk = q / my;
-        const long long mi = o - q * mx, mj = q - mk * my;
-        const long long cell = ((2 * mk + cz) * nc1 + (2 * mj + cy)) * nc0 + (2 * mi + cx);
+        long long cell;
+        if (cells) {
+          cell = cells[o];
+        } else {
+          const long long q = o / mx, mk = q / my;
+          const long long mi = o - q * mx, mj = q - mk * my;
+          cell = ((2 * mk + cz) * nc1 + (2 * mj + cy)) * nc0 + (2 * mi + cx);
+        }
         v = T(G[cell * gstride + (long long)e * Cfg::N3 + c * N2 + l]);
       }
     }
@@ -528,8 +589,97 @@ int line_pack_impl(sf_op *op, DevBuf &buf)
     const long long blocks = std::min<long long>((n + 255) / 256, 152 * 32);
     line_pack_geometry_kernel<N, T><<<(unsigned)blocks, 256>>>((const double *)op->geo64.ptr, op->geo_stride,
                                                               (T *)buf.ptr + base, n, count, nc[0], nc[1], cx,
-                                                              cy, cz, mx, my);
+                                                              cy, cz, mx, my, nullptr);
     SF_CUDA_TRY(cudaGetLastError());
+  }
+  return SF_OK;
+}
+
+// unstructured meshes: the geometry of each colour's cells in walk order
+template <int N, typename T>
+int line_unstr_pack_impl(sf_op *op, DevBuf &buf)
+{
+  using Cfg = LineCfg<N, T>;
+  const sf_unstructured &M = *op->unstr;
+  long long total = 0;
+  for (size_t c = 0; c + 1 < M.color_start.size(); ++c)
+    total += (M.color_start[c + 1] - M.color_start[c] + Cfg::K - 1) / Cfg::K * Cfg::GB;
+  const size_t bytes = (size_t)total * sizeof(T);
+  if (buf.bytes != bytes) {
+    const int e = buf.alloc(bytes);
+    if (e != SF_OK) return e;
+  }
+  long long base = 0;
+  for (size_t c = 0; c + 1 < M.color_start.size(); ++c) {
+    const long long count = M.color_start[c + 1] - M.color_start[c];
+    const long long n = (count + Cfg::K - 1) / Cfg::K * Cfg::GB;
+    if (n == 0) continue;
+    const long long blocks = std::min<long long>((n + 255) / 256, 152 * 32);
+    line_pack_geometry_kernel<N, T><<<(unsigned)blocks, 256>>>(
+        (const double *)op->geo64.ptr, op->geo_stride, (T *)buf.ptr + base, n, count, 1, 1, 0, 0, 0, 1, 1,
+        (const int *)M.cells.ptr + M.color_start[c]);
+    SF_CUDA_TRY(cudaGetLastError());
+    base += n;
+  }
+  return SF_OK;
+}
+
+template <int N, typename T>
+int line_unstr_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
+{
+  using Cfg = LineCfg<N, T>;
+  const sf_unstructured &M = *op->unstr;
+  LineArgs<N, T> A{};
+  const Shape1D &s = op->shape;
+  A.S = eo_of<N, T>(s.S, false);
+  A.ST = eo_of<N, T>(s.S, true);
+  A.D = eo_of<N, T>(s.D, false);
+  A.DT = eo_of<N, T>(s.D, true);
+  for (int i = 0; i < N; ++i) A.w[i] = T(s.wq[i]);
+  A.x = x;
+  A.y = y;
+  A.err = (int *)op->dev_err.ptr;
+  A.idx = (const int *)M.idx.ptr;
+  A.umask = (const unsigned *)M.masks.ptr;
+  A.mx = A.my = 1;
+  const T *geo = (const T *)(sizeof(T) == 8 ? op->geoLine64.ptr : op->geoLine32.ptr);
+  if (!geo) {
+    set_error("line kernel: walk-ordered geometry missing");
+    return SF_ERR_STATE;
+  }
+  void (*kern)(const LineArgs<N, T>) = line_vmult_kernel<N, T, true, false, OP_LAPLACE, true>;
+  const size_t smem = 128 + size_t(Cfg::GROUPS) * Cfg::GROUP_BYTES;
+  const int threads = Cfg::GT * Cfg::GROUPS;
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   cudaSharedmemCarveoutMaxShared));
+  int per_sm = 0;
+  SF_RET_IF(resident_blocks_per_sm((const void *)kern, threads, smem, &per_sm));
+  int n_sm = 0, dev = 0;
+  SF_CUDA_TRY(cudaGetDevice(&dev));
+  SF_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+  long long base = 0;
+  for (size_t c = 0; c + 1 < M.color_start.size(); ++c) {
+    A.count = M.color_start[c + 1] - M.color_start[c];
+    if (A.count == 0) continue;
+    A.ucells = (const int *)M.cells.ptr + M.color_start[c];
+    A.geo = geo + base;
+    base += (A.count + Cfg::K - 1) / Cfg::K * Cfg::GB;
+    A.color = (int)c;
+    const long long steps = (A.count + Cfg::K - 1) / Cfg::K;
+    const long long blocks =
+        std::min<long long>((steps + Cfg::GROUPS - 1) / Cfg::GROUPS, (long long)per_sm * n_sm);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = c > 0 ? 1 : 0; // colour 0 reads x behind its producer
+    SF_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A));
   }
   return SF_OK;
 }
@@ -537,6 +687,7 @@ int line_pack_impl(sf_op *op, DevBuf &buf)
 template <int N, typename T>
 int line_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
 {
+  if (op->desc.kind == SF_OP_LAPLACE_UNSTRUCTURED) return line_unstr_vmult_impl<N, T>(op, x, y, st);
   using Cfg = LineCfg<N, T>;
   LineArgs<N, T> A{};
   const Shape1D &s = op->shape;
@@ -629,6 +780,10 @@ int line_vmult_n(const sf_op *op, int prec, const void *x, void *y, cudaStream_t
 template <int N>
 int line_pack_n(sf_op *op, int prec)
 {
+  if (op->unstr) {
+    if (prec == SF_FP64) return line_unstr_pack_impl<N, double>(op, op->geoLine64);
+    return line_unstr_pack_impl<N, float>(op, op->geoLine32);
+  }
   if (prec == SF_FP64) return line_pack_impl<N, double>(op, op->geoLine64);
   return line_pack_impl<N, float>(op, op->geoLine32);
 }
