@@ -281,6 +281,14 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
       ++nk;
     }
     T v[N], g[N], gz[N];
+    ColumnMask nmsk;
+    long long nnb = 0;
+    int nn[N];
+    if constexpr (UNSTR) {
+      // the next cell's node indices and masks arrive during this step's
+      // sweeps; its x column is gathered after the quadrature-point operation
+      unstr_column<N, T>(A, used && o + step < A.count, o + step, l, nn, nmsk);
+    }
     // ---- sweeps S_z (gathered column), S_x, S_y and D_y ----
     eo_apply<N, 1>(A.S, xv, v);
 #pragma unroll
@@ -464,13 +472,9 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
       y_ready = true;
     }
     T yo[N];
-    ColumnMask nmsk;
-    long long nnb = 0;
-    int nn[N];
     if constexpr (UNSTR) {
 #pragma unroll
       for (int c = 0; c < N; ++c) yo[c] = ((msk.add >> c) & 1u) ? A.y[cn[c]] : T(0);
-      unstr_column<N, T>(A, nvalid, o + step, l, nn, nmsk);
       gather_nodes<N, T>(A.x, nn, nmsk.keep, xv);
     } else {
       load_column_sums<N, T>(A.y + nb, plane, msk.add, yo);
