@@ -247,7 +247,7 @@ int sf_create_unstructured(int degree, int basis, long long n_cells, long long n
       }
     }
     int c = 0;
-    while (stamp[(size_t)c] == (int)e) ++c;
+    while (c < 1023 && stamp[(size_t)c] == (int)e) ++c;
     if (c >= 1023) return fail(SF_ERR_UNSUPPORTED, "mesh needs more than 1023 colours");
     color[(size_t)e] = c;
     n_colors = std::max(n_colors, c + 1);
