@@ -48,6 +48,15 @@ def algorithmic_bytes(p, n_dofs, n_cells, s):
     return 2 * s * n_dofs + 6 * s * (p + 1) ** 3 * n_cells
 
 
+def workload_config(p, ncells):
+    """the workload keys both arms report (the continuous node count
+    includes the Dirichlet boundary nodes)"""
+    return {"workload": "continuous Laplacian matvec, deformed %d^3 hex mesh, p=%d" % (ncells, p),
+            "degree": p, "n_cells": [ncells] * 3, "n_dofs": (p * ncells + 1) ** 3, "deform": DEFORM,
+            "geometry": "merged 6-entry JxW J^-1 J^-T per Gauss point, in the apply's precision",
+            "dirichlet": True}
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -199,8 +208,7 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "continuous Laplacian, deformed mesh, p=%d (CPU sample 16^3)" % p,
-                       "degree": p, "n_cells": [16, 16, 16], "deform": DEFORM},
+            "config": workload_config(p, args.ncells),
             "cpu_baseline": base,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -433,6 +441,7 @@ def run_ours(args):
     # ---- headline: FP32, degree p, inputs resident ----
     op = sfgpu.Operator(sfgpu.OP_LAPLACE, degree=p, n_cells=NCELLS, deform=DEFORM)
     N, C = op.n_dofs, op.n_cells
+    assert N == workload_config(p, args.ncells)["n_dofs"]
     gen = torch.Generator(device="cuda").manual_seed(1234 + rank)
     x64 = torch.rand(N, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1
     x32 = x64.float()
@@ -577,13 +586,10 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 5),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": "continuous Laplacian matvec, deformed %d^3 hex mesh, p=%d, FP32"
-                                   % (args.ncells, p),
-                       "degree": p, "n_cells": list(NCELLS), "n_dofs": N, "deform": DEFORM,
-                       "geometry": "merged 6-entry JxW J^-1 J^-T per Gauss point, FP32",
-                       "dirichlet": True, "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "working set %.2f GB > 129 MB L2, no flush" % (bytes_apply / 1e9),
-                       "fp64_gdofs_same_degree": fp64_value, "kernel_variants": variants},
+            "config": dict(workload_config(p, args.ncells),
+                           parallelism="replicas" if world > 1 else "single GPU",
+                           l2="working set %.2f GB > 129 MB L2, no flush" % (bytes_apply / 1e9),
+                           fp64_gdofs_same_degree=fp64_value, kernel_variants=variants),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": MEASURED_TRAFFIC.get((p, args.ncells)),
