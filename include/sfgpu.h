@@ -119,6 +119,7 @@ int sf_destroy(sf_op *op);
  *    [0, n_nodes) of node (x, y, z) of cell e, in the cell-local order of the
  *    structured layout (x fastest).  Each cell's orientation is the caller's:
  *    a rotated or reflected cell lists its nodes in its own local frame.
+ *    A cell lists each node once (SF_ERR_INVALID otherwise).
  *  - merged6[e][6][(p+1)^3]: JxW J^-1 J^-T at the Gauss points of cell e in
  *    that local frame (order xx, yy, zz, xy, xz, yz; quadrature weight
  *    included), as sf_set_geometry.

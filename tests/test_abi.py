@@ -69,3 +69,58 @@ def test_shape_tables_match_oracle():
             assert np.abs(D - a["D"]).max() < 2e-15 * np.abs(a["D"]).max()
             assert np.abs(x - a["xq"]).max() < 2e-16
             assert np.abs(w - a["wq"]).max() < 2e-15
+
+
+def test_size_limits_without_gpu():
+    """meshes past the index limits are refused before any device memory is
+    touched: 2^31 cells, a continuous node plane block of 2^31 entries (the
+    kernels' 32-bit node offsets), 2^40 vector entries"""
+    sfgpu, L = _lib()
+    h = C.c_void_p()
+
+    def desc(kind, degree, nc):
+        d = sfgpu.Desc()
+        d.kind, d.degree, d.precisions, d.penalty = kind, degree, 3, 1.0
+        for k in range(3):
+            d.n_cells[k], d.length[k] = nc[k], 1.0
+        return d
+
+    for kind, degree, nc, what in ((sfgpu.OP_LAPLACE, 1, (2048, 2048, 512), b"2^31 - 1 cells"),
+                                   (sfgpu.OP_LAPLACE, 8, (20000, 20000, 1), b"node plane"),
+                                   (sfgpu.OP_DG_SIPG, 8, (1200, 1200, 1200), b"too large")):
+        assert L.sf_create(C.byref(desc(kind, degree, nc)), C.byref(h)) == sfgpu.SF_ERR_INVALID, nc
+        assert what in L.sf_last_error()
+        assert not h.value
+
+
+def test_unstructured_validation_without_gpu():
+    """sf_create_unstructured checks its host arrays before any device work:
+    node indices in range, each node once per cell, degree, basis, counts"""
+    import numpy as np
+    sfgpu, L = _lib()
+    p, n3 = 1, 8
+    idx = np.arange(2 * n3, dtype=np.int32)
+    idx[n3:] -= 4                       # second cell shares a face with the first
+    geo = np.zeros(2 * 6 * n3)
+    h = C.c_void_p()
+
+    def create(cells, n_cells=2, n_nodes=12, degree=p, basis=0, precisions=3, geometry=geo):
+        return L.sf_create_unstructured(degree, basis, n_cells, n_nodes, cells.ctypes.data,
+                                        None if geometry is None else geometry.ctypes.data, None,
+                                        precisions, C.byref(h))
+
+    assert create(idx, geometry=None) == sfgpu.SF_ERR_NULL
+    assert create(idx, degree=9) == sfgpu.SF_ERR_UNSUPPORTED
+    assert create(idx, basis=5) == sfgpu.SF_ERR_INVALID
+    assert create(idx, n_cells=0) == sfgpu.SF_ERR_INVALID
+    assert create(idx, n_nodes=0) == sfgpu.SF_ERR_INVALID
+    assert create(idx, precisions=0) == sfgpu.SF_ERR_INVALID
+    bad = idx.copy()
+    bad[3] = 12
+    assert create(bad) == sfgpu.SF_ERR_INVALID
+    assert b"out of range" in L.sf_last_error()
+    bad = idx.copy()
+    bad[n3 + 5] = bad[n3 + 2]
+    assert create(bad) == sfgpu.SF_ERR_INVALID
+    assert b"same node twice" in L.sf_last_error()
+    assert not h.value
