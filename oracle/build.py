@@ -121,8 +121,9 @@ def build_ref() -> list[str]:
     outs = []
     # the DG headers put an OpenMP 'private' clause that the access macro of
     # ref_shim.h would rewrite, so they are built without OpenMP (serial)
-    # the cell Laplacian's mass-matrix and convection variants are the same
-    # adapter compiled with the reference's DO_MASS_MATRIX / DO_CONVECTION
+    # the cell Laplacian's mass-matrix, convection and face variants are the
+    # same adapter compiled with the reference's DO_MASS_MATRIX /
+    # DO_CONVECTION / DO_FACES
     for name, src, extra, omp, defs in [("ref_kernel", "ref_kernel", [REF_INC], False, []),
                                         ("ref_cell_gll", "ref_cell_gll", [REF_INC, REF_SRC], True, []),
                                         ("ref_cell_hermite", "ref_cell_hermite", [REF_INC], False, []),
@@ -130,6 +131,10 @@ def build_ref() -> list[str]:
                                          ["-DDO_MASS_MATRIX"]),
                                         ("ref_cell_convection", "ref_cell_hermite", [REF_INC], False,
                                          ["-DDO_CONVECTION"]),
+                                        ("ref_cell_faces", "ref_cell_hermite", [REF_INC], False,
+                                         ["-DDO_FACES"]),
+                                        ("ref_cell_faces_convection", "ref_cell_hermite", [REF_INC], False,
+                                         ["-DDO_FACES", "-DDO_CONVECTION"]),
                                         ("ref_dg", "ref_dg", [pdir, REF_INC], False, [])]:
         inc = ["-fopenmp"] if omp else []
         for d in extra:

@@ -67,6 +67,8 @@ def lib():
         L.sfo_cont_diagonal.argtypes = [C.POINTER(Mesh), _dp, C.c_void_p, _dp]
         L.sfo_cell_apply.argtypes = [C.POINTER(Shape), _dp, C.c_int, _dp, _dp]
         L.sfo_cell_op.argtypes = [C.POINTER(Shape), C.c_int, _dp, C.c_double, _dp, _dp, _dp]
+        L.sfo_cell_faces.argtypes = [C.POINTER(Shape), C.c_int, _dp, C.c_double, _dp, _dp, _dp]
+        L.sfo_cell_faces_apply.argtypes = [C.c_int, C.c_int, C.c_longlong, _dp, _dp, _dp, _dp]
         L.sfo_cont_apply_op.argtypes = [C.POINTER(Mesh), C.c_int, _dp, _dp, _dp]
         L.sfo_unstructured_apply.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_void_p,
                                              _dp, C.c_void_p, _dp, _dp]
@@ -190,6 +192,28 @@ def cell_op(degree, basis, kind, ij, jxw, b, x):
     lib().sfo_cell_op(C.byref(s), kind, np.ascontiguousarray(ij, dtype=np.float64), jxw,
                       np.ascontiguousarray(b, dtype=np.float64), np.ascontiguousarray(x, dtype=np.float64), out)
     return out
+
+
+def cell_faces(degree, conv, ij, jxw, b, x):
+    """the DO_FACES build of the Hermite-like cell operator: Cartesian
+    Laplacian (conv False) or convection form (conv True) of one cell plus the
+    face terms between its own faces at 0 and 1"""
+    s = shape(degree, BASIS_HERMITE)
+    out = np.zeros((degree + 1) ** 3)
+    lib().sfo_cell_faces(C.byref(s), int(bool(conv)), np.ascontiguousarray(ij, dtype=np.float64), jxw,
+                         np.ascontiguousarray(b, dtype=np.float64), np.ascontiguousarray(x, dtype=np.float64),
+                         out)
+    return out
+
+
+def cell_faces_apply(degree, conv, n_cells, h, x, b=(0.0, 0.0, 0.0)):
+    """cell_faces on every cell of a cell-major vector (n^3 entries per cell)
+    with cell size h"""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros_like(x)
+    lib().sfo_cell_faces_apply(degree, int(bool(conv)), int(n_cells), np.ascontiguousarray(h, dtype=np.float64),
+                               np.ascontiguousarray(b, dtype=np.float64), x, y)
+    return y
 
 
 def cont_apply_op(m: Mesh, kind, x, b=(0.0, 0.0, 0.0)):

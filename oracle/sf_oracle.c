@@ -550,8 +550,10 @@ SFO_INLINE void cell_integrate_n(int n, const sfo_shape *s, const double *tx, co
   sweep(n, 0, 0, 0, 0, s->S_eo, a, out);
 }
 
-/* geometry pointer Gcell has 6 blocks of geo_stride entries (0 => one
- * constant tensor for the whole cell, reference Cartesian form) */
+/* geometry pointer Gcell has 6 blocks of geo_stride entries, quadrature
+ * weight included; geo_stride 0: G holds the 6 entries of one constant
+ * tensor for the whole cell and the weight w_q is applied here, the
+ * reference's Cartesian form (evaluation_cell_laplacian.h:368-371,:395-411) */
 SFO_INLINE void cell_apply_n(int n, const sfo_shape *s, const double *G, int gs,
                              const double *kappa, const double *in, double *out)
 {
@@ -562,14 +564,15 @@ SFO_INLINE void cell_apply_n(int n, const sfo_shape *s, const double *G, int gs,
   for (int q = 0; q < nq; ++q) {
     const int o = gs ? q : 0;
     const double *g = G + o;
-    const int S6 = gs;
+    const int S6 = gs ? gs : 1;
+    const double wq = gs ? 1. : s->wq[q / (n * n)] * s->wq[(q / n) % n] * s->wq[q % n];
     const double k = kappa ? kappa[q] : 1.;
     const double t0 = gx[q] * g[0] + gy[q] * g[3 * S6] + gz[q] * g[4 * S6];
     const double t1 = gx[q] * g[3 * S6] + gy[q] * g[1 * S6] + gz[q] * g[5 * S6];
     const double t2 = gx[q] * g[4 * S6] + gy[q] * g[5 * S6] + gz[q] * g[2 * S6];
-    gx[q] = t0 * k;
-    gy[q] = t1 * k;
-    gz[q] = t2 * k;
+    gx[q] = t0 * wq * k;
+    gy[q] = t1 * wq * k;
+    gz[q] = t2 * wq * k;
   }
   cell_integrate_n(n, s, gx, gy, gz, out);
 }
@@ -633,6 +636,138 @@ void sfo_cell_op(const sfo_shape *s, int kind, const double *ij, double jxw,
                  const double *b, const double *in, double *out)
 {
   cell_op_n(s->n, s, kind, ij, jxw, b, in, out);
+}
+
+/* face values of one cell layer: F[i2 n + i1] <- S (along i1) then S (along
+ * i2) of the node layer, or the transposes (back to the nodes) */
+static void face_interp2(int n, const double *S, int transpose, const double *in, double *out)
+{
+  double t[SFO_MAX_N * SFO_MAX_N];
+  for (int i2 = 0; i2 < n; ++i2)
+    for (int a = 0; a < n; ++a) {
+      double v = 0.;
+      for (int i1 = 0; i1 < n; ++i1) v += (transpose ? S[i1 * n + a] : S[a * n + i1]) * in[i2 * n + i1];
+      t[i2 * n + a] = v;
+    }
+  for (int bq = 0; bq < n; ++bq)
+    for (int a = 0; a < n; ++a) {
+      double v = 0.;
+      for (int i2 = 0; i2 < n; ++i2) v += (transpose ? S[i2 * n + bq] : S[bq * n + i2]) * t[i2 * n + a];
+      out[bq * n + a] = v;
+    }
+}
+
+/* The face terms of the DO_FACES build of the cell Laplacian
+ * (evaluation_cell_laplacian.h:505-797, set-up :84-100): per direction f the
+ * cell's own faces at 1 ("right", node layer p) and at 0 ("left", layer 0)
+ * act as the two sides of one face, with no neighbour.  Face-local
+ * coordinates (i1, i2) run along directions f+1 and f+2 (mod 3).  The values
+ * and the Hermite-like normal derivatives hd (u_{p-1} - u_p), hd (u_1 - u_0)
+ * (hd = phi_0'(0)) are interpolated to the face Gauss points; with
+ * W = -w_q1 w_q2 / prod_{e != f} ij_e:
+ *  Laplacian (:688-708): a = (uR + uL) / 2, g = ij_f (nR + nL),
+ *    v = W (2 sigma a - g / 2), sigma = (p+1)^2 ij_f; the right face tests
+ *    with -v, the left with +v, and both normal-derivative slots with
+ *    d = W ij_f a, mapped back with the forward S (:756-759, as the
+ *    reference) and injected through the two end layers (:760-766);
+ *  convection (:558-567): flux = ((uR + uL) b_f + |b_f| (uR - uL)) / 2, the
+ *    right face tests with W flux, the left with -W flux.
+ * The reference also adds tangential-gradient terms with a zero normal
+ * Jacobian (normal_jac[f][0..1] = 0, :88-93): they are zero and left out. */
+static void cell_faces_term(const sfo_shape *s, int conv, const double *ij, const double *b,
+                            const double *in, double *out)
+{
+  const int n = s->n, p = n - 1, nf = n * n;
+  const int str[3] = {1, n, n * n};
+  const double hd = s->hermite_d0;
+  for (int f = 0; f < 3; ++f) {
+    const int o1 = str[f], s1 = str[(f + 1) % 3], s2 = str[(f + 2) % 3];
+    double fjxw = 1.;
+    for (int e = 0; e < 3; ++e)
+      if (e != f) fjxw /= ij[e];
+    double uR[SFO_MAX_N * SFO_MAX_N], uL[SFO_MAX_N * SFO_MAX_N], dR[SFO_MAX_N * SFO_MAX_N],
+        dL[SFO_MAX_N * SFO_MAX_N];
+    for (int i2 = 0; i2 < n; ++i2)
+      for (int i1 = 0; i1 < n; ++i1) {
+        const int k = i2 * n + i1, base = i2 * s2 + i1 * s1;
+        uR[k] = in[p * o1 + base];
+        uL[k] = in[base];
+        dR[k] = hd * (in[(p - 1) * o1 + base] - uR[k]);
+        dL[k] = hd * (in[o1 + base] - uL[k]);
+      }
+    face_interp2(n, s->S, 0, uR, uR);
+    face_interp2(n, s->S, 0, uL, uL);
+    face_interp2(n, s->S, 0, dR, dR);
+    face_interp2(n, s->S, 0, dL, dL);
+    double cR[SFO_MAX_N * SFO_MAX_N], cL[SFO_MAX_N * SFO_MAX_N], dv[SFO_MAX_N * SFO_MAX_N];
+    for (int q2 = 0; q2 < n; ++q2)
+      for (int q1 = 0; q1 < n; ++q1) {
+        const int q = q2 * n + q1;
+        const double W = -(s->wq[q2] * s->wq[q1]) * fjxw;
+        if (conv) {
+          const double flux = 0.5 * (b[f] * (uR[q] + uL[q]) + fabs(b[f]) * (uR[q] - uL[q]));
+          cR[q] = flux * W;
+          cL[q] = -(flux * W);
+          dv[q] = 0.;
+        } else {
+          const double sigma = (double)(n * n) * ij[f];
+          const double a = 0.5 * (uR[q] + uL[q]);
+          const double g = ij[f] * dR[q] + ij[f] * dL[q];
+          const double v = W * (a * 2. * sigma - g * 0.5);
+          cR[q] = -v;
+          cL[q] = v;
+          dv[q] = W * ij[f] * a;
+        }
+      }
+    face_interp2(n, s->S, 1, cR, cR);
+    face_interp2(n, s->S, 1, cL, cL);
+    if (!conv) face_interp2(n, s->S, 0, dv, dv);
+    for (int i2 = 0; i2 < n; ++i2)
+      for (int i1 = 0; i1 < n; ++i1) {
+        const int k = i2 * n + i1, base = i2 * s2 + i1 * s1;
+        if (conv) {
+          out[p * o1 + base] += cR[k];
+        } else {
+          out[p * o1 + base] += cR[k] - dv[k] * hd;
+          out[(p - 1) * o1 + base] += hd * dv[k];
+        }
+      }
+    for (int i2 = 0; i2 < n; ++i2)
+      for (int i1 = 0; i1 < n; ++i1) {
+        const int k = i2 * n + i1, base = i2 * s2 + i1 * s1;
+        if (conv) {
+          out[base] += cL[k];
+        } else {
+          out[base] += cL[k] - dv[k] * hd;
+          out[o1 + base] += hd * dv[k];
+        }
+      }
+    (void)nf;
+  }
+}
+
+void sfo_cell_faces(const sfo_shape *s, int conv, const double *ij, double jxw, const double *b,
+                    const double *in, double *out)
+{
+  if (conv) {
+    cell_op_n(s->n, s, 2, ij, jxw, b, in, out);
+  } else {
+    const double G[6] = {jxw * ij[0] * ij[0], jxw * ij[1] * ij[1], jxw * ij[2] * ij[2], 0., 0., 0.};
+    cell_apply_k(s, G, 0, NULL, in, out);
+  }
+  cell_faces_term(s, conv, ij, b, in, out);
+}
+
+void sfo_cell_faces_apply(int degree, int conv, long long n_cells, const double *h, const double *b,
+                          const double *x, double *y)
+{
+  sfo_shape s;
+  sfo_shape_init(degree, SFO_BASIS_HERMITE, &s);
+  const long long nq = (long long)s.n * s.n * s.n;
+  const double ij[3] = {1. / h[0], 1. / h[1], 1. / h[2]};
+  const double jxw = h[0] * h[1] * h[2];
+#pragma omp parallel for schedule(static)
+  for (long long e = 0; e < n_cells; ++e) sfo_cell_faces(&s, conv, ij, jxw, b, x + e * nq, y + e * nq);
 }
 
 /* ------------------------------------------------------------------------ */

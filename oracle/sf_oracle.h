@@ -103,6 +103,16 @@ void sfo_cell_apply(const sfo_shape *s, const double *Gcell, int geo_stride,
  * :328-354) */
 void sfo_cell_op(const sfo_shape *s, int kind, const double *ij, double jxw,
                  const double *b, const double *in, double *out);
+/* the DO_FACES build of the cell operator (evaluation_cell_laplacian.h:
+ * 505-797): the Cartesian Laplacian (conv = 0) or the convection form
+ * (conv = 1) of one cell plus face terms that couple the cell's faces at 0
+ * and 1 in each direction, Hermite-like basis */
+void sfo_cell_faces(const sfo_shape *s, int conv, const double *ij, double jxw, const double *b,
+                    const double *in, double *out);
+/* the same operator on every cell of a cell-major vector (n^3 entries per
+ * cell) with cell size h */
+void sfo_cell_faces_apply(int degree, int conv, long long n_cells, const double *h, const double *b,
+                          const double *x, double *y);
 /* y = A x on the affine continuous mesh (m->deform ignored) for those two
  * operators; Dirichlet rows as in sfo_cont_apply */
 void sfo_cont_apply_op(const sfo_mesh *m, int kind, const double *b,

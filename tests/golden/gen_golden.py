@@ -234,7 +234,10 @@ def cellop_fixtures():
     """the reference's DO_MASS_MATRIX and DO_CONVECTION builds of the
     Hermite-like cell operator (velocity (1, 2, 3)): single Cartesian cells
     with inverse Jacobian diag(4, 2, 4/3) and small affine boxes with
-    homogeneous Dirichlet conditions.  Degree 2 is stored too, but the
+    homogeneous Dirichlet conditions; the DO_FACES builds (Laplacian and
+    convection) on the same single cells (their face set-up takes the
+    reference's fixed Jacobian diag(4, 2, 4/3), evaluation_cell_laplacian.h:
+    46,84-100).  Degree 2 is stored too, but the
     reference's transposed values kernel drops the middle point for odd n
     (matrix_vector_kernel.h:130-131), which is wrong for the Hermite-like
     degree-2 basis (the reference's degree-2 mass matrix is not symmetric),
@@ -248,6 +251,8 @@ def cellop_fixtures():
         out["cell_x_%d" % p] = x
         out["cell_mass_%d" % p] = R.herm_cell(p, ij, jxw, x, "mass")
         out["cell_conv_%d" % p] = R.herm_cell(p, ij, jxw, x, "convection")
+        out["cell_faces_%d" % p] = R.herm_cell(p, ij, jxw, x, "faces")
+        out["cell_faces_conv_%d" % p] = R.herm_cell(p, ij, jxw, x, "faces_convection")
         nc = (3, 2, 2) if p <= 4 else (2, 2, 2)
         length = (1.0, 0.8, 1.2)
         _, _, N = cont_index_arrays(p, nc)

@@ -228,3 +228,75 @@ def test_continuous_mass_convection(golden, p):
     x = g["cont_x_%d" % p]
     assert rel(O.cont_apply_op(m, O.OP_MASS, x), g["cont_mass_%d" % p]) < 1e-13
     assert rel(O.cont_apply_op(m, O.OP_CONVECTION, x, (1, 2, 3)), g["cont_conv_%d" % p]) < 1e-13
+
+
+# the DO_FACES builds of the cell operator (Laplacian and convection form)
+# on one Cartesian cell; degree 2 again by a dense formulation
+@pytest.mark.parametrize("p", [1, 3, 4, 5, 6, 7, 8])
+def test_cell_faces(golden, p):
+    g = golden("cell_ops.npz")
+    jxw = 1.0 / np.prod(CELL_IJ)
+    x = g["cell_x_%d" % p]
+    assert rel(O.cell_faces(p, False, CELL_IJ, jxw, (0, 0, 0), x), g["cell_faces_%d" % p]) < 1e-13
+    assert rel(O.cell_faces(p, True, CELL_IJ, jxw, (1, 2, 3), x), g["cell_faces_conv_%d" % p]) < 1e-13
+
+
+def faces_dense(p, conv, ij, jxw, b):
+    """the DO_FACES cell operator as a dense matrix from the 1D tables: the
+    Kronecker cell term plus, per direction f, the face terms written with
+    layer-selection matrices and the face interpolation S x S"""
+    n = p + 1
+    a = O.shape_arrays(p, O.BASIS_HERMITE)
+    S, D, w, hd = a["S"], a["D"], a["wq"], a["hermite_d0"]
+    W = np.diag(w)
+    k = np.kron
+    M1, L1, C1 = S.T @ W @ S, (D @ S).T @ W @ (D @ S), (D @ S).T @ W @ S
+    if conv:
+        A = jxw * (ij[0] * b[0] * k(k(M1, M1), C1) + ij[1] * b[1] * k(k(M1, C1), M1)
+                   + ij[2] * b[2] * k(k(C1, M1), M1))
+    else:
+        A = jxw * (ij[0] ** 2 * k(k(M1, M1), L1) + ij[1] ** 2 * k(k(M1, L1), M1)
+                   + ij[2] ** 2 * k(k(L1, M1), M1))
+    F2 = k(S, S)
+    grid = np.arange(n ** 3).reshape(n, n, n)        # [z, y, x]
+    for f in range(3):
+        d1, d2 = (f + 1) % 3, (f + 2) % 3
+
+        def sel(layer):
+            R = np.zeros((n * n, n ** 3))
+            for i2 in range(n):
+                for i1 in range(n):
+                    c = [0, 0, 0]
+                    c[f], c[d1], c[d2] = layer, i1, i2
+                    R[i2 * n + i1, grid[c[2], c[1], c[0]]] = 1.0
+            return R
+        W2 = -np.diag(k(w, w)) * np.prod([1.0 / ij[e] for e in range(3) if e != f])
+        uR, uL = F2 @ sel(p), F2 @ sel(0)
+        if conv:
+            flux = 0.5 * (b[f] * (uR + uL) + abs(b[f]) * (uR - uL))
+            A += sel(p).T @ F2.T @ W2 @ flux - sel(0).T @ F2.T @ W2 @ flux
+        else:
+            nR, nL = F2 @ (hd * (sel(p - 1) - sel(p))), F2 @ (hd * (sel(1) - sel(0)))
+            avg = 0.5 * (uR + uL)
+            v = W2 @ (2 * n * n * ij[f] * avg - 0.5 * ij[f] * (nR + nL))
+            td = F2 @ (W2 @ (ij[f] * avg))            # forward S, as the reference
+            A += sel(p).T @ (F2.T @ -v - hd * td) + sel(p - 1).T @ (hd * td)
+            A += sel(0).T @ (F2.T @ v - hd * td) + sel(1).T @ (hd * td)
+    return A
+
+
+@pytest.mark.parametrize("p", [1, 2, 4])
+def test_cell_faces_dense(p):
+    jxw = 1.0 / np.prod(CELL_IJ)
+    b = np.array([0.7, -1.3, 0.4])
+    x = np.random.default_rng(p).uniform(-1, 1, (p + 1) ** 3)
+    for conv in (False, True):
+        ref = faces_dense(p, conv, CELL_IJ, jxw, b) @ x
+        assert rel(O.cell_faces(p, conv, CELL_IJ, jxw, b, x), ref) < 1e-14, conv
+    # the cell-major apply is the cell operator on every cell
+    h = 1.0 / CELL_IJ
+    X = np.random.default_rng(10 + p).uniform(-1, 1, 3 * (p + 1) ** 3)
+    Y = O.cell_faces_apply(p, True, 3, h, X, b)
+    n3 = (p + 1) ** 3
+    for e in range(3):
+        assert rel(Y[e * n3:(e + 1) * n3], O.cell_faces(p, True, CELL_IJ, jxw, b, X[e * n3:(e + 1) * n3])) < 1e-15
