@@ -75,9 +75,18 @@ typedef enum {
                           constant b = desc.velocity, affine meshes; the
                           DO_CONVECTION variant (evaluation_cell_laplacian.h:
                           328-354), there with b = (1, 2, 3)                 */
-  SF_OP_LAPLACE_UNSTRUCTURED = 6 /* continuous Laplacian on an unstructured
+  SF_OP_LAPLACE_UNSTRUCTURED = 6, /* continuous Laplacian on an unstructured
                           hexahedral mesh (sf_create_unstructured; the
                           reference has no mesh input at all)                */
+  SF_OP_LAPLACE_FACES = 7, /* the DO_FACES build of the cell Laplacian
+                          (evaluation_cell_laplacian.h:505-797): per
+                          Cartesian cell of a cell-major vector (n^3 entries
+                          per cell, Hermite-like basis), the cell Laplacian
+                          plus face terms between the cell's own faces at 0
+                          and 1; block diagonal, sf_vmult / sf_vmult_batched */
+  SF_OP_CONVECTION_FACES = 8 /* the DO_FACES + DO_CONVECTION build: the cell
+                          convection form (u, b . grad v), b = desc.velocity,
+                          plus upwind fluxes between the cell's own faces    */
 } sf_op_kind;
 
 typedef enum { SF_BASIS_GLL = 0, SF_BASIS_HERMITE = 1 } sf_basis;

@@ -146,7 +146,10 @@ public:
   // the reference's compile-time variants of this class, DO_MASS_MATRIX and
   // DO_CONVECTION (evaluation_cell_laplacian.h:22-24, :299-354): set to
   // SF_OP_MASS or SF_OP_CONVECTION before initialize() (affine meshes);
-  // the convection velocity defaults to the reference's b_d = d + 1
+  // the convection velocity defaults to the reference's b_d = d + 1.
+  // DO_FACES (:505-797): SF_OP_LAPLACE_FACES or SF_OP_CONVECTION_FACES, which
+  // act on a cell-major E-vector (n_cells (degree+1)^3 entries, Hermite-like
+  // basis) as the reference's class does
   int cell_operator = SF_OP_LAPLACE;
   double convection[3] = {1.0, 2.0, 3.0};
 

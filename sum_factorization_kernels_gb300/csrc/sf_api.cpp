@@ -63,6 +63,8 @@ int check_prec(const sf_op *op, int prec)
   return SF_OK;
 }
 
+bool is_cell_faces(int kind) { return kind == SF_OP_LAPLACE_FACES || kind == SF_OP_CONVECTION_FACES; }
+
 bool is_continuous(int kind)
 {
   return kind == SF_OP_LAPLACE || kind == SF_OP_MASS || kind == SF_OP_CONVECTION ||
@@ -143,10 +145,8 @@ int sf_create(const sf_desc *desc, sf_op **out)
   if (!desc || !out) return fail(SF_ERR_NULL, "desc/op is NULL");
   *out = nullptr;
   const sf_desc &d = *desc;
-  if (d.kind < SF_OP_LAPLACE || d.kind > SF_OP_CONVECTION) {
-    if (d.kind == SF_OP_LAPLACE_UNSTRUCTURED) return fail(SF_ERR_INVALID, "unstructured meshes: sf_create_unstructured");
-    return fail(SF_ERR_INVALID, "unknown operator kind");
-  }
+  if (d.kind < SF_OP_LAPLACE || d.kind > SF_OP_CONVECTION_FACES) return fail(SF_ERR_INVALID, "unknown operator kind");
+  if (d.kind == SF_OP_LAPLACE_UNSTRUCTURED) return fail(SF_ERR_INVALID, "unstructured meshes: sf_create_unstructured");
   const bool cont = is_continuous(d.kind);
   if (d.degree < 1 || d.degree > kMaxDegree) return fail(SF_ERR_UNSUPPORTED, "degree must be 1..8");
   for (int k = 0; k < 3; ++k) {
@@ -421,6 +421,7 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
   if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
   if (is_continuous(op->desc.kind)) return launch_cont_vmult(op, prec, x, y, st);
+  if (is_cell_faces(op->desc.kind)) return launch_cell_faces(op, prec, 1, x, y, st);
   if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
     return launch_dg_precomputed(op, prec, 1, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
   return launch_dg_vmult(op, prec, 1, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
@@ -429,7 +430,8 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
 int sf_vmult_transpose(sf_op *op, int prec, const void *x, void *y, void *stream)
 {
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
-  if (op->desc.kind == SF_OP_CONVECTION) return fail(SF_ERR_UNSUPPORTED, "no transpose of the convection form");
+  if (op->desc.kind == SF_OP_CONVECTION || is_cell_faces(op->desc.kind))
+    return fail(SF_ERR_UNSUPPORTED, "no transpose of the convection form or of the face-term operators");
   if (op->desc.kind != SF_OP_DG_ADVECT) return sf_vmult(op, prec, x, y, stream);
   return sf_vmult_transpose_batched(op, prec, 1, x, y, stream);
 }
@@ -450,6 +452,7 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
                                (char *)y + r * op->n_dofs * es, st));
     return SF_OK;
   }
+  if (is_cell_faces(op->desc.kind)) return launch_cell_faces(op, prec, nrhs, x, y, st);
   if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
     return launch_dg_precomputed(op, prec, nrhs, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
   return launch_dg_vmult(op, prec, nrhs, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
@@ -458,7 +461,8 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
 int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void *stream)
 {
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
-  if (op->desc.kind == SF_OP_CONVECTION) return fail(SF_ERR_UNSUPPORTED, "no transpose of the convection form");
+  if (op->desc.kind == SF_OP_CONVECTION || is_cell_faces(op->desc.kind))
+    return fail(SF_ERR_UNSUPPORTED, "no transpose of the convection form or of the face-term operators");
   if (op->desc.kind != SF_OP_DG_ADVECT) return sf_vmult_batched(op, prec, nrhs, x, y, stream);
   SF_RET(check_prec(op, prec));
   SF_RET(check_ptr(x, prec, "x"));
@@ -487,6 +491,8 @@ int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv, 
   SF_RET(check_ptr(x_new, prec, "x_new"));
   SF_RET(check_ptr(t, prec, "t"));
   if (x_old == x_new) return fail(SF_ERR_INVALID, "x_old and x_new must not alias");
+  if (is_cell_faces(op->desc.kind))
+    return fail(SF_ERR_UNSUPPORTED, "Chebyshev steps: not for the face-term operators");
   cudaStream_t st = (cudaStream_t)stream;
   if (op->desc.kind == SF_OP_DG_SIPG || op->desc.kind == SF_OP_DG_ADVECT)
     return launch_dg_vmult(op, prec, 1, false, x_old, x_new, b, diag_inv, t, c_np, c_tm, st);
@@ -562,7 +568,7 @@ int sf_diagonal(sf_op *op, int prec, void *diag, void *stream)
   SF_RET(check_prec(op, prec));
   SF_RET(check_ptr(diag, prec, "diag"));
   if (op->desc.kind == SF_OP_MASS || op->desc.kind == SF_OP_CONVECTION ||
-      op->desc.kind == SF_OP_LAPLACE_UNSTRUCTURED)
+      op->desc.kind == SF_OP_LAPLACE_UNSTRUCTURED || is_cell_faces(op->desc.kind))
     return fail(SF_ERR_UNSUPPORTED, "diagonal: structured Laplacian and DG operators only");
   if (op->desc.kind == SF_OP_LAPLACE) return launch_cont_diagonal(op, prec, diag, (cudaStream_t)stream);
   if (op->desc.kind == SF_OP_DG_PRECOMPUTED)

@@ -43,6 +43,9 @@ int launch_dg_precomputed(const sf_op *op, int prec, int nrhs, const void *x, vo
                           const void *cheb_dinv, void *cheb_t, double c_np, double c_tm, cudaStream_t st);
 int launch_dg_precomputed_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
 
+// sf_cell_faces.cu: the DO_FACES cell operators (block diagonal, cell-major)
+int launch_cell_faces(const sf_op *op, int prec, int nrhs, const void *x, void *y, cudaStream_t st);
+
 // blocks of a kernel that fit on one SM with the maximum shared-memory
 // carveout: the occupancy calculator does not account for the carveout
 // preference, so persistent grids size themselves from the limits directly

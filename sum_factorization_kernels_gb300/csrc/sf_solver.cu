@@ -553,8 +553,9 @@ extern "C" int sf_cg_solve(sf_op *op, const double *b, double *x, const sf_solve
     set_error("invalid solver options");
     return SF_ERR_INVALID;
   }
-  if (op->desc.kind == SF_OP_DG_ADVECT || op->desc.kind == SF_OP_CONVECTION) {
-    set_error("CG needs a symmetric operator; advection and convection are not");
+  if (op->desc.kind == SF_OP_DG_ADVECT || op->desc.kind == SF_OP_CONVECTION ||
+      op->desc.kind == SF_OP_LAPLACE_FACES || op->desc.kind == SF_OP_CONVECTION_FACES) {
+    set_error("CG needs a symmetric operator; advection, convection and the face-term operators are not");
     return SF_ERR_STATE;
   }
   if (!(op->desc.precisions & 1) || (o.mode == SF_SOLVE_MIXED && !(op->desc.precisions & 2))) {

@@ -22,6 +22,7 @@ STATUS = {0: "SF_OK", -1: "SF_ERR_INVALID", -2: "SF_ERR_NULL", -3: "SF_ERR_UNSUP
 FP64, FP32 = 0, 1
 OP_LAPLACE, OP_DG_SIPG, OP_DG_ADVECT, OP_DG_PRECOMPUTED, OP_MASS, OP_CONVECTION = 0, 1, 2, 3, 4, 5
 OP_LAPLACE_UNSTRUCTURED = 6
+OP_LAPLACE_FACES, OP_CONVECTION_FACES = 7, 8   # DO_FACES builds, cell-major vectors
 BASIS_GLL, BASIS_HERMITE = 0, 1
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2
