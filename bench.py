@@ -392,6 +392,16 @@ def secondary_configs(stream, peak):
         t = time_apply(op, x, y, 30, 5, stream)
         res[name] = {"gdofs": round(op.n_dofs / t / 1e9, 3), "hbm_frac": round(8 * op.n_dofs / t / 1e9 / peak, 4)}
         del op, x, y
+    # the DO_FACES builds on the cell-major vector of the same 64^3 cells
+    # (n^3 entries per cell; 2 s C n^3 algorithmic bytes)
+    for name, kind in (("laplace_faces", sfgpu.OP_LAPLACE_FACES), ("convection_faces", sfgpu.OP_CONVECTION_FACES)):
+        op = sfgpu.Operator(kind, degree=4, n_cells=(64, 64, 64), velocity=(1.0, 2.0, 3.0))
+        x = torch.rand(op.n_dofs, device="cuda", dtype=torch.float32) * 2 - 1
+        y = torch.empty_like(x)
+        t = time_apply(op, x, y, 30, 5, stream)
+        res[name] = {"gdofs": round(op.n_dofs / t / 1e9, 3), "hbm_frac": round(8 * op.n_dofs / t / 1e9 / peak, 4),
+                     "n_dofs": op.n_dofs}
+        del op, x, y
     out["cell_variants_p4_64c_affine_fp32"] = res
     # ---- unstructured hexahedral input: the 48^3 p=4 box given as cell-node
     # index arrays (lexicographic numbering) and per-cell merged geometry

@@ -24,7 +24,8 @@
 // GPU mapping as the DG kernels: CPB consecutive cells per block, n^2
 // threads per cell, z columns read and written straight from the vector.
 // Per cell: the input slab X (kept for the face terms), three work slabs
-// and four face arrays in shared memory.  Thread (a, b) owns the z column
+// and four face arrays in shared memory, laid out per degree and precision
+// by faces_layout.  Thread (a, b) owns the z column
 // (x, y) = (a, b), the x line (y, z) = (a, b) and the y line (x, z) = (a, b)
 // in the cell term, and face point (q1, q2) = (a, b) in the face terms.
 #include "sf_launch.h"
@@ -33,14 +34,64 @@
 namespace sf {
 namespace {
 
+// Shared-memory layout per cell: four slabs (X, Sa, Sb, Sc) RS words apart
+// with entry (x, y, z) at SX x + SY y + SZ z, four face arrays FA words apart
+// with entry (i2, i1) at FN i2 + i1, and a cell stride of CW words.
+struct FacesLayout {
+  int SX, SY, SZ, RS, FN, FA, CW;
+};
+
+// Layouts from a shared-memory bank model of every access of the kernel
+// (the cell term's z, x and y line patterns on the four slabs, the face
+// phases' layer reads, row and column passes and injections): stride
+// permutations of (1, P1, P2), slab size, face-array strides and the cell
+// stride searched with the per-cell words held at most 8 above those of the
+// padded layout (strides (1, n + 1, n (n + 1) + 1), dense face arrays), so
+// that residency does not drop.  Modelled wavefronts per cell
+// (Laplacian, FP32) against the padded layout: n=2 31/56, 3 125/268,
+// 4 198/348, 5 382/513, 6 619/805, 7 832/1045, 8 1008/2208, 9 1478/1919;
+// ncu counts 532 per cell for the padded layout at n=5 (model 513).
+constexpr FacesLayout faces_layout(int n, int elem)
+{
+  return elem == 4 ? (n == 2   ? FacesLayout{5, 2, 1, 9, 3, 6, 60}
+                      : n == 3 ? FacesLayout{3, 1, 10, 29, 6, 21, 200}
+                      : n == 4 ? FacesLayout{19, 4, 1, 76, 5, 24, 400}
+                      : n == 5 ? FacesLayout{5, 25, 1, 130, 5, 25, 637}
+                      : n == 6 ? FacesLayout{1, 6, 39, 237, 7, 44, 1124}
+                      : n == 7 ? FacesLayout{1, 7, 52, 361, 7, 56, 1681}
+                      : n == 8 ? FacesLayout{67, 1, 8, 533, 9, 72, 2420}
+                               : FacesLayout{1, 9, 81, 731, 9, 81, 3249})
+                   : (n == 2   ? FacesLayout{5, 2, 1, 9, 3, 6, 60}
+                      : n == 3 ? FacesLayout{5, 1, 13, 40, 3, 9, 196}
+                      : n == 4 ? FacesLayout{19, 4, 1, 73, 5, 20, 372}
+                      : n == 5 ? FacesLayout{1, 5, 25, 126, 5, 25, 617}
+                      : n == 6 ? FacesLayout{41, 1, 6, 241, 6, 40, 1124}
+                      : n == 7 ? FacesLayout{1, 7, 49, 343, 7, 56, 1601}
+                      : n == 8 ? FacesLayout{66, 1, 8, 526, 9, 72, 2392}
+                               : FacesLayout{1, 9, 81, 729, 9, 89, 3281});
+}
+
+// every slab entry on its own word inside RS, everything inside CW
+constexpr bool faces_layout_fits(int n, FacesLayout L)
+{
+  bool seen[4096] = {};
+  if (L.RS > 4096 || L.FN < n || L.FA < n * L.FN || L.CW < 4 * L.RS + 4 * L.FA) return false;
+  for (int z = 0; z < n; ++z)
+    for (int y = 0; y < n; ++y)
+      for (int x = 0; x < n; ++x) {
+        const int i = L.SX * x + L.SY * y + L.SZ * z;
+        if (i < 0 || i >= L.RS || seen[i]) return false;
+        seen[i] = true;
+      }
+  return true;
+}
+
 template <int N, typename T>
 struct FacesCfg {
   static constexpr int CPB = CellsPerBlock<N>::value;
-  static constexpr int SY = N + 1, SZ = N * (N + 1) + 1; // padded slab strides (SX = 1)
-  static constexpr int RS = N * SZ;                      // words per slab
-  static constexpr int FA = N * N;                       // words per face array
-  static constexpr int CELL_WORDS = 4 * RS + 4 * FA;
-  static constexpr size_t SMEM = (size_t)CPB * CELL_WORDS * sizeof(T);
+  static constexpr FacesLayout L = faces_layout(N, (int)sizeof(T));
+  static constexpr size_t SMEM = (size_t)CPB * L.CW * sizeof(T);
+  static_assert(faces_layout_fits(N, L), "face-operator layout overlaps");
 };
 
 template <int N, typename T>
@@ -65,17 +116,19 @@ __global__ void __launch_bounds__(FacesCfg<N, T>::CPB * N * N)
 {
   using Cfg = FacesCfg<N, T>;
   constexpr int N2 = N * N, N3 = N2 * N, P = N - 1;
-  constexpr int SY = Cfg::SY, SZ = Cfg::SZ;
+  constexpr int SX = Cfg::L.SX, SY = Cfg::L.SY, SZ = Cfg::L.SZ, FN = Cfg::L.FN, FA = Cfg::L.FA;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int k = threadIdx.x / N2, l = threadIdx.x % N2;
   const int a = l % N, b = l / N;
-  T *X = reinterpret_cast<T *>(smem_raw) + k * Cfg::CELL_WORDS;
-  T *Sa = X + Cfg::RS, *Sb = Sa + Cfg::RS, *Sc = Sb + Cfg::RS;
-  T *F = Sc + Cfg::RS;
+  T *X = reinterpret_cast<T *>(smem_raw) + k * Cfg::L.CW;
+  T *Sa = X + Cfg::L.RS, *Sb = Sa + Cfg::L.RS, *Sc = Sb + Cfg::L.RS;
+  T *F = Sc + Cfg::L.RS;
   const long long cell = (long long)blockIdx.x * Cfg::CPB + k;
   const bool valid = cell < A.n_cells;
   const long long base = ((long long)blockIdx.y * A.n_cells + (valid ? cell : 0)) * N3;
-  const int zc = a + SY * b, xl = SY * a + SZ * b, yl = a + SZ * b;
+  // line bases: z column (x, y) = (a, b), x line (y, z) = (a, b), y line (x, z) = (a, b)
+  const int zc = SX * a + SY * b, xl = SY * a + SZ * b, yl = SX * a + SZ * b;
+  const int fq = FN * b + a; // face point (q1, q2) = (a, b)
   T v[N], g[N];
 
   // ---- input z column; S_z ----
@@ -89,10 +142,10 @@ __global__ void __launch_bounds__(FacesCfg<N, T>::CPB * N * N)
   __syncthreads();
   // ---- S_x ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = Sa[xl + m];
+  for (int m = 0; m < N; ++m) v[m] = Sa[xl + SX * m];
   eo_apply<N, 1>(A.S, v, v);
 #pragma unroll
-  for (int m = 0; m < N; ++m) Sa[xl + m] = v[m];
+  for (int m = 0; m < N; ++m) Sa[xl + SX * m] = v[m];
   __syncthreads();
   T *Y;
   if constexpr (!CONV) {
@@ -109,10 +162,10 @@ __global__ void __launch_bounds__(FacesCfg<N, T>::CPB * N * N)
     __syncthreads();
     // ---- D_x into Sb; D_z in registers ----
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = Sa[xl + m];
+    for (int m = 0; m < N; ++m) v[m] = Sa[xl + SX * m];
     eo_apply<N, -1>(A.D, v, g);
 #pragma unroll
-    for (int m = 0; m < N; ++m) Sb[xl + m] = g[m];
+    for (int m = 0; m < N; ++m) Sb[xl + SX * m] = g[m];
     T gz[N];
 #pragma unroll
     for (int c = 0; c < N; ++c) v[c] = Sa[zc + SZ * c];
@@ -134,10 +187,10 @@ __global__ void __launch_bounds__(FacesCfg<N, T>::CPB * N * N)
     __syncthreads();
     // ---- + D_x^T ----
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = Sb[xl + m];
+    for (int m = 0; m < N; ++m) v[m] = Sb[xl + SX * m];
     eo_apply<N, -1>(A.DT, v, g);
 #pragma unroll
-    for (int m = 0; m < N; ++m) Sa[xl + m] += g[m];
+    for (int m = 0; m < N; ++m) Sa[xl + SX * m] += g[m];
     __syncthreads();
     // ---- + D_y^T, S_y^T ----
 #pragma unroll
@@ -151,10 +204,10 @@ __global__ void __launch_bounds__(FacesCfg<N, T>::CPB * N * N)
     __syncthreads();
     // ---- S_x^T ----
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = Sa[xl + m];
+    for (int m = 0; m < N; ++m) v[m] = Sa[xl + SX * m];
     eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-    for (int m = 0; m < N; ++m) Sa[xl + m] = v[m];
+    for (int m = 0; m < N; ++m) Sa[xl + SX * m] = v[m];
     __syncthreads();
     // ---- S_z^T ----
 #pragma unroll
@@ -180,10 +233,10 @@ __global__ void __launch_bounds__(FacesCfg<N, T>::CPB * N * N)
     __syncthreads();
     // ---- + b_x / h_x D_x^T r ----
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = Sa[xl + m];
+    for (int m = 0; m < N; ++m) v[m] = Sa[xl + SX * m];
     eo_apply<N, -1>(A.DT, v, g);
 #pragma unroll
-    for (int m = 0; m < N; ++m) Sc[xl + m] = fma(A.c[0], g[m], Sc[xl + m]);
+    for (int m = 0; m < N; ++m) Sc[xl + SX * m] = fma(A.c[0], g[m], Sc[xl + SX * m]);
     __syncthreads();
     // ---- + b_z / h_z D_z^T r, S_z^T ----
 #pragma unroll
@@ -204,10 +257,10 @@ __global__ void __launch_bounds__(FacesCfg<N, T>::CPB * N * N)
     __syncthreads();
     // ---- S_x^T ----
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = Sc[xl + m];
+    for (int m = 0; m < N; ++m) v[m] = Sc[xl + SX * m];
     eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-    for (int m = 0; m < N; ++m) Sc[xl + m] = v[m];
+    for (int m = 0; m < N; ++m) Sc[xl + SX * m] = v[m];
     Y = Sc;
   }
   __syncthreads();
@@ -219,9 +272,9 @@ __global__ void __launch_bounds__(FacesCfg<N, T>::CPB * N * N)
   constexpr int NB = CONV ? 2 : 3; // face arrays mapped back
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
-    const int so = f == 0 ? 1 : f == 1 ? SY : SZ;  // stride along f
-    const int s1 = f == 0 ? SY : f == 1 ? SZ : 1;  // along f+1 (i1)
-    const int s2 = f == 0 ? SZ : f == 1 ? 1 : SY;  // along f+2 (i2)
+    const int so = f == 0 ? SX : f == 1 ? SY : SZ; // stride along f
+    const int s1 = f == 0 ? SY : f == 1 ? SZ : SX; // along f+1 (i1)
+    const int s2 = f == 0 ? SZ : f == 1 ? SX : SY; // along f+2 (i2)
     // interpolate the node layers: along i1, then along i2
     for (int t = l; t < NL * N; t += N2) {
       const int kk = t / N, i2 = t % N;
@@ -230,35 +283,35 @@ __global__ void __launch_bounds__(FacesCfg<N, T>::CPB * N * N)
       for (int j = 0; j < N; ++j) v[j] = X[layer * so + i2 * s2 + j * s1];
       eo_apply<N, 1>(A.S, v, v);
 #pragma unroll
-      for (int j = 0; j < N; ++j) F[kk * N2 + i2 * N + j] = v[j];
+      for (int j = 0; j < N; ++j) F[kk * FA + i2 * FN + j] = v[j];
     }
     __syncthreads();
     for (int t = l; t < NL * N; t += N2) {
       const int kk = t / N, q1 = t % N;
 #pragma unroll
-      for (int j = 0; j < N; ++j) v[j] = F[kk * N2 + j * N + q1];
+      for (int j = 0; j < N; ++j) v[j] = F[kk * FA + j * FN + q1];
       eo_apply<N, 1>(A.S, v, v);
 #pragma unroll
-      for (int j = 0; j < N; ++j) F[kk * N2 + j * N + q1] = v[j];
+      for (int j = 0; j < N; ++j) F[kk * FA + j * FN + q1] = v[j];
     }
     __syncthreads();
     // face quadrature point (q1, q2) = (a, b)
     {
       const T W = A.fw[f] * (A.w[b] * A.w[a]);
-      const T uR = F[l], uL = F[N2 + l];
+      const T uR = F[fq], uL = F[FA + fq];
       if constexpr (CONV) {
         const T bn = A.bn[f];
         const T flux = T(0.5) * (bn * (uR + uL) + fabs(bn) * (uR - uL));
-        F[l] = flux * W;
-        F[N2 + l] = -(flux * W);
+        F[fq] = flux * W;
+        F[FA + fq] = -(flux * W);
       } else {
-        const T nR = A.hd * (F[2 * N2 + l] - uR), nL = A.hd * (F[3 * N2 + l] - uL);
+        const T nR = A.hd * (F[2 * FA + fq] - uR), nL = A.hd * (F[3 * FA + fq] - uL);
         const T avg = T(0.5) * (uR + uL);
         const T gs = A.ij[f] * nR + A.ij[f] * nL;
         const T vv = W * (avg * T(2) * A.sigma[f] - gs * T(0.5));
-        F[l] = -vv;
-        F[N2 + l] = vv;
-        F[2 * N2 + l] = W * A.ij[f] * avg;
+        F[fq] = -vv;
+        F[FA + fq] = vv;
+        F[2 * FA + fq] = W * A.ij[f] * avg;
       }
     }
     __syncthreads();
@@ -266,34 +319,34 @@ __global__ void __launch_bounds__(FacesCfg<N, T>::CPB * N * N)
     for (int t = l; t < NB * N; t += N2) {
       const int kk = t / N, r = t % N;
 #pragma unroll
-      for (int j = 0; j < N; ++j) v[j] = F[kk * N2 + r * N + j];
+      for (int j = 0; j < N; ++j) v[j] = F[kk * FA + r * FN + j];
       if (kk == 2) eo_apply<N, 1>(A.S, v, v);
       else eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-      for (int j = 0; j < N; ++j) F[kk * N2 + r * N + j] = v[j];
+      for (int j = 0; j < N; ++j) F[kk * FA + r * FN + j] = v[j];
     }
     __syncthreads();
     for (int t = l; t < NB * N; t += N2) {
       const int kk = t / N, q1 = t % N;
 #pragma unroll
-      for (int j = 0; j < N; ++j) v[j] = F[kk * N2 + j * N + q1];
+      for (int j = 0; j < N; ++j) v[j] = F[kk * FA + j * FN + q1];
       if (kk == 2) eo_apply<N, 1>(A.S, v, v);
       else eo_apply<N, 1>(A.ST, v, v);
 #pragma unroll
-      for (int j = 0; j < N; ++j) F[kk * N2 + j * N + q1] = v[j];
+      for (int j = 0; j < N; ++j) F[kk * FA + j * FN + q1] = v[j];
     }
     __syncthreads();
     // inject: one thread per face node, right face first, then left
     {
       const int off = b * s2 + a * s1;
       if constexpr (CONV) {
-        Y[P * so + off] += F[l];
-        Y[off] += F[N2 + l];
+        Y[P * so + off] += F[fq];
+        Y[off] += F[FA + fq];
       } else {
-        const T td = F[2 * N2 + l];
-        Y[P * so + off] += F[l] - td * A.hd;
+        const T td = F[2 * FA + fq];
+        Y[P * so + off] += F[fq] - td * A.hd;
         Y[(P - 1) * so + off] += A.hd * td;
-        Y[off] += F[N2 + l] - td * A.hd;
+        Y[off] += F[FA + fq] - td * A.hd;
         Y[so + off] += A.hd * td;
       }
     }

@@ -4,8 +4,9 @@ device memory): ``python -m sum_factorization_kernels_gb300.timing KIND ...``.
 KIND is ``laplace`` (continuous, deformed mesh), ``sipg`` (DG SIPG),
 ``advect`` (DG upwind advection with inverse mass), ``precomputed`` (DG
 SIPG in tensor-product form with precomputed 1D matrices), ``mass`` /
-``convection`` (continuous, affine) or ``unstructured`` (the affine box given
-as cell-node index arrays and per-cell geometry).  Prints one line with the
+``convection`` (continuous, affine), ``unstructured`` (the affine box given
+as cell-node index arrays and per-cell geometry) or ``faces`` /
+``convection_faces`` (the DO_FACES cell operators on cell-major vectors).  Prints one line with the
 apply rate summed over the right-hand sides and the vector traffic it implies.
 Used to drive profiler captures of one kernel on a small case.
 """
@@ -54,13 +55,17 @@ def make_operator(kind: str, degree: int, ncells: int):
         return sf.Operator(sf.OP_DG_ADVECT, degree=degree, n_cells=n, velocity=(1.0, 0.5, 0.25), inverse_mass=1)
     if kind == "precomputed":
         return sf.Operator(sf.OP_DG_PRECOMPUTED, degree=degree, n_cells=n)
+    if kind == "faces":
+        return sf.Operator(sf.OP_LAPLACE_FACES, degree=degree, n_cells=n)
+    if kind == "convection_faces":
+        return sf.Operator(sf.OP_CONVECTION_FACES, degree=degree, n_cells=n, velocity=(1.0, 2.0, 3.0))
     raise ValueError("unknown operator kind %r" % kind)
 
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("kind", choices=["laplace", "sipg", "advect", "precomputed", "mass", "convection",
-                                     "unstructured"])
+                                     "unstructured", "faces", "convection_faces"])
     ap.add_argument("--degree", type=int, default=4)
     ap.add_argument("--ncells", type=int, default=32, help="cells per direction")
     ap.add_argument("--prec", choices=["fp32", "fp64"], default="fp32")
