@@ -67,6 +67,28 @@ int main()
                 kind == SF_OP_MASS ? "DO_MASS_MATRIX" : "DO_CONVECTION", e);
     fails += !(e < 1e-12);
   }
+  // the DO_FACES variants (cell-major E-vector), p = 4
+  for (int kind : {SF_OP_LAPLACE_FACES, SF_OP_CONVECTION_FACES}) {
+    const unsigned nc[3] = {3, 2, 2};
+    const double L[3] = {0.75, 1.0, 1.5};
+    sfgpu::EvaluationCellLaplacian<4, float> ev;
+    ev.cell_operator = kind;
+    ev.initialize(nc, L);
+    std::vector<double> x(ev.n_dofs()), yr(ev.n_dofs());
+    std::vector<float> xf(x.size());
+    for (size_t i = 0; i < x.size(); ++i) xf[i] = (float)(x[i] = U(gen));
+    ev.input_array.upload(xf);
+    ev.matrix_vector_product();
+    cudaDeviceSynchronize();
+    const std::vector<float> yf = ev.output_array.download();
+    const std::vector<double> y(yf.begin(), yf.end());
+    const double h[3] = {0.25, 0.5, 0.75}, b[3] = {1.0, 2.0, 3.0};
+    sfo_cell_faces_apply(4, kind == SF_OP_CONVECTION_FACES, 12, h, b, x.data(), yr.data());
+    const double e = rel(y, yr);
+    std::printf("EvaluationCellLaplacian<4,float> (%s) rel err %.3e\n",
+                kind == SF_OP_LAPLACE_FACES ? "DO_FACES" : "DO_FACES + DO_CONVECTION", e);
+    fails += !(e < 6e-6);
+  }
   // DG SIPG, p = 5: do_matvec, do_chebyshev, emulate_cheby_vector_updates
   {
     const unsigned nc[3] = {4, 3, 3};
