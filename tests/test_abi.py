@@ -124,3 +124,26 @@ def test_unstructured_validation_without_gpu():
     assert create(bad) == sfgpu.SF_ERR_INVALID
     assert b"same node twice" in L.sf_last_error()
     assert not h.value
+
+
+def test_operator_kinds_without_gpu():
+    """kinds past the enum and the unstructured kind are refused by sf_create
+    before any device work; the face-term kinds pass the kind check and reach
+    the degree check"""
+    sfgpu, L = _lib()
+    h = C.c_void_p()
+    d = sfgpu.Desc()
+    d.degree, d.precisions = 3, 3
+    for k in range(3):
+        d.n_cells[k], d.length[k] = 2, 1.0
+    for kind in (-1, 9, 100):
+        d.kind = kind
+        assert L.sf_create(C.byref(d), C.byref(h)) == sfgpu.SF_ERR_INVALID, kind
+    d.kind = sfgpu.OP_LAPLACE_UNSTRUCTURED
+    assert L.sf_create(C.byref(d), C.byref(h)) == sfgpu.SF_ERR_INVALID
+    assert b"sf_create_unstructured" in L.sf_last_error()
+    d.degree = 9
+    for kind in (sfgpu.OP_LAPLACE_FACES, sfgpu.OP_CONVECTION_FACES):
+        d.kind = kind
+        assert L.sf_create(C.byref(d), C.byref(h)) == sfgpu.SF_ERR_UNSUPPORTED, kind
+    assert not h.value
