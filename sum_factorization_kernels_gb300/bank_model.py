@@ -1,6 +1,7 @@
 """Shared-memory bank model of the sweep kernels and the layout search behind
 their slab tables (``pack_params`` in ``csrc/sf_laplace_line.cu``,
-``dg_slabs`` and ``dg_inv_layout`` in ``csrc/sf_dg.cu``).
+``dg_slabs`` and ``dg_inv_layout`` in ``csrc/sf_dg.cu``, ``faces_layout`` in
+``csrc/sf_cell_faces.cu``).
 
 Model: shared memory has 32 banks of 4 bytes.  One warp-wide access takes as
 many wavefronts as the largest number of distinct 4-byte words that its
@@ -153,4 +154,109 @@ def pack_params_from_source(path=None):
             vals = _ints(m.group(2))
             n = int(m.group(1)) if m.group(1) else 9
             out[(elem, n)] = tuple(vals[:7]) + (tuple(vals[7:11]), tuple(vals[11:15]), tuple(vals[15:19]))
+    return out
+
+
+# ---- the DO_FACES kernel (csrc/sf_cell_faces.cu) ----
+# cells per block (n^2 threads per cell, cell-major lanes)
+FACES_CPB = {2: 32, 3: 14, 4: 8, 5: 5, 6: 7, 7: 5, 8: 2, 9: 3}
+
+
+def faces_padded(n):
+    """the padded layout (SX, SY, SZ, RS, FN, FA, CW): strides (1, n + 1,
+    n (n + 1) + 1), dense face arrays"""
+    sz = n * (n + 1) + 1
+    return (1, n + 1, sz, n * sz, n, n * n, 4 * n * sz + 4 * n * n)
+
+
+def faces_cost(n, elem, layout, conv=False):
+    """wavefronts per cell of every shared access of cell_faces_kernel with
+    the layout (SX, SY, SZ, RS, FN, FA, CW): the cell term's z, x and y line
+    patterns on the slabs X, Sa, Sb, Sc, and per face direction the layer
+    reads and row / column passes over the face arrays, the point phase, the
+    injections into the output slab and the final column read.  Lanes without
+    work in a pass repeat an active lane of their warp."""
+    sx, sy, sz, rs, fn, fa, cw = layout
+    cpb = FACES_CPB[n]
+    nt = cpb * n * n
+    warps = (nt + 31) // 32
+    t = np.arange(32 * warps)
+    act = t < nt
+    tt = np.minimum(t, nt - 1)
+    k, l = tt // (n * n), tt % (n * n)
+    a, b = l % n, l // n
+    base = k * cw
+    X, Sa, Sb, Sc, Fb = 0, rs, 2 * rs, 3 * rs, 4 * rs
+    acc = []
+
+    def add(addr, mask=None, count=1):
+        m = act if mask is None else (act & mask)
+        acc.extend([(addr, m)] * count)
+
+    line = {"z": lambda m: sx * a + sy * b + sz * m, "x": lambda m: sx * m + sy * a + sz * b,
+            "y": lambda m: sx * a + sy * m + sz * b}
+    if conv:
+        ops = [(X, "z", 1), (Sa, "z", 1), (Sa, "x", 2), (Sa, "y", 2), (Sc, "y", 1), (Sa, "x", 1), (Sc, "x", 2),
+               (Sa, "z", 1), (Sc, "z", 2), (Sc, "y", 2), (Sc, "x", 2), (Sc, "z", 1)]
+    else:
+        ops = [(X, "z", 1), (Sa, "z", 1), (Sa, "x", 2), (Sa, "y", 2), (Sc, "y", 1), (Sa, "x", 1), (Sb, "x", 1),
+               (Sa, "z", 1), (Sb, "z", 2), (Sc, "z", 2), (Sa, "z", 1), (Sb, "x", 1), (Sa, "x", 2), (Sc, "y", 1),
+               (Sa, "y", 2), (Sa, "x", 2), (Sa, "z", 2), (Sa, "z", 1)]
+    for off, pat, cnt in ops:
+        for m in range(n):
+            add(base + off + line[pat](m), count=cnt)
+    nl, nb = (2, 2) if conv else (4, 3)
+    st = (sx, sy, sz)
+    for f in range(3):
+        so, s1, s2 = st[f], st[(f + 1) % 3], st[(f + 2) % 3]
+        for ntask, kind in ((nl, "layers"), (nl, "cols"), (nb, "rows"), (nb, "cols")):
+            for rep in range((ntask * n + n * n - 1) // (n * n)):
+                task = l + rep * n * n
+                busy = task < ntask * n
+                kk, r = np.minimum(task, ntask * n - 1) // n, np.minimum(task, ntask * n - 1) % n
+                layer = np.choose(np.minimum(kk, 3), [n - 1, 0, max(n - 2, 0), 1])
+                for j in range(n):
+                    if kind == "layers":
+                        add(base + X + layer * so + r * s2 + j * s1, busy)
+                        add(base + Fb + kk * fa + r * fn + j, busy)
+                    elif kind == "cols":
+                        add(base + Fb + kk * fa + j * fn + r, busy, 2)
+                    else:
+                        add(base + Fb + kk * fa + r * fn + j, busy, 2)
+        q = b * fn + a
+        add(base + Fb + q, count=2)
+        add(base + Fb + fa + q, count=2)
+        if not conv:
+            add(base + Fb + 2 * fa + q, count=3)
+            add(base + Fb + 3 * fa + q)
+        y_slab = Sc if conv else Sa
+        for layer in ([n - 1, 0] if conv else [n - 1, n - 2, 0, 1]):
+            add(base + y_slab + layer * so + b * s2 + a * s1, count=2)
+    y_slab = Sc if conv else Sa
+    for m in range(n):
+        add(base + y_slab + line["z"](m))
+    rows = []
+    for addr, m in acc:
+        A, M = addr.reshape(warps, 32).copy(), m.reshape(warps, 32)
+        for w in range(warps):
+            if M[w].any():
+                row = A[w]
+                row[~M[w]] = row[M[w]][0]
+                rows.append(row)
+    return wavefronts(np.array(rows), elem) / cpb
+
+
+def faces_layout_from_source(path=None):
+    """{(elem, n): (SX, SY, SZ, RS, FN, FA, CW)} parsed from faces_layout in
+    sf_cell_faces.cu"""
+    src = open(path or os.path.join(CSRC, "sf_cell_faces.cu")).read()
+    body = src[src.index("constexpr FacesLayout faces_layout"):]
+    body = body[:body.index("\n}\n")]
+    f32, f64 = re.split(r"\n\s*: \(n == 2", body, maxsplit=1)
+    f64 = "n == 2" + f64
+    out = {}
+    for elem, part in ((4, f32), (8, f64)):
+        for m in re.finditer(r"(?:n == (\d)\s*\?\s*)?FacesLayout\{([^}]*)\}", part):
+            n = int(m.group(1)) if m.group(1) else 9
+            out[(elem, n)] = tuple(_ints(m.group(2)))
     return out

@@ -66,3 +66,25 @@ def test_tables_no_worse_than_padded_layout():
     lanes = B.lane_map(5, 4, 5, False)
     old5 = B.slab_cost(5, 4, lanes, (1, 5, 25, 253), (6, 9, 4)) + B.slab_cost(5, 4, lanes, (1, 5, 37, 185), (2, 0, 2))
     assert (B.line_cost(5, 4, t[(4, 5)]), old5, B.ideal(5, 4, 4, 23)) == (540, 660, 460)
+
+
+def test_faces_layouts():
+    """the DO_FACES kernel's layout table (parsed from the CUDA source): every
+    entry fits, costs no more than the padded layout in both variants and
+    holds the per-cell words within 8 of it; the padded layout's model count
+    at p=4 FP32 is within 4 % of ncu's 532 wavefronts per cell, and the
+    searched one gives the 382 quoted in the source"""
+    t = B.faces_layout_from_source()
+    assert sorted(t) == [(e, n) for e in (4, 8) for n in range(2, 10)]
+    for (elem, n), L in t.items():
+        sx, sy, sz, rs, fn, fa, cw = L
+        g = np.arange(n)
+        v = (sx * g[:, None, None] + sy * g[None, :, None] + sz * g[None, None, :]).ravel()
+        assert len(np.unique(v)) == v.size and v.max() < rs
+        assert fn >= n and fa >= n * fn and cw >= 4 * rs + 4 * fa
+        pad = B.faces_padded(n)
+        assert cw <= pad[6] + 8, (elem, n)
+        for conv in (False, True):
+            assert B.faces_cost(n, elem, L, conv) <= B.faces_cost(n, elem, pad, conv), (elem, n, conv)
+    assert abs(B.faces_cost(5, 4, B.faces_padded(5)) - 532) < 0.04 * 532
+    assert round(B.faces_cost(5, 4, t[(4, 5)])) == 382
