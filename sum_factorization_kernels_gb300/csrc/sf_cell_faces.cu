@@ -42,8 +42,9 @@ struct FacesLayout {
 };
 
 // Layouts from a shared-memory bank model of every access of the kernel
-// (the cell term's z, x and y line patterns on the four slabs, the face
-// phases' layer reads, row and column passes and injections): stride
+// (faces_cost in sum_factorization_kernels_gb300/bank_model.py: the cell
+// term's z, x and y line patterns on the four slabs, the face phases' layer
+// reads, row and column passes and injections): stride
 // permutations of (1, P1, P2), slab size, face-array strides and the cell
 // stride searched with the per-cell words held at most 8 above those of the
 // padded layout (strides (1, n + 1, n (n + 1) + 1), dense face arrays), so
