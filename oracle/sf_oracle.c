@@ -677,7 +677,7 @@ static void face_interp2(int n, const double *S, int transpose, const double *in
 static void cell_faces_term(const sfo_shape *s, int conv, const double *ij, const double *b,
                             const double *in, double *out)
 {
-  const int n = s->n, p = n - 1, nf = n * n;
+  const int n = s->n, p = n - 1;
   const int str[3] = {1, n, n * n};
   const double hd = s->hermite_d0;
   for (int f = 0; f < 3; ++f) {
@@ -742,7 +742,6 @@ static void cell_faces_term(const sfo_shape *s, int conv, const double *ij, cons
           out[o1 + base] += hd * dv[k];
         }
       }
-    (void)nf;
   }
 }
 

@@ -228,12 +228,12 @@ int sf_create_unstructured(int degree, int basis, long long n_cells, long long n
   // a cell's columns write its nodes from different threads with one
   // store-or-add decision per node: a node listed twice would be written twice
   {
-    std::vector<long long> seen((size_t)n_nodes, -1);
+    std::vector<int> seen((size_t)n_nodes, -1);
     for (long long e = 0; e < n_cells; ++e)
       for (int q = 0; q < n3; ++q) {
-        long long &s = seen[(size_t)cell_nodes[e * n3 + q]];
-        if (s == e) return fail(SF_ERR_INVALID, "a cell lists the same node twice");
-        s = e;
+        int &s = seen[(size_t)cell_nodes[e * n3 + q]];
+        if (s == (int)e) return fail(SF_ERR_INVALID, "a cell lists the same node twice");
+        s = (int)e;
       }
   }
   // greedy colouring: a cell takes the smallest colour no cell sharing one of
