@@ -4,8 +4,10 @@ Workload (the metric's configuration): 64x64x64 hexahedral cells on [0,1]^3
 mapped by x_i <- x_i + 0.05 sin(2 pi x_j) sin(2 pi x_k), Gauss quadrature
 with n = p+1 points, precomputed merged 6-entry geometry per quadrature point,
 homogeneous Dirichlet boundary, input uniform[-1,1].  Headline: degree 4,
-FP32 operator; the JSON line also carries the degree 2..8 sweep in FP32 and
-FP64 with the relative error of every FP32 apply against the FP64 apply.
+FP32 operator.  The JSON line also carries the degree 2..8 sweep in FP32 and
+FP64, each apply with its relative error against the FP64 CPU oracle on the
+same mesh and vector, and the FP32-inner / FP64-refined CG against the plain
+FP64 CG on the same operator.
 
 One step = one operator apply y = A x with x and the geometry resident in
 HBM (the working set, 0.9 GB at p=4 FP32, exceeds the 129 MB L2, so no
@@ -13,15 +15,18 @@ explicit flush).  e2e = the same apply through the C ABI with the input
 copied from pinned host memory and the result copied back every step (steps
 pipelined on three streams with double-buffered device vectors).
 
-``--impl reference`` times the reference's CPU algorithm for the same apply
-on the host cores (the FP64 oracle port, OpenMP over all host threads) on a
-bounded sample of cells and prints the same metric.
+CPU leg (``cpu_baseline``, and the whole of ``--impl reference``): the FP64
+oracle port of the reference's cell algorithm (gather -> even-odd sum
+factorisation -> scatter), built -O3 for the host CPU with OpenMP over all
+host threads, timed on the full workload.  The same leg uses the oracle's
+checker build to state the error of every GPU apply of the sweep.
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import platform
 import statistics
 import sys
 import time
@@ -38,8 +43,8 @@ MEASURED_TRAFFIC = {(4, 64): 985032704}
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the 8 colour launches "
                   "of one apply, caches warm (--cache-control none)")
 UNIT = "GDoF/s"
-REF_BUDGET_S = 120.0  # CPU seconds of the --impl reference run's timed steps
 DEFORM = 0.05
+CPU_REPEATS = 5          # the CPU baseline reports the best of this many applies
 
 
 def algorithmic_bytes(p, n_dofs, n_cells, s):
@@ -49,11 +54,11 @@ def algorithmic_bytes(p, n_dofs, n_cells, s):
 
 
 def workload_config(p, ncells):
-    """the workload keys both arms report (the continuous node count
-    includes the Dirichlet boundary nodes)"""
+    """the workload keys both arms report, identical in both (the continuous
+    node count includes the Dirichlet boundary nodes)"""
     return {"workload": "continuous Laplacian matvec, deformed %d^3 hex mesh, p=%d" % (ncells, p),
             "degree": p, "n_cells": [ncells] * 3, "n_dofs": (p * ncells + 1) ** 3, "deform": DEFORM,
-            "geometry": "merged 6-entry JxW J^-1 J^-T per Gauss point, in the apply's precision",
+            "geometry": "merged 6-entry JxW J^-1 J^-T per Gauss point, precomputed",
             "dirichlet": True}
 
 
@@ -64,6 +69,21 @@ def measured_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def host_cpu():
+    model = platform.processor() or platform.machine()
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu part", "hardware"):
+                    model = line.split(":", 1)[1].strip()
+                    if key == "model name":
+                        break
+    except OSError:
+        pass
+    return {"machine": platform.machine(), "model": model, "nproc": os.cpu_count()}
 
 
 class ClockSampler:
@@ -161,60 +181,173 @@ def max_over_ranks(v, world):
     return float(t.item())
 
 
-def cpu_reference(p, seconds=12.0, n_threads=None):
-    """time the FP64 oracle port of the reference's cell algorithm (gather ->
-    even-odd sum factorisation -> scatter) on a bounded sample mesh"""
+def check_status(op, what):
+    """a bounded wait inside a kernel that timed out invalidates the applies
+    it belongs to: the run fails instead of reporting them"""
+    s = op.device_status()
+    if s != 0:
+        raise SystemExit("device status %d after %s: results invalid" % (s, what))
+
+
+# --------------------------------------------------------------------------
+# CPU leg: the oracle port timed on the host cores (cpu_baseline and the
+# reference arm), and the oracle's checker build stating the GPU's errors
+# --------------------------------------------------------------------------
+def _cpu_env():
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_PLACES", "cores")
+
+
+def cpu_cont_setup(p, ncells):
+    """mesh, precomputed geometry and input of the continuous workload for
+    the timed port (the geometry precomputed as on the GPU)"""
     import numpy as np
 
+    _cpu_env()
     from oracle import oracle as O
 
-    threads = n_threads or os.cpu_count() or 1
-    nc = (16, 16, 16)
-    m = O.mesh(p, nc, deform=DEFORM)
+    m = O.mesh(p, (ncells,) * 3, deform=DEFORM)
     G = O.cont_geometry(m)
-    x = np.random.default_rng(1).uniform(-1, 1, O.cont_n_dofs(m))
-    O.cont_apply(m, G, x, n_threads=threads)  # warm-up
-    reps, t0 = 0, time.perf_counter()
-    while True:
-        O.cont_apply(m, G, x, n_threads=threads)
-        reps += 1
-        el = time.perf_counter() - t0
-        if el >= seconds or reps >= 100000:
-            break
-    n_dofs = O.cont_n_dofs(m)
-    return {"value": n_dofs * reps / el / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "16^3 cells of the deformed mesh, p=%d, FP64, %d applies in %.1f s" % (p, reps, el)}
+    x = np.random.default_rng(20241203).uniform(-1, 1, O.cont_n_dofs(m))
+    return O, m, G, x
+
+
+def cpu_time_best(fn, repeats):
+    ts = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    return min(ts), ts
+
+
+def cpu_cont_baseline(p, ncells, repeats=CPU_REPEATS):
+    """best of `repeats` full applies of the port on the whole workload"""
+    import numpy as np
+
+    O, m, G, x = cpu_cont_setup(p, ncells)
+    L = O.perf_lib()
+    threads = os.cpu_count() or 1
+    y = np.empty_like(x)
+    O.cont_apply(m, G, x, n_threads=threads, y=y, L=L)  # warm-up (page-in, thread pool)
+    best, ts = cpu_time_best(lambda: O.cont_apply(m, G, x, n_threads=threads, y=y, L=L), repeats)
+    n = O.cont_n_dofs(m)
+    return {"value": round(n / best / 1e9, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "the full %d^3 deformed p=%d workload (%d DoFs), FP64, precomputed geometry, best of %d "
+                      "applies (%s s)" % (ncells, p, n, repeats, ", ".join("%.3f" % t for t in ts)),
+            "build": "gcc -O3 -mcpu/-march=native -ffp-contract=fast -fopenmp, OMP_PROC_BIND=close",
+            "host": host_cpu()}
+
+
+def cpu_check_sweep(sweep, ncells):
+    """relative error of every sweep apply against the FP64 oracle (checker
+    build) on the same mesh and vector; geometry computed per cell"""
+    import numpy as np
+
+    _cpu_env()
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    for ent in sweep:
+        host = ent.pop("_host", None)
+        if host is None:
+            continue
+        x, y64, y32 = host
+        m = O.mesh(ent["degree"], (ncells,) * 3, deform=DEFORM)
+        yo = O.cont_apply(m, None, x, n_threads=threads)
+        nrm = float(np.linalg.norm(yo))
+        ent["fp64_rel_err_vs_oracle"] = float("%.3g" % (np.linalg.norm(y64 - yo) / nrm))
+        ent["fp32_rel_err_vs_oracle"] = float("%.3g" % (np.linalg.norm(y32.astype(np.float64) - yo) / nrm))
+        del yo, host
+
+
+def cpu_dg_baselines(configs):
+    """the port's DG SIPG apply (config 3) and DG advection apply (config 5)
+    on the full 48^3 meshes, best of CPU_REPEATS, beside the GPU numbers"""
+    import numpy as np
+
+    _cpu_env()
+    from oracle import oracle as O
+
+    L = O.perf_lib()
+    threads = os.cpu_count() or 1
+    out = {}
+    h = 1.0 / 48
+    g = O.dg(5, (48, 48, 48), (h, h, h), penalty=1.0)
+    n = O.dg_n_dofs(g)
+    x = np.random.default_rng(3).standard_normal(n)
+    y = np.empty_like(x)
+    O.dg_sipg_apply(g, x, L=L, y=y)
+    best, ts = cpu_time_best(lambda: O.dg_sipg_apply(g, x, L=L, y=y), CPU_REPEATS)
+    out["dg_sipg_p5_48c_cg"] = {"cpu_port_apply_fp64_gdofs": round(n / best / 1e9, 4), "cores": threads,
+                                "sample": "full 48^3 p=5 apply, best of %d" % CPU_REPEATS}
+    g = O.dg(4, (48, 48, 48), (h, h, h), velocity=(1.0, 0.5, 0.25), inverse_mass=1)
+    n = O.dg_n_dofs(g)
+    x = np.random.default_rng(5).uniform(-1, 1, n)
+    y = np.empty_like(x)
+    O.dg_advect_apply(g, x, L=L, y=y)
+    best, ts = cpu_time_best(lambda: O.dg_advect_apply(g, x, L=L, y=y), CPU_REPEATS)
+    out["dg_advect_p4_48c_8rhs"] = {"cpu_port_apply_fp64_gdofs_per_rhs": round(n / best / 1e9, 4),
+                                    "cores": threads,
+                                    "sample": "full 48^3 p=4 apply of one right-hand side (with M^-1), best of %d"
+                                              % CPU_REPEATS}
+    for key, ent in out.items():
+        if configs and key in configs:
+            cfg = configs[key]
+            cfg["cpu_baseline"] = ent
+            if key == "dg_sipg_p5_48c_cg":
+                cfg["fp32_apply_over_cpu"] = round(cfg["apply_fp32_gdofs"] / ent["cpu_port_apply_fp64_gdofs"], 1)
+                cfg["fp64_apply_over_cpu"] = round(cfg["apply_fp64_gdofs"] / ent["cpu_port_apply_fp64_gdofs"], 1)
+            else:
+                c = ent["cpu_port_apply_fp64_gdofs_per_rhs"]
+                cfg["fp32_forward_over_cpu"] = round(cfg["fp32"]["forward_gdofs_total_8rhs"] / c, 1)
+                cfg["fp64_forward_over_cpu"] = round(cfg["fp64"]["forward_gdofs_total_8rhs"] / c, 1)
+    return out
 
 
 def run_reference(args):
+    """the reference's CPU algorithm (the oracle port, -O3, all host threads)
+    on the same workload: each step is one full apply"""
+    import numpy as np
+
     rank, world, _ = dist_setup(args.gpus)
     if rank != 0:
         return
-    p = args.degree
-    per_step = []
-    base = None
-    # each step is a bounded sample: the whole run stays within about
-    # REF_BUDGET_S seconds of CPU time whatever --steps is
-    step_s = max(0.05, min(args.ref_seconds, REF_BUDGET_S / max(1, args.steps)))
+    p, nc = args.degree, args.ncells
+    O, m, G, x = cpu_cont_setup(p, nc)
+    L = O.perf_lib()
+    threads = os.cpu_count() or 1
+    y = np.empty_like(x)
+    n = O.cont_n_dofs(m)
     for _ in range(args.warmup):
-        cpu_reference(p, seconds=min(1.0, step_s))
+        O.cont_apply(m, G, x, n_threads=threads, y=y, L=L)
+    ts = []
     for _ in range(args.steps):
-        r = cpu_reference(p, seconds=step_s)
-        per_step.append(r["value"])
-        base = r
-    value = statistics.median(per_step)
-    base["value"] = value
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        t0 = time.perf_counter()
+        O.cont_apply(m, G, x, n_threads=threads, y=y, L=L)
+        ts.append(time.perf_counter() - t0)
+    best, med = min(ts), statistics.median(ts)
+    value = n / best / 1e9
+    base = {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "the full %d^3 deformed p=%d workload (%d DoFs) every step, FP64, precomputed geometry; "
+                      "value from the best of %d steps (median %.4f s, best %.4f s)" % (nc, p, n, len(ts), med, best),
+            "build": "gcc -O3 -mcpu/-march=native -ffp-contract=fast -fopenmp, OMP_PROC_BIND=close",
+            "host": host_cpu()}
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(best * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": workload_config(p, args.ncells),
+            "config": workload_config(p, nc),
             "cpu_baseline": base,
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def time_apply(op, x, y, steps, warmup, stream):
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def time_apply(op, x, y, steps, warmup, stream, what="apply"):
     import torch
     for _ in range(warmup):
         op.vmult(x, y, stream=stream)
@@ -225,7 +358,46 @@ def time_apply(op, x, y, steps, warmup, stream):
         op.vmult(x, y, stream=stream)
     e1.record(stream)
     torch.cuda.synchronize()
+    check_status(op, what)
     return e0.elapsed_time(e1) / 1e3 / steps
+
+
+def solve_entry(code, st):
+    return {"status": code, "iterations": st.iterations, "outer": st.outer_iterations,
+            "rel_residual": float("%.3g" % st.rel_residual), "seconds": round(st.seconds, 3),
+            "operator_applies": st.operator_applies}
+
+
+def cont_cg_sweep(degrees, ncells):
+    """the benchmark spec's target: FP32-inner / FP64-refined CG against plain FP64
+    CG to 1e-10 on the continuous Laplacian of the deformed mesh, Chebyshev(5)
+    Jacobi preconditioner for both, right-hand side uniform[-1,1]"""
+    import numpy as np
+    import torch
+
+    from sum_factorization_kernels_gb300 import sfgpu
+
+    out = {"n_cells": [ncells] * 3, "rtol": 1e-10, "preconditioner": "Chebyshev(5) of D^-1 A, both solves",
+           "degrees": {}}
+    for q in degrees:
+        op = sfgpu.Operator(sfgpu.OP_LAPLACE, degree=q, n_cells=(ncells,) * 3, deform=DEFORM)
+        b = torch.tensor(np.random.default_rng(30 + q).uniform(-1, 1, op.n_dofs), device="cuda")
+        res = {"n_dofs": op.n_dofs}
+        for name, mode in (("mixed_fp32_inner", sfgpu.SOLVE_MIXED), ("all_fp64", sfgpu.SOLVE_FP64)):
+            opts = sfgpu.default_solve_opts(mode=mode, precond=sfgpu.PRECOND_CHEBYSHEV, cheb_degree=5,
+                                            rtol=1e-10, max_iter=20000)
+            # preconditioner setup (diagonal, eigenvalue estimate) is cached per handle
+            op.cg_solve(b, torch.zeros_like(b), sfgpu.default_solve_opts(mode=mode, max_iter=1, rtol=0.5))
+            xs = torch.zeros_like(b)
+            code, st = op.cg_solve(b, xs, opts)
+            res[name] = solve_entry(code, st)
+        check_status(op, "continuous CG p=%d" % q)
+        if res["mixed_fp32_inner"]["seconds"] > 0:
+            res["fp64_over_mixed_wall_time"] = round(res["all_fp64"]["seconds"] / res["mixed_fp32_inner"]["seconds"], 2)
+        out["degrees"][str(q)] = res
+        del op, b
+        torch.cuda.empty_cache()
+    return out
 
 
 def secondary_configs(stream, peak):
@@ -248,7 +420,7 @@ def secondary_configs(stream, peak):
     op = sfgpu.Operator(sfgpu.OP_LAPLACE, degree=4, n_cells=(16, 16, 16))
     x = torch.tensor(np.random.default_rng(20241203).uniform(-1.0, 1.0, op.n_dofs), device="cuda")
     y = torch.empty_like(x)
-    t = time_apply(op, x, y, 50, 5, stream)
+    t = time_apply(op, x, y, 50, 5, stream, "config 1")
     g = np.load(os.path.join(ROOT, "tests", "golden", "cont.npz"))
     idx = g["q4_16_sample_idx"]
     yh = y.cpu().numpy()
@@ -262,10 +434,10 @@ def secondary_configs(stream, peak):
     b = torch.tensor(np.random.default_rng(3).standard_normal(N), device="cuda")
     xd32 = torch.randn(N, device="cuda", dtype=torch.float32)
     yd32 = torch.empty_like(xd32)
-    t32 = time_apply(op, xd32, yd32, 20, 3, stream)
+    t32 = time_apply(op, xd32, yd32, 20, 3, stream, "config 3 FP32")
     xd64 = xd32.double()
     yd64 = torch.empty_like(xd64)
-    t64 = time_apply(op, xd64, yd64, 5, 2, stream)
+    t64 = time_apply(op, xd64, yd64, 5, 2, stream, "config 3 FP64")
     res = {"n_dofs": N, "apply_fp32_gdofs": round(N / t32 / 1e9, 3),
            "apply_fp32_hbm_frac": round(2 * 4 * N / t32 / 1e9 / peak, 4),
            "apply_fp64_gdofs": round(N / t64 / 1e9, 3)}
@@ -275,9 +447,8 @@ def secondary_configs(stream, peak):
                                         rtol=1e-10, project_constant=1, max_iter=4000)
         op.cg_solve(b, torch.zeros_like(b), opts)  # preconditioner setup (cached per handle)
         code, st = op.cg_solve(b, xs, opts)
-        res[name] = {"status": code, "iterations": st.iterations, "outer": st.outer_iterations,
-                     "rel_residual": float("%.3g" % st.rel_residual), "seconds": round(st.seconds, 3),
-                     "operator_applies": st.operator_applies}
+        res[name] = solve_entry(code, st)
+    check_status(op, "config 3 CG")
     if res["mixed_fp32_inner"]["seconds"] > 0:
         res["fp64_over_mixed_wall_time"] = round(res["all_fp64"]["seconds"] / res["mixed_fp32_inner"]["seconds"], 2)
     out["dg_sipg_p5_48c_cg"] = res
@@ -285,8 +456,8 @@ def secondary_configs(stream, peak):
     # the same SIPG problem class in the tensor-product form with precomputed
     # 1D matrices (PrecomputedDGLaplacian): apply and mixed-precision CG
     op = sfgpu.Operator(sfgpu.OP_DG_PRECOMPUTED, degree=5, n_cells=(48, 48, 48), length=(1.0, 1.0, 1.0))
-    t32 = time_apply(op, xd32, yd32, 20, 3, stream)
-    t64 = time_apply(op, xd64, yd64, 5, 2, stream)
+    t32 = time_apply(op, xd32, yd32, 20, 3, stream, "precomputed FP32")
+    t64 = time_apply(op, xd64, yd64, 5, 2, stream, "precomputed FP64")
     res = {"n_dofs": N, "apply_fp32_gdofs": round(N / t32 / 1e9, 3),
            "apply_fp32_hbm_frac": round(2 * 4 * N / t32 / 1e9 / peak, 4),
            "apply_fp64_gdofs": round(N / t64 / 1e9, 3)}
@@ -295,9 +466,8 @@ def secondary_configs(stream, peak):
                                     rtol=1e-10, project_constant=1, max_iter=4000)
     op.cg_solve(b, torch.zeros_like(b), opts)
     code, st = op.cg_solve(b, xs, opts)
-    res["mixed_fp32_inner"] = {"status": code, "iterations": st.iterations, "outer": st.outer_iterations,
-                               "rel_residual": float("%.3g" % st.rel_residual), "seconds": round(st.seconds, 3),
-                               "operator_applies": st.operator_applies}
+    res["mixed_fp32_inner"] = solve_entry(code, st)
+    check_status(op, "precomputed CG")
     out["dg_precomputed_p5_48c"] = res
     del op, b, xd32, yd32, xd64, yd64
     torch.cuda.empty_cache()
@@ -310,7 +480,7 @@ def secondary_configs(stream, peak):
     for prec, dt in (("fp32", torch.float32), ("fp64", torch.float64)):
         xx = (torch.rand(op.n_dofs, device="cuda", dtype=torch.float64) * 2 - 1).to(dt)
         yy = torch.empty_like(xx)
-        tf = time_apply(op, xx, yy, 20, 3, stream)
+        tf = time_apply(op, xx, yy, 20, 3, stream, "config 4 forward")
         dk = torch.empty(nq, dtype=dt, device="cuda")
         for _ in range(3):
             op.kappa_gradient(xx, yy, dk)
@@ -321,6 +491,7 @@ def secondary_configs(stream, peak):
             op.kappa_gradient(xx, yy, dk)
         e1.record()
         torch.cuda.synchronize()
+        check_status(op, "config 4 dkappa")
         tg = e0.elapsed_time(e1) / 1e3 / 10
         res[prec] = {"forward_gdofs": round(op.n_dofs / tf / 1e9, 3),
                      "dkappa_gdofs": round(op.n_dofs / tg / 1e9, 3)}
@@ -335,7 +506,7 @@ def secondary_configs(stream, peak):
     for prec, dt in (("fp32", torch.float32), ("fp64", torch.float64)):
         xx = (torch.rand(8 * N, device="cuda", dtype=torch.float64) * 2 - 1).to(dt)
         yy = torch.empty_like(xx)
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
         for _ in range(3):
             op.vmult_batched(xx, yy, 8, stream=stream)
             op.vmult_transpose_batched(xx, yy, 8, stream=stream)
@@ -354,9 +525,9 @@ def secondary_configs(stream, peak):
         ev[3].record(stream)
         for _ in range(reps):
             op.lsrk_step(xx, old, tmp, 1e-3, nrhs=8, stream=stream)
-        ev.append(torch.cuda.Event(enable_timing=True))
         ev[4].record(stream)
         torch.cuda.synchronize()
+        check_status(op, "config 5 %s" % prec)
         tf = ev[0].elapsed_time(ev[1]) / 1e3 / reps
         tt = ev[1].elapsed_time(ev[2]) / 1e3 / reps
         ts = ev[3].elapsed_time(ev[4]) / 1e3 / reps
@@ -377,6 +548,7 @@ def secondary_configs(stream, peak):
         s_ = slice(r * N, (r + 1) * N)
         lhs, rhs = float(torch.dot(ax[s_], y64[s_])), float(torch.dot(x64[s_], aty[s_]))
         worst = max(worst, abs(lhs - rhs) / float(ax[s_].norm() * y64[s_].norm()))
+    check_status(op, "config 5 dot test")
     res["adjoint_dot_test_rel"] = float("%.3g" % worst)
     out["dg_advect_p4_48c_8rhs"] = res
     del op
@@ -389,7 +561,7 @@ def secondary_configs(stream, peak):
         op = sfgpu.Operator(kind, degree=4, n_cells=(64, 64, 64), velocity=(1.0, 2.0, 3.0))
         x = torch.rand(op.n_dofs, device="cuda", dtype=torch.float32) * 2 - 1
         y = torch.empty_like(x)
-        t = time_apply(op, x, y, 30, 5, stream)
+        t = time_apply(op, x, y, 30, 5, stream, name)
         res[name] = {"gdofs": round(op.n_dofs / t / 1e9, 3), "hbm_frac": round(8 * op.n_dofs / t / 1e9 / peak, 4)}
         del op, x, y
     # the DO_FACES builds on the cell-major vector of the same 64^3 cells
@@ -398,7 +570,7 @@ def secondary_configs(stream, peak):
         op = sfgpu.Operator(kind, degree=4, n_cells=(64, 64, 64), velocity=(1.0, 2.0, 3.0))
         x = torch.rand(op.n_dofs, device="cuda", dtype=torch.float32) * 2 - 1
         y = torch.empty_like(x)
-        t = time_apply(op, x, y, 30, 5, stream)
+        t = time_apply(op, x, y, 30, 5, stream, name)
         res[name] = {"gdofs": round(op.n_dofs / t / 1e9, 3), "hbm_frac": round(8 * op.n_dofs / t / 1e9 / peak, 4),
                      "n_dofs": op.n_dofs}
         del op, x, y
@@ -407,25 +579,15 @@ def secondary_configs(stream, peak):
     # index arrays (lexicographic numbering) and per-cell merged geometry
     # (affine tensor times Gauss weights); bytes: vectors, geometry, indices
     # and the per-column masks ----
+    from sum_factorization_kernels_gb300.timing import unstructured_box
     p_, nc_ = 4, 48
     n_ = p_ + 1
-    S_, D_, xq_, wq_ = sfgpu.shape_tables(p_)
-    Nx = p_ * nc_ + 1
-    cz, cy, cx = np.meshgrid(np.arange(n_), np.arange(n_), np.arange(n_), indexing="ij")
-    kk, jj, ii = np.meshgrid(np.arange(nc_), np.arange(nc_), np.arange(nc_), indexing="ij")
-    idx = (((kk.ravel()[:, None] * p_ + cz.ravel()[None, :]) * Nx + (jj.ravel()[:, None] * p_ + cy.ravel()[None, :]))
-           * Nx + (ii.ravel()[:, None] * p_ + cx.ravel()[None, :])).astype(np.int32)
-    w3 = (wq_[:, None, None] * wq_[None, :, None] * wq_[None, None, :]).ravel()
-    h = 1.0 / nc_
-    g1 = np.zeros((6, n_ ** 3))
-    g1[:3] = h * w3                             # JxW / h_d^2 = h
-    geo = np.broadcast_to(g1, (nc_ ** 3, 6, n_ ** 3))
-    N = Nx ** 3
+    idx, geo, N = unstructured_box(p_, nc_)
     op = sfgpu.Operator.unstructured(p_, idx, geo, N, dirichlet=None, precisions=2)
     del geo, idx
     x = torch.rand(N, device="cuda", dtype=torch.float32) * 2 - 1
     y = torch.empty_like(x)
-    t = time_apply(op, x, y, 30, 5, stream)
+    t = time_apply(op, x, y, 30, 5, stream, "unstructured")
     C = nc_ ** 3
     bytes_apply = 8 * N + C * (6 * n_ ** 3 * 4 + n_ ** 3 * 4 + n_ ** 2 * 4)
     out["unstructured_p4_48c_fp32"] = {"n_dofs": N, "gdofs": round(N / t / 1e9, 3),
@@ -437,6 +599,7 @@ def secondary_configs(stream, peak):
 
 
 def run_ours(args):
+    import numpy as np
     import torch
 
     from sum_factorization_kernels_gb300 import sfgpu
@@ -474,19 +637,12 @@ def run_ours(args):
     barrier(world)
     t_step = e0.elapsed_time(e1) / 1e3 / args.steps
     clk = clocks.stop()
+    check_status(op, "the timed applies")
     t_step = max_over_ranks(t_step, world)
     value = N * world / t_step / 1e9
     bytes_apply = algorithmic_bytes(p, N, C, 4)
     achieved = bytes_apply / t_step / 1e9
     launches_per_apply = 8  # one launch per colour class
-
-    # ---- the other kernel variant at the headline degree (plane ownership) ----
-    variants = {"line_gdofs": round(value / world, 3)}
-    for name, var in (("pair_fp32x2_gdofs", sfgpu.KERNEL_PAIR),):
-        op.set_kernel_variant(var)
-        tv = time_apply(op, x32, y32, max(10, args.steps // 2), 3, stream)
-        variants[name] = round(N / tv / 1e9, 3)
-    op.set_kernel_variant(sfgpu.KERNEL_AUTO)
 
     # ---- e2e: pinned host input -> device -> apply -> host, every step ----
     # Steps are pipelined on three streams with two device buffer pairs:
@@ -538,57 +694,71 @@ def run_ours(args):
     e2e_steps(args.steps)
     torch.cuda.synchronize()
     t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    check_status(op, "the e2e applies")
     e2e = {"value": N * world / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": 4 * N,
            "d2h_bytes_per_step": 4 * N,
            "pipelined": "2 device buffer pairs: H2D of step k+1 and D2H of step k-1 overlap the apply of step k; "
                         "each copy in %d pieces on %d streams" % (nch, nch)}
     if not torch.equal(yh[(args.steps - 1) & 1], yd[(args.steps - 1) & 1].cpu()):
         raise SystemExit("e2e: the result read back differs from the device result")
+    del op, xh, yh, xd, yd, x64, x32, y32
+    torch.cuda.empty_cache()
 
-    # ---- FP64 at the headline degree and the degree sweep ----
+    # ---- the degree sweep, FP32 and FP64; inputs from a seeded host
+    # generator so the CPU leg checks every apply on the same vector ----
     sweep = []
     fp64_value = None
+    check = rank == 0 and world == 1 and not args.no_cpu
     if not args.no_sweep:
-        y64 = torch.empty_like(x64)
-        del op, xh, yh, xd, yd
-        torch.cuda.empty_cache()
         degrees = [int(d) for d in args.sweep.split(",")]
         for q in degrees:
             opq = sfgpu.Operator(sfgpu.OP_LAPLACE, degree=q, n_cells=NCELLS, deform=DEFORM)
             Nq = opq.n_dofs
-            xq64 = torch.rand(Nq, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1
+            xh64 = np.random.default_rng(4000 + q).uniform(-1, 1, Nq)
+            xq64 = torch.from_numpy(xh64).cuda()
             xq32 = xq64.float()
             yq64 = torch.empty_like(xq64)
             yq32 = torch.empty_like(xq32)
             reps64 = max(2, min(args.steps, 6))
-            t64 = time_apply(opq, xq64, yq64, reps64, 2, stream)
-            t32 = time_apply(opq, xq32, yq32, max(3, args.steps), 2, stream)
+            t64 = time_apply(opq, xq64, yq64, reps64, 2, stream, "FP64 sweep p=%d" % q)
+            t32 = time_apply(opq, xq32, yq32, max(3, args.steps), 2, stream, "FP32 sweep p=%d" % q)
             err = float((yq32.double() - yq64).norm() / yq64.norm())
-            variants_q = {}
-            for name, var in (("line", sfgpu.KERNEL_GENERIC), ("pair_fp32x2", sfgpu.KERNEL_PAIR)):
-                opq.set_kernel_variant(var)
-                tv = time_apply(opq, xq32, yq32, max(3, args.steps // 2), 2, stream)
-                variants_q[name] = round(Nq / tv / 1e9, 3)
-            opq.set_kernel_variant(sfgpu.KERNEL_AUTO)
             b32 = algorithmic_bytes(q, Nq, opq.n_cells, 4)
             b64 = algorithmic_bytes(q, Nq, opq.n_cells, 8)
             ent = {"degree": q, "n_dofs": Nq,
                    "fp32_gdofs": round(Nq / t32 / 1e9, 3), "fp32_hbm_frac": round(b32 / t32 / 1e9 / peak, 4),
                    "fp64_gdofs": round(Nq / t64 / 1e9, 3), "fp64_hbm_frac": round(b64 / t64 / 1e9 / peak, 4),
-                   "fp32_rel_err_vs_fp64": float("%.3g" % err), "fp32_variants_gdofs": variants_q}
+                   "fp32_rel_err_vs_fp64": float("%.3g" % err)}
+            if check:
+                ent["_host"] = (xh64, yq64.cpu().numpy(), yq32.cpu().numpy())
             sweep.append(ent)
             if q == p:
                 fp64_value = ent["fp64_gdofs"]
             del opq, xq64, xq32, yq64, yq32
             torch.cuda.empty_cache()
 
+    cg = None
+    if not args.no_cg and world == 1:
+        cg = cont_cg_sweep([int(d) for d in args.cg_degrees.split(",")], args.cg_ncells)
+
     configs = None
     if not args.no_configs and world == 1:
         configs = secondary_configs(stream, peak)
+        if cg is not None:
+            configs["cont_cg_p4_8"] = cg
+    elif cg is not None:
+        configs = {"cont_cg_p4_8": cg}
 
+    # ---- CPU leg (rank 0, one GPU): the port timed on the full workload,
+    # the oracle's errors of every sweep apply, DG baselines ----
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_reference(p, seconds=args.ref_seconds)
+    if check:
+        cpu = cpu_cont_baseline(p, args.ncells)
+        cpu_check_sweep(sweep, args.ncells)
+        if configs is not None and not args.no_configs:
+            cpu_dg_baselines(configs)
+    for ent in sweep:
+        ent.pop("_host", None)
 
     if rank == 0:
         line = {
@@ -596,10 +766,10 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 5),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": dict(workload_config(p, args.ncells),
-                           parallelism="replicas" if world > 1 else "single GPU",
-                           l2="working set %.2f GB > 129 MB L2, no flush" % (bytes_apply / 1e9),
-                           fp64_gdofs_same_degree=fp64_value, kernel_variants=variants),
+            "config": workload_config(p, args.ncells),
+            "details": {"parallelism": "replicas" if world > 1 else "single GPU",
+                        "l2": "working set %.2f GB > 129 MB L2, no flush" % (bytes_apply / 1e9),
+                        "fp64_gdofs_same_degree": fp64_value},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": MEASURED_TRAFFIC.get((p, args.ncells)),
@@ -627,9 +797,11 @@ def main():
     ap.add_argument("--ncells", type=int, default=64, help="cells per direction")
     ap.add_argument("--sweep", default="2,3,4,5,6,7,8")
     ap.add_argument("--no-sweep", action="store_true")
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU leg (baseline and oracle errors)")
     ap.add_argument("--no-configs", action="store_true", help="skip configs 1, 3, 4, 5")
-    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cg", action="store_true", help="skip the continuous CG comparison")
+    ap.add_argument("--cg-degrees", default="4,5,6,7,8")
+    ap.add_argument("--cg-ncells", type=int, default=64)
     ap.add_argument("--e2e-chunks", type=int, default=1, help="pieces per host-device copy in the e2e leg")
     args = ap.parse_args()
     if args.impl == "reference":

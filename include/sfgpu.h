@@ -231,16 +231,11 @@ int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void 
 /* Kernel selection for the continuous Laplacian apply.  SF_KERNEL_AUTO and
  * SF_KERNEL_GENERIC: the packed line-ownership kernel (one thread per line
  * of a cell, several cells per warp group) for both precisions, structured
- * or unstructured.  SF_KERNEL_PAIR: the FP32 paired line-ownership kernel
- * (two cells per thread in packed FP32x2 arithmetic; structured meshes).
- * SF_KERNEL_CELL: one block of cells per launch with block barriers and
- * geometry read in the quadrature-point operation (unstructured meshes).
- * For comparisons; no reference counterpart. */
+ * or unstructured.  Other values are rejected with SF_ERR_INVALID.  No
+ * reference counterpart. */
 typedef enum {
   SF_KERNEL_AUTO = 0,
-  SF_KERNEL_GENERIC = 1,
-  SF_KERNEL_PAIR = 2,
-  SF_KERNEL_CELL = 3
+  SF_KERNEL_GENERIC = 1
 } sf_kernel_variant;
 int sf_set_kernel_variant(sf_op *op, int variant);
 /* Device-side error flags of the handle's kernels (bit 0: a bounded wait
@@ -265,7 +260,9 @@ typedef struct {
   int eig_iterations;    /* Lanczos steps for lambda_max (default 12)            */
   double rtol;           /* relative residual target |b - A x| / |b|             */
   int max_iter;          /* total inner iterations allowed                       */
-  double inner_rtol;     /* SF_SOLVE_MIXED: inner relative tolerance (1e-3)     */
+  double inner_rtol;     /* SF_SOLVE_MIXED: floor of the inner solves' relative
+                            tolerance (1e-6); each stops at max(inner_rtol,
+                            rtol |b| / (2 |r|)) for the outer residual r    */
   int project_constant;  /* 1: remove the mean from b and x (periodic SIPG)      */
 } sf_solve_opts;
 

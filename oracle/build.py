@@ -12,8 +12,14 @@
 The reference is compiled with its generic one-lane ``VectorizedArray``
 (ISA macros undefined, empty ``x86intrin.h`` stand-in), so the reference's
 lane-interleaved DG vectors coincide with the cell-major layout used here.
-Two DG headers are copied into ``oracle/_ref/patched/`` and patched at build
-time (PATCHES below); nothing of the reference is stored in the repository.
+Four reference headers (``evaluation_dg_laplacian.h``,
+``evaluation_dg_advect.h``, ``precomputed_dg_laplacian.h``,
+``matrix_vector_kernel.h``) are copied into ``oracle/_ref/patched/`` and
+patched at build time (PATCHES below); nothing of the reference is stored in
+the repository.
+
+``build_oracle_perf()`` compiles the same oracle source for timing (the CPU
+baseline of ``bench.py``).
 """
 from __future__ import annotations
 
@@ -23,7 +29,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("SF_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: SF_REFERENCE_ROOT, else a checkout named
+# "reference" beside this repository
+REF_ROOT = os.environ.get("SF_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 REF_INC = os.path.join(REF_ROOT, "legacy", "include")
 REF_SRC = os.path.join(REF_ROOT, "legacy", "src")
 OUT_REF = os.path.join(HERE, "_ref")
@@ -86,6 +94,24 @@ def build_oracle(force: bool = False) -> str:
         return out
     tmp = out + ".tmp%d" % os.getpid()
     _run(["gcc", "-O2", "-std=c11", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src, "-lm"])
+    os.replace(tmp, out)
+    return out
+
+
+def build_oracle_perf(force: bool = False) -> str:
+    """the oracle source compiled for timing as the CPU baseline: -O3, tuned
+    for the host CPU, floating-point contraction allowed (the flags the
+    reference's drivers are benchmarked with), OpenMP"""
+    import platform
+    out = os.path.join(HERE, "liboracle_perf.so")
+    src = os.path.join(HERE, "sf_oracle.c")
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "sf_oracle.h"))):
+        return out
+    tune = "-mcpu=native" if platform.machine() in ("aarch64", "arm64") else "-march=native"
+    tmp = out + ".tmp%d" % os.getpid()
+    _run(["gcc", "-O3", tune, "-ffp-contract=fast", "-std=gnu11", "-fopenmp", "-fPIC", "-shared", "-o", tmp,
+          src, "-lm"])
     os.replace(tmp, out)
     return out
 

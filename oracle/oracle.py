@@ -51,41 +51,57 @@ class DG(C.Structure):
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
 
+def _load(path):
+    L = C.CDLL(path)
+    L.sfo_shape_init.argtypes = [C.c_int, C.c_int, C.POINTER(Shape)]
+    L.sfo_apply_1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp,
+                               C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.sfo_cont_n_dofs.argtypes = [C.POINTER(Mesh)]
+    L.sfo_cont_n_dofs.restype = C.c_longlong
+    L.sfo_cont_geometry.argtypes = [C.POINTER(Mesh), _dp]
+    L.sfo_cont_apply.argtypes = [C.POINTER(Mesh), C.c_void_p, C.c_void_p, _dp, _dp, C.c_int]
+    L.sfo_cont_kappa_grad.argtypes = [C.POINTER(Mesh), _dp, _dp, _dp, _dp]
+    L.sfo_cont_diagonal.argtypes = [C.POINTER(Mesh), _dp, C.c_void_p, _dp]
+    L.sfo_cell_apply.argtypes = [C.POINTER(Shape), _dp, C.c_int, _dp, _dp]
+    L.sfo_cell_op.argtypes = [C.POINTER(Shape), C.c_int, _dp, C.c_double, _dp, _dp, _dp]
+    L.sfo_cell_faces.argtypes = [C.POINTER(Shape), C.c_int, _dp, C.c_double, _dp, _dp, _dp]
+    L.sfo_cell_faces_apply.argtypes = [C.c_int, C.c_int, C.c_longlong, _dp, _dp, _dp, _dp]
+    L.sfo_cont_apply_op.argtypes = [C.POINTER(Mesh), C.c_int, _dp, _dp, _dp]
+    L.sfo_unstructured_apply.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_void_p,
+                                         _dp, C.c_void_p, _dp, _dp]
+    L.sfo_dg_n_dofs.argtypes = [C.POINTER(DG)]
+    L.sfo_dg_n_dofs.restype = C.c_longlong
+    for f in ("sfo_dg_sipg_apply", "sfo_dg_advect_apply", "sfo_dg_advect_apply_transpose"):
+        getattr(L, f).argtypes = [C.POINTER(DG), _dp, _dp]
+    L.sfo_dg_sipg_diagonal.argtypes = [C.POINTER(DG), _dp]
+    L.sfo_dg_precomputed_apply.argtypes = [C.POINTER(DG), _dp, _dp]
+    L.sfo_dg_precomputed_diagonal.argtypes = [C.POINTER(DG), _dp]
+    L.sfo_dg_precomputed_matrices.argtypes = [C.c_int, _dp, _dp, _dp]
+    L.sfo_dg_rk_stage.argtypes = [C.POINTER(DG), _dp, _dp, _dp, _dp, C.c_double, C.c_double]
+    L.sfo_dg_lsrk_step.argtypes = [C.POINTER(DG), C.c_double, _dp, _dp, _dp]
+    L.sfo_chebyshev_update.argtypes = [C.c_longlong, _dp, _dp, _dp, _dp, _dp, _dp,
+                                       C.c_double, C.c_double]
+    return L
+
+
 def lib():
+    """the checker build (-O2, ISO C: no floating-point contraction)"""
     global _lib
     if _lib is None:
-        path = _build.build_oracle()
-        L = C.CDLL(path)
-        L.sfo_shape_init.argtypes = [C.c_int, C.c_int, C.POINTER(Shape)]
-        L.sfo_apply_1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp,
-                                   C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
-        L.sfo_cont_n_dofs.argtypes = [C.POINTER(Mesh)]
-        L.sfo_cont_n_dofs.restype = C.c_longlong
-        L.sfo_cont_geometry.argtypes = [C.POINTER(Mesh), _dp]
-        L.sfo_cont_apply.argtypes = [C.POINTER(Mesh), _dp, C.c_void_p, _dp, _dp, C.c_int]
-        L.sfo_cont_kappa_grad.argtypes = [C.POINTER(Mesh), _dp, _dp, _dp, _dp]
-        L.sfo_cont_diagonal.argtypes = [C.POINTER(Mesh), _dp, C.c_void_p, _dp]
-        L.sfo_cell_apply.argtypes = [C.POINTER(Shape), _dp, C.c_int, _dp, _dp]
-        L.sfo_cell_op.argtypes = [C.POINTER(Shape), C.c_int, _dp, C.c_double, _dp, _dp, _dp]
-        L.sfo_cell_faces.argtypes = [C.POINTER(Shape), C.c_int, _dp, C.c_double, _dp, _dp, _dp]
-        L.sfo_cell_faces_apply.argtypes = [C.c_int, C.c_int, C.c_longlong, _dp, _dp, _dp, _dp]
-        L.sfo_cont_apply_op.argtypes = [C.POINTER(Mesh), C.c_int, _dp, _dp, _dp]
-        L.sfo_unstructured_apply.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_void_p,
-                                             _dp, C.c_void_p, _dp, _dp]
-        L.sfo_dg_n_dofs.argtypes = [C.POINTER(DG)]
-        L.sfo_dg_n_dofs.restype = C.c_longlong
-        for f in ("sfo_dg_sipg_apply", "sfo_dg_advect_apply", "sfo_dg_advect_apply_transpose"):
-            getattr(L, f).argtypes = [C.POINTER(DG), _dp, _dp]
-        L.sfo_dg_sipg_diagonal.argtypes = [C.POINTER(DG), _dp]
-        L.sfo_dg_precomputed_apply.argtypes = [C.POINTER(DG), _dp, _dp]
-        L.sfo_dg_precomputed_diagonal.argtypes = [C.POINTER(DG), _dp]
-        L.sfo_dg_precomputed_matrices.argtypes = [C.c_int, _dp, _dp, _dp]
-        L.sfo_dg_rk_stage.argtypes = [C.POINTER(DG), _dp, _dp, _dp, _dp, C.c_double, C.c_double]
-        L.sfo_dg_lsrk_step.argtypes = [C.POINTER(DG), C.c_double, _dp, _dp, _dp]
-        L.sfo_chebyshev_update.argtypes = [C.c_longlong, _dp, _dp, _dp, _dp, _dp, _dp,
-                                           C.c_double, C.c_double]
-        _lib = L
+        _lib = _load(_build.build_oracle())
     return _lib
+
+
+_perf = None
+
+
+def perf_lib():
+    """the same source built for timing (-O3, native CPU tuning, contraction
+    allowed): the CPU baseline; results agree with lib() to rounding"""
+    global _perf
+    if _perf is None:
+        _perf = _load(_build.build_oracle_perf())
+    return _perf
 
 
 def shape(degree: int, basis: int = BASIS_GLL) -> Shape:
@@ -150,11 +166,15 @@ def cont_geometry(m: Mesh) -> np.ndarray:
     return G
 
 
-def cont_apply(m: Mesh, G, x, kappa=None, n_threads=0):
-    y = np.zeros(cont_n_dofs(m))
+def cont_apply(m: Mesh, G, x, kappa=None, n_threads=0, y=None, L=None):
+    """y = A x; G None computes each cell's geometry on the fly (no
+    [cell][6][n^3] array); L selects the library build (default: the
+    checker build)"""
+    y = np.zeros(cont_n_dofs(m)) if y is None else y
     k = np.ascontiguousarray(kappa, dtype=np.float64) if kappa is not None else None
-    lib().sfo_cont_apply(C.byref(m), np.ascontiguousarray(G), k.ctypes.data if k is not None else None,
-                         np.ascontiguousarray(x, dtype=np.float64), y, n_threads)
+    g = None if G is None else np.ascontiguousarray(G).ctypes.data
+    (L or lib()).sfo_cont_apply(C.byref(m), g, k.ctypes.data if k is not None else None,
+                                np.ascontiguousarray(x, dtype=np.float64), y, n_threads)
     return y
 
 
@@ -306,18 +326,18 @@ def dg_n_dofs(g: DG) -> int:
     return int(lib().sfo_dg_n_dofs(C.byref(g)))
 
 
-def _dg_call(name, g, x):
-    y = np.zeros(dg_n_dofs(g))
-    getattr(lib(), name)(C.byref(g), np.ascontiguousarray(x, dtype=np.float64), y)
+def _dg_call(name, g, x, L=None, y=None):
+    y = np.zeros(dg_n_dofs(g)) if y is None else y
+    getattr(L or lib(), name)(C.byref(g), np.ascontiguousarray(x, dtype=np.float64), y)
     return y
 
 
-def dg_sipg_apply(g, x):
-    return _dg_call("sfo_dg_sipg_apply", g, x)
+def dg_sipg_apply(g, x, L=None, y=None):
+    return _dg_call("sfo_dg_sipg_apply", g, x, L, y)
 
 
-def dg_advect_apply(g, x):
-    return _dg_call("sfo_dg_advect_apply", g, x)
+def dg_advect_apply(g, x, L=None, y=None):
+    return _dg_call("sfo_dg_advect_apply", g, x, L, y)
 
 
 def dg_advect_apply_transpose(g, x):

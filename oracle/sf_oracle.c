@@ -813,11 +813,49 @@ static void mapping_jacobian(const sfo_mesh *m, const double X[3], const double 
   J[2][2] = h[2];
 }
 
+/* merged tensor JxW J^-1 J^-T (times the Gauss weights) of cell (i, j, k) at
+ * its n^3 Gauss points: g[e n^3 + q], e = xx, yy, zz, xy, xz, yz */
+static void cont_cell_geometry(const sfo_mesh *m, const sfo_shape *s, int i, int j, int k,
+                               const double h[3], double *g)
+{
+  const int n = s->n, nq = n * n * n;
+  for (int qz = 0; qz < n; ++qz)
+    for (int qy = 0; qy < n; ++qy)
+      for (int qx = 0; qx < n; ++qx) {
+        const int q = (qz * n + qy) * n + qx;
+        const double X[3] = {(i + s->xq[qx]) * h[0], (j + s->xq[qy]) * h[1],
+                             (k + s->xq[qz]) * h[2]};
+        double J[3][3];
+        mapping_jacobian(m, X, h, J);
+        const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                           J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        double Ji[3][3];
+        Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+        Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+        Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+        const double jxw = det * ((s->wq[qz] * s->wq[qy]) * s->wq[qx]);
+        static const int pr[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+        for (int e = 0; e < 6; ++e) {
+          const int d0 = pr[e][0], d1 = pr[e][1];
+          const double v = Ji[d0][0] * Ji[d1][0] + Ji[d0][1] * Ji[d1][1] +
+                           Ji[d0][2] * Ji[d1][2];
+          g[e * nq + q] = jxw * v;
+        }
+      }
+}
+
 void sfo_cont_geometry(const sfo_mesh *m, double *G)
 {
   sfo_shape s;
   sfo_shape_init(m->degree, m->basis, &s);
-  const int n = s.n, nq = n * n * n;
+  const int nq = s.n * s.n * s.n;
   const long long C = (long long)m->n_cells[0] * m->n_cells[1] * m->n_cells[2];
   double h[3];
   for (int d = 0; d < 3; ++d) h[d] = m->length[d] / m->n_cells[d];
@@ -826,37 +864,7 @@ void sfo_cont_geometry(const sfo_mesh *m, double *G)
     const int i = (int)(cell % m->n_cells[0]);
     const int j = (int)((cell / m->n_cells[0]) % m->n_cells[1]);
     const int k = (int)(cell / ((long long)m->n_cells[0] * m->n_cells[1]));
-    double *g = G + cell * 6 * nq;
-    for (int qz = 0; qz < n; ++qz)
-      for (int qy = 0; qy < n; ++qy)
-        for (int qx = 0; qx < n; ++qx) {
-          const int q = (qz * n + qy) * n + qx;
-          const double X[3] = {(i + s.xq[qx]) * h[0], (j + s.xq[qy]) * h[1],
-                               (k + s.xq[qz]) * h[2]};
-          double J[3][3];
-          mapping_jacobian(m, X, h, J);
-          const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
-                             J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                             J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-          double Ji[3][3];
-          Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
-          Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
-          Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
-          Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
-          Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
-          Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
-          Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
-          Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
-          Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
-          const double jxw = det * ((s.wq[qz] * s.wq[qy]) * s.wq[qx]);
-          static const int pr[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
-          for (int e = 0; e < 6; ++e) {
-            const int d0 = pr[e][0], d1 = pr[e][1];
-            const double v = Ji[d0][0] * Ji[d1][0] + Ji[d0][1] * Ji[d1][1] +
-                             Ji[d0][2] * Ji[d1][2];
-            g[e * nq + q] = jxw * v;
-          }
-        }
+    cont_cell_geometry(m, &s, i, j, k, h, G + cell * 6 * nq);
   }
 }
 
@@ -880,13 +888,16 @@ void sfo_cont_apply(const sfo_mesh *m, const double *G, const double *kappa,
   sfo_shape_init(m->degree, m->basis, &s);
   const int n = s.n, nq = n * n * n;
   const long long N = sfo_cont_n_dofs(m);
-  memset(y, 0, sizeof(double) * N);
 #ifdef _OPENMP
   if (n_threads > 0) omp_set_num_threads(n_threads);
 #else
   (void)n_threads;
 #endif
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < N; ++i) y[i] = 0.;
   const int nx = m->n_cells[0], ny = m->n_cells[1], nz = m->n_cells[2];
+  double h[3];
+  for (int d = 0; d < 3; ++d) h[d] = m->length[d] / m->n_cells[d];
   /* 8-colour cell order: cells of one colour share no node */
   for (int color = 0; color < 8; ++color) {
     const int cx = color & 1, cy = (color >> 1) & 1, cz = (color >> 2) & 1;
@@ -894,16 +905,19 @@ void sfo_cont_apply(const sfo_mesh *m, const double *G, const double *kappa,
     const long long count = (long long)mx * my * mz;
 #pragma omp parallel
     {
-      double *u = (double *)malloc(sizeof(double) * nq * 2);
-      double *v = u + nq;
+      /* G == NULL: each cell's geometry is computed where it is used */
+      double *u = (double *)malloc(sizeof(double) * nq * (G ? 2 : 8));
+      double *v = u + nq, *gc = u + 2 * nq;
 #pragma omp for schedule(static)
       for (long long t = 0; t < count; ++t) {
         const int i = 2 * (int)(t % mx) + cx;
         const int j = 2 * (int)((t / mx) % my) + cy;
         const int k = 2 * (int)(t / ((long long)mx * my)) + cz;
         const long long cell = ((long long)k * ny + j) * nx + i;
+        const double *Gc = G ? G + cell * 6 * nq : gc;
+        if (!G) cont_cell_geometry(m, &s, i, j, k, h, gc);
         cont_gather(m, i, j, k, x, u);
-        cell_apply_k(&s, G + cell * 6 * nq, nq, kappa ? kappa + cell * nq : NULL, u, v);
+        cell_apply_k(&s, Gc, nq, kappa ? kappa + cell * nq : NULL, u, v);
         for (int c = 0; c < n; ++c)
           for (int b = 0; b < n; ++b)
             for (int a = 0; a < n; ++a) {
@@ -919,6 +933,7 @@ void sfo_cont_apply(const sfo_mesh *m, const double *G, const double *kappa,
     const int p = m->degree;
     const long long Nx = (long long)p * nx + 1, Ny = (long long)p * ny + 1,
                     Nz = (long long)p * nz + 1;
+#pragma omp parallel for schedule(static)
     for (long long Z = 0; Z < Nz; ++Z)
       for (long long Y = 0; Y < Ny; ++Y)
         for (long long X = 0; X < Nx; ++X)

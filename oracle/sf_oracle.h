@@ -84,7 +84,9 @@ typedef struct {
 long long sfo_cont_n_dofs(const sfo_mesh *m);
 /* merged tensor G[cell][6][nq] = JxW * J^-1 J^-T (order xx,yy,zz,xy,xz,yz) */
 void sfo_cont_geometry(const sfo_mesh *m, double *G);
-/* y = A x (kappa may be NULL => 1).  Dirichlet rows: y_b = x_b. */
+/* y = A x (kappa may be NULL => 1).  Dirichlet rows: y_b = x_b.  G may be
+ * NULL: each cell's merged tensor is then computed where it is used (the
+ * same values as sfo_cont_geometry, without the [cell][6][nq] array). */
 void sfo_cont_apply(const sfo_mesh *m, const double *G, const double *kappa,
                     const double *x, double *y, int n_threads);
 /* dL/dkappa_q = grad(u)_q . G_q grad(lam)_q with Dirichlet entries zeroed */

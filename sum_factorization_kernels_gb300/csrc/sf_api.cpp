@@ -1,6 +1,7 @@
 // sf_api.cpp -- the C ABI (include/sfgpu.h): argument validation, handle
 // state, dispatch to the kernel launchers.  No exception leaves this file.
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
@@ -79,30 +80,32 @@ int check_ptr(const void *p, int prec, const char *name)
   return SF_OK;
 }
 
+// NVTX names of a handle's calls, after the reference's LIKWID regions
+void name_regions(sf_op *op)
+{
+  const int p = op->desc.degree;
+  const int k = op->desc.kind;
+  if (k == SF_OP_DG_SIPG || k == SF_OP_DG_PRECOMPUTED) {
+    std::snprintf(op->region_mv, sizeof op->region_mv, "real_dg_laplacian_3d_deg_%dmv", p);
+    std::snprintf(op->region_ch, sizeof op->region_ch, "real_dg_laplacian_3d_deg_%dch", p);
+  } else if (k == SF_OP_DG_ADVECT) {
+    std::snprintf(op->region_mv, sizeof op->region_mv, "dg_advect_3d_deg_%dmv", p);
+    std::snprintf(op->region_ch, sizeof op->region_ch, "dg_advect_3d_deg_%drk", p);
+  } else {
+    std::snprintf(op->region_mv, sizeof op->region_mv, "cell_laplacian_deg_%d", p);
+    std::snprintf(op->region_ch, sizeof op->region_ch, "cell_laplacian_deg_%d_cheby", p);
+  }
+}
+
 #define SF_RET(x)                                                              \
   do {                                                                         \
     int r_ = (x);                                                              \
     if (r_ != SF_OK) return r_;                                                \
   } while (0)
 
-// derived FP32 copies of the FP64 geometry (and coefficient): the natural
-// layout for the generic kernels, the colour-major plane layout for the
-// FP32 degree 1..4 kernel
-// The pair kernel reads its own FP32 geometry layout; that copy exists only
-// while the pair variant is selected.
-int derive_variant_geometry(sf_op *op)
-{
-  const bool fp32 = (op->desc.precisions & 2) && op->deformed && op->desc.kind == SF_OP_LAPLACE;
-  const double *k64 = op->has_kappa ? (const double *)op->kap64.ptr : nullptr;
-  if (fp32 && op->kernel_variant == SF_KERNEL_PAIR)
-    SF_RET(repack_pair_geometry(op, (const double *)op->geo64.ptr, op->geo_stride, k64, 0));
-  else
-    op->geoPair.release();
-  return SF_OK;
-}
-
 // derived copies of the FP64 geometry: the walk-ordered blocks of the line
-// kernel (each prepared precision), the natural FP32 copy and the variant's
+// kernel (each prepared precision) and the natural FP32 copy (diagonal,
+// kappa gradient)
 int derive_fp32_geometry(sf_op *op)
 {
   if (!op->deformed) return SF_OK;
@@ -115,7 +118,6 @@ int derive_fp32_geometry(sf_op *op)
   const size_t entries = (size_t)op->n_cells * op->geo_stride;
   if (op->geo32.bytes != entries * sizeof(float)) SF_RET(op->geo32.alloc(entries * sizeof(float)));
   SF_RET(launch_convert((long long)entries, SF_FP64, op->geo64.ptr, SF_FP32, op->geo32.ptr, 0));
-  SF_RET(derive_variant_geometry(op));
   SF_CUDA_TRY(cudaDeviceSynchronize());
   return SF_OK;
 }
@@ -167,6 +169,7 @@ int sf_create(const sf_desc *desc, sf_op **out)
   op->desc.basis = basis;
   fill_shape(d.degree, basis, op->shape);
   op->n = d.degree + 1;
+  name_regions(op);
   for (int k = 0; k < 3; ++k) op->h[k] = d.length[k] / d.n_cells[k];
   op->n_cells = (long long)d.n_cells[0] * d.n_cells[1] * d.n_cells[2];
   if (op->n_cells >= (1LL << 31)) {
@@ -306,6 +309,7 @@ int sf_create_unstructured(int degree, int basis, long long n_cells, long long n
   }
   fill_shape(degree, basis, op->shape);
   op->n = n;
+  name_regions(op);
   op->n_cells = n_cells;
   op->n_dofs = n_nodes;
   op->unstr.reset(new (std::nothrow) sf_unstructured());
@@ -397,11 +401,9 @@ int sf_set_coefficient(sf_op *op, const double *kappa)
 int sf_set_kernel_variant(sf_op *op, int variant)
 {
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
-  if (variant < SF_KERNEL_AUTO || variant > SF_KERNEL_CELL)
+  if (variant < SF_KERNEL_AUTO || variant > SF_KERNEL_GENERIC)
     return fail(SF_ERR_INVALID, "unknown kernel variant");
   op->kernel_variant = variant;
-  SF_RET(derive_variant_geometry(op));
-  SF_CUDA_TRY(cudaDeviceSynchronize());
   return SF_OK;
 }
 
@@ -420,6 +422,7 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
   SF_RET(check_ptr(y, prec, "y"));
   if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
+  const Region region(op->region_mv);
   if (is_continuous(op->desc.kind)) return launch_cont_vmult(op, prec, x, y, st);
   if (is_cell_faces(op->desc.kind)) return launch_cell_faces(op, prec, 1, x, y, st);
   if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
@@ -445,6 +448,7 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
   if (nrhs < 1 || nrhs > 64) return fail(SF_ERR_INVALID, "nrhs must be 1..64");
   if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
+  const Region region(op->region_mv);
   if (is_continuous(op->desc.kind)) {
     const size_t es = elem_size(prec);
     for (int r = 0; r < nrhs; ++r)
@@ -470,6 +474,7 @@ int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, voi
   if (nrhs < 1 || nrhs > 64) return fail(SF_ERR_INVALID, "nrhs must be 1..64");
   if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
+  const Region region(op->region_mv);
   const void *src = x;
   if (op->desc.inverse_mass) {
     const size_t bytes = (size_t)nrhs * op->n_dofs * elem_size(prec);
@@ -494,6 +499,7 @@ int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv, 
   if (is_cell_faces(op->desc.kind))
     return fail(SF_ERR_UNSUPPORTED, "Chebyshev steps: not for the face-term operators");
   cudaStream_t st = (cudaStream_t)stream;
+  const Region region(op->region_ch);
   if (op->desc.kind == SF_OP_DG_SIPG || op->desc.kind == SF_OP_DG_ADVECT)
     return launch_dg_vmult(op, prec, 1, false, x_old, x_new, b, diag_inv, t, c_np, c_tm, st);
   if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
@@ -517,6 +523,7 @@ int sf_rk_stage(sf_op *op, int prec, int nrhs, const void *src, const void *upd,
   if (src == vec_np || (c_tm != 0.0 && src == vec_tm))
     return fail(SF_ERR_INVALID, "src must not be an output vector");
   if (c_tm != 0.0 && vec_np == vec_tm) return fail(SF_ERR_INVALID, "vec_np and vec_tm must differ");
+  const Region region(op->region_ch);
   return launch_dg_rk_stage(op, prec, nrhs, src, upd, vec_np, c_tm != 0.0 ? vec_tm : nullptr, c_np, c_tm,
                             (cudaStream_t)stream);
 }

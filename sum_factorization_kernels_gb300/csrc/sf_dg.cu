@@ -803,14 +803,14 @@ int launch_dg_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st)
     int r = buf.alloc(n3 * sizeof(double));
     if (r) return r;
     SF_CUDA_TRY(cudaMemcpyAsync(buf.ptr, pat, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
-    pattern_kernel<double><<<152 * 8, 256, 0, st>>>(op->n_dofs, n3, (const double *)buf.ptr, (double *)diag);
+    pattern_kernel<double><<<device_sm_count() * 8, 256, 0, st>>>(op->n_dofs, n3, (const double *)buf.ptr, (double *)diag);
   } else {
     float pf[kMaxN * kMaxN * kMaxN];
     for (int i = 0; i < n3; ++i) pf[i] = float(pat[i]);
     int r = buf.alloc(n3 * sizeof(float));
     if (r) return r;
     SF_CUDA_TRY(cudaMemcpyAsync(buf.ptr, pf, n3 * sizeof(float), cudaMemcpyHostToDevice, st));
-    pattern_kernel<float><<<152 * 8, 256, 0, st>>>(op->n_dofs, n3, (const float *)buf.ptr, (float *)diag);
+    pattern_kernel<float><<<device_sm_count() * 8, 256, 0, st>>>(op->n_dofs, n3, (const float *)buf.ptr, (float *)diag);
   }
   SF_CUDA_TRY(cudaGetLastError());
   // the staging buffer is released when buf goes out of scope; wait for the

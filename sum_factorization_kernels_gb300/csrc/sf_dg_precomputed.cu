@@ -388,10 +388,10 @@ int launch_dg_precomputed_diagonal(const sf_op *op, int prec, void *diag, cudaSt
   SF_CUDA_TRY(cudaMemcpyAsync(buf.ptr, prec == SF_FP64 ? (const void *)pat : (const void *)patf, n3 * es,
                               cudaMemcpyHostToDevice, st));
   if (prec == SF_FP64)
-    precomputed_pattern_kernel<double><<<152 * 8, 256, 0, st>>>(op->n_dofs, n3, (const double *)buf.ptr,
+    precomputed_pattern_kernel<double><<<device_sm_count() * 8, 256, 0, st>>>(op->n_dofs, n3, (const double *)buf.ptr,
                                                                (double *)diag);
   else
-    precomputed_pattern_kernel<float><<<152 * 8, 256, 0, st>>>(op->n_dofs, n3, (const float *)buf.ptr,
+    precomputed_pattern_kernel<float><<<device_sm_count() * 8, 256, 0, st>>>(op->n_dofs, n3, (const float *)buf.ptr,
                                                               (float *)diag);
   SF_CUDA_TRY(cudaGetLastError());
   // the staging buffer is released when buf goes out of scope

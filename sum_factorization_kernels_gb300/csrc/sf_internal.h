@@ -8,6 +8,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/sfgpu.h"
 
@@ -49,6 +50,19 @@ struct DevBuf {
   ~DevBuf() { release(); }
 };
 
+// NVTX range around one library call, named after the LIKWID region the
+// reference's drivers put around the same operation
+// (legacy/src/test_program.cc:107-109: cell_laplacian_deg_<p>;
+// legacy/include/evaluation_dg_laplacian.h:525-529:
+// real_dg_laplacian_3d_deg_<p>{mv,ch}; legacy/include/evaluation_dg_advect.h:
+// 693-695: dg_advect_3d_deg_<p>{mv,rk})
+struct Region {
+  explicit Region(const char *name) { nvtxRangePushA(name); }
+  ~Region() { nvtxRangePop(); }
+  Region(const Region &) = delete;
+  Region &operator=(const Region &) = delete;
+};
+
 } // namespace sf
 
 // unstructured-mesh data of a SF_OP_LAPLACE_UNSTRUCTURED handle
@@ -72,12 +86,12 @@ struct sf_op {
   sf::DevBuf kap64, kap32;      // [cell][n^3] coefficient
   bool has_kappa = false;
   sf::DevBuf scratch;           // operator-private scratch (transpose, M^-1)
-  sf::DevBuf geoPair;           // FP32 geometry for the pair kernel (pair-interleaved)
   sf::DevBuf geoLine64, geoLine32; // geometry in the line kernel's walk order
   std::unique_ptr<sf_unstructured> unstr; // SF_OP_LAPLACE_UNSTRUCTURED only
-  long long geoPair_stride = 0;
   sf::DevBuf dev_err;           // device error flags (bounded waits)
   int kernel_variant = 0;       // sf_kernel_variant
+  char region_mv[48] = {};      // NVTX names of the apply and of the smoother /
+  char region_ch[48] = {};      // Runge-Kutta step (sf::Region)
   double h[3];
 };
 

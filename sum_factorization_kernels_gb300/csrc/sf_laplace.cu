@@ -1,10 +1,10 @@
 // sf_laplace.cu -- continuous FE Laplacian -div(kappa grad u) on hexahedral
 // meshes of degree 1..8: operator apply, geometry, kappa-gradient, diagonal.
 //
-// The operator apply itself lives in sf_laplace_line.cu (default, both
-// precisions) and sf_laplace_pair.cu (FP32x2 variant, on request); this file
-// holds the setup (geometry), diagonal and kappa-gradient kernels, which use
-// a cell pipeline with one block of CPB cells and block barriers.
+// The operator apply itself lives in sf_laplace_line.cu (both precisions,
+// structured and unstructured meshes); this file holds the setup
+// (geometry), diagonal and kappa-gradient kernels, which use a cell
+// pipeline with one block of CPB cells and block barriers.
 //
 // Per cell the operator is y_e = S^T (sum_d D_d^T t_d), t = kappa_q G_q D S x_e
 // (S: basis -> Gauss values, D: collocation derivative, G: merged
@@ -226,70 +226,6 @@ __global__ void __launch_bounds__(CellsPerBlock<N>::value *N *N)
       r = wq * (A.aff[0] * ux * gx[c] + A.aff[1] * uy * gy[c] + A.aff[2] * uz * gz[c]);
     }
     if (p.valid) A.y[p.cell * N3 + q] = r;
-  }
-}
-
-// Unstructured hexahedral mesh: node (a, b, z) of cell e is
-// idx[e n^3 + z n^2 + b n + a] (the caller's numbering carries each cell's
-// orientation); masks[e n^2 + (a + n b)] holds, for the column's n nodes,
-// bit z: the node is free (else homogeneous Dirichlet: read as zero, row
-// y = x) and bit 16 + z: a cell of an earlier colour already wrote it (add,
-// else store).  One launch per colour class of a greedy colouring; cells of
-// one class share no node.
-struct UnstrArgs {
-  const int *__restrict__ idx;
-  const unsigned *__restrict__ masks;
-  const int *__restrict__ cells;  // this colour's cells
-  long long count;
-};
-
-template <int N, typename T>
-__global__ void __launch_bounds__(CellsPerBlock<N>::value *N *N)
-    unstr_vmult_kernel(const __grid_constant__ ContArgs<N, T> A, const __grid_constant__ UnstrArgs U)
-{
-  constexpr int N2 = N * N, N3 = N * N * N;
-  constexpr int CPB = CellsPerBlock<N>::value;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *smem = reinterpret_cast<T *>(smem_raw);
-  const int tid = threadIdx.x;
-  const int cs = tid / N2;
-  const int t = tid - cs * N2;
-  const int a = t % N, b = t / N;
-  T *B0 = smem + cs * 4 * N3, *B1 = B0 + N3, *B2 = B1 + N3, *B3 = B2 + N3;
-  const long long ord = (long long)blockIdx.x * CPB + cs;
-  const bool valid = ord < U.count;
-  const long long cell = valid ? (long long)__ldg(U.cells + ord) : 0;
-  const unsigned msk = valid ? __ldg(U.masks + cell * N2 + t) : 0u;
-  int node[N];
-  T v[N];
-#pragma unroll
-  for (int c = 0; c < N; ++c) {
-    node[c] = valid ? __ldg(U.idx + cell * N3 + c * N2 + t) : 0;
-    v[c] = ((msk >> c) & 1u) ? __ldg(A.x + node[c]) : T(0);
-  }
-  cell_gradients<N, T>(A, v, B0, B1, B2, B3, t, a, b);
-  T tz[N];
-#pragma unroll
-  for (int c = 0; c < N; ++c) {
-    const int q = t + N2 * c;
-    const T ux = B0[q], uy = B2[q], uz = B3[q];
-    const T *G = A.geo + cell * A.geo_stride + q;
-    const T g0 = valid ? __ldg(G) : T(0), g1 = valid ? __ldg(G + N3) : T(0), g2 = valid ? __ldg(G + 2 * N3) : T(0),
-            g3 = valid ? __ldg(G + 3 * N3) : T(0), g4 = valid ? __ldg(G + 4 * N3) : T(0),
-            g5 = valid ? __ldg(G + 5 * N3) : T(0);
-    B0[q] = ux * g0 + uy * g3 + uz * g4;
-    B2[q] = ux * g3 + uy * g1 + uz * g5;
-    tz[c] = ux * g4 + uy * g5 + uz * g2;
-  }
-  cell_integrate<N, T>(A, tz, v, B0, B1, B2, t, a, b);
-  if (valid) {
-#pragma unroll
-    for (int c = 0; c < N; ++c) {
-      T val = v[c];
-      if ((msk >> (16 + c)) & 1u) val += A.y[node[c]];
-      if (!((msk >> c) & 1u)) val = __ldg(A.x + node[c]);
-      A.y[node[c]] = val;
-    }
   }
 }
 
@@ -608,11 +544,7 @@ int cont_kgrad_n(const sf_op *op, int prec, const void *u, const void *l, void *
 
 int launch_cont_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
 {
-  // unstructured meshes: the line kernel with index arrays by default, the
-  // block-barrier cell pipeline as the generic variant
-  if (op->desc.kind == SF_OP_LAPLACE_UNSTRUCTURED && op->kernel_variant == SF_KERNEL_CELL)
-    return launch_unstructured_vmult(op, prec, x, y, st);
-  if (pair_path(op, prec)) return launch_cont_vmult_pair(op, (const float *)x, (float *)y, st);
+  // structured and unstructured meshes: the packed line-ownership kernel
   return launch_cont_vmult_line(op, prec, x, y, st);
 }
 
@@ -623,44 +555,6 @@ int launch_cont_kappa_grad(const sf_op *op, int prec, const void *u, const void 
 }
 
 namespace {
-template <int N, typename T>
-int unstr_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
-{
-  constexpr int CPB = CellsPerBlock<N>::value;
-  constexpr int N3 = N * N * N;
-  const sf_unstructured &M = *op->unstr;
-  ContArgs<N, T> A = make_args<N, T>(op);
-  A.x = x;
-  A.y = y;
-  A.geo = (const T *)(sizeof(T) == 8 ? op->geo64.ptr : op->geo32.ptr);
-  A.geo_stride = 6 * N3;
-  if (!A.geo) {
-    set_error("unstructured mesh: geometry missing");
-    return SF_ERR_STATE;
-  }
-  const size_t smem = size_t(CPB) * 4 * N3 * sizeof(T);
-  SF_CUDA_TRY(cudaFuncSetAttribute(unstr_vmult_kernel<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  UnstrArgs U;
-  U.idx = (const int *)M.idx.ptr;
-  U.masks = (const unsigned *)M.masks.ptr;
-  for (size_t c = 0; c + 1 < M.color_start.size(); ++c) {
-    U.cells = (const int *)M.cells.ptr + M.color_start[c];
-    U.count = M.color_start[c + 1] - M.color_start[c];
-    if (U.count == 0) continue;
-    const long long blocks = (U.count + CPB - 1) / CPB;
-    unstr_vmult_kernel<N, T><<<dim3((unsigned)blocks), dim3(CPB * N * N), smem, st>>>(A, U);
-    SF_CUDA_TRY(cudaGetLastError());
-  }
-  return SF_OK;
-}
-
-template <int N>
-int unstr_vmult_n(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
-{
-  if (prec == SF_FP64) return unstr_vmult_impl<N, double>(op, (const double *)x, (double *)y, st);
-  return unstr_vmult_impl<N, float>(op, (const float *)x, (float *)y, st);
-}
-
 template <int N>
 int cont_diag_n(const sf_op *op, int prec, void *d, cudaStream_t st)
 {
@@ -668,21 +562,6 @@ int cont_diag_n(const sf_op *op, int prec, void *d, cudaStream_t st)
   return cont_diag_impl<N, float>(op, (float *)d, st);
 }
 } // namespace
-
-int launch_unstructured_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
-{
-  switch (op->n) {
-  case 2: return unstr_vmult_n<2>(op, prec, x, y, st);
-  case 3: return unstr_vmult_n<3>(op, prec, x, y, st);
-  case 4: return unstr_vmult_n<4>(op, prec, x, y, st);
-  case 5: return unstr_vmult_n<5>(op, prec, x, y, st);
-  case 6: return unstr_vmult_n<6>(op, prec, x, y, st);
-  case 7: return unstr_vmult_n<7>(op, prec, x, y, st);
-  case 8: return unstr_vmult_n<8>(op, prec, x, y, st);
-  case 9: return unstr_vmult_n<9>(op, prec, x, y, st);
-  default: set_error("unsupported degree"); return SF_ERR_UNSUPPORTED;
-  }
-}
 
 int launch_cont_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st)
 {
@@ -704,7 +583,7 @@ int launch_geometry(const sf_op *op, double *G, cudaStream_t st)
   A.deform = op->desc.deform;
   A.stride = op->geo_stride;
   A.G = G;
-  geometry_kernel<<<152 * 16, 256, 0, st>>>(A);
+  geometry_kernel<<<device_sm_count() * 16, 256, 0, st>>>(A);
   SF_CUDA_TRY(cudaGetLastError());
   return SF_OK;
 }

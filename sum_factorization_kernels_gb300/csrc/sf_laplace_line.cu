@@ -590,7 +590,7 @@ int line_pack_impl(sf_op *op, DevBuf &buf)
     if (n == 0) continue;
     const int cx = color & 1, cy = (color >> 1) & 1, cz = (color >> 2) & 1;
     const int mx = (nc[0] - cx + 1) / 2, my = (nc[1] - cy + 1) / 2;
-    const long long blocks = std::min<long long>((n + 255) / 256, 152 * 32);
+    const long long blocks = stream_grid(n, 256, 32);
     line_pack_geometry_kernel<N, T><<<(unsigned)blocks, 256>>>((const double *)op->geo64.ptr, op->geo_stride,
                                                               (T *)buf.ptr + base, n, count, nc[0], nc[1], cx,
                                                               cy, cz, mx, my, nullptr);
@@ -618,7 +618,7 @@ int line_unstr_pack_impl(sf_op *op, DevBuf &buf)
     const long long count = M.color_start[c + 1] - M.color_start[c];
     const long long n = (count + Cfg::K - 1) / Cfg::K * Cfg::GB;
     if (n == 0) continue;
-    const long long blocks = std::min<long long>((n + 255) / 256, 152 * 32);
+    const long long blocks = stream_grid(n, 256, 32);
     line_pack_geometry_kernel<N, T><<<(unsigned)blocks, 256>>>(
         (const double *)op->geo64.ptr, op->geo_stride, (T *)buf.ptr + base, n, count, 1, 1, 0, 0, 0, 1, 1,
         (const int *)M.cells.ptr + M.color_start[c]);

@@ -9,7 +9,6 @@ namespace sf {
 
 // sf_laplace.cu
 int launch_cont_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st);
-int launch_unstructured_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st);
 int launch_cont_kappa_grad(const sf_op *op, int prec, const void *u, const void *lam, void *dk,
                            cudaStream_t st);
 int launch_geometry(const sf_op *op, double *G, cudaStream_t st);
@@ -19,12 +18,6 @@ int launch_cont_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st)
 int launch_cont_vmult_line(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st);
 // walk-ordered copy of the FP64 geometry for the line kernel (geoLine64 / geoLine32)
 int pack_line_geometry(sf_op *op, int prec);
-
-// sf_laplace_pair.cu (FP32, two cells per thread in packed FP32x2)
-bool pair_path(const sf_op *op, int prec);
-int launch_cont_vmult_pair(const sf_op *op, const float *x, float *y, cudaStream_t st);
-int repack_pair_geometry(sf_op *op, const double *G64, long long s64, const double *kap64,
-                         cudaStream_t st);
 
 // sf_dg.cu
 int launch_dg_vmult(const sf_op *op, int prec, int nrhs, bool transpose, const void *x, void *y,
@@ -45,6 +38,12 @@ int launch_dg_precomputed_diagonal(const sf_op *op, int prec, void *diag, cudaSt
 
 // sf_cell_faces.cu: the DO_FACES cell operators (block diagonal, cell-major)
 int launch_cell_faces(const sf_op *op, int prec, int nrhs, const void *x, void *y, cudaStream_t st);
+
+// SM count of the current device (cached per device ordinal)
+int device_sm_count();
+// grid of a grid-stride kernel over n items: one block per `threads` items,
+// at most per_sm blocks per SM
+int stream_grid(long long n, int threads, int per_sm);
 
 // blocks of a kernel that fit on one SM with the maximum shared-memory
 // carveout: the occupancy calculator does not account for the carveout

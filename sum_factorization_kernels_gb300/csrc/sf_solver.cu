@@ -5,14 +5,23 @@
 //  * SF_SOLVE_MIXED: FP64 iterative refinement.  Each outer step forms the
 //    true residual r = b - A x with the FP64 operator, solves A d = r / |r|
 //    approximately with an FP32 preconditioned CG (FP32 operator, FP32
-//    vectors, FP64 reductions) and updates x += |r| d in FP64.
+//    vectors, FP64 reductions) and updates x += |r| d in FP64.  Each inner
+//    solve stops at the relative residual the outer iteration still needs
+//    (half of rtol |b| / |r|), but not below inner_rtol.
 //  * Preconditioners: none, Jacobi (inverse diagonal) or a Chebyshev
 //    polynomial of D^-1 A (the smoother form of the reference's fused
 //    Chebyshev step, evaluation_dg_laplacian.h:485-502) with lambda_max from
 //    a Lanczos estimate built out of the CG coefficients of a few Jacobi-CG
 //    steps, range [lambda_max / range, 1.2 lambda_max].
-//  * Scalars (alpha, beta, dot products) stay on the device; the host reads
-//    one residual norm per iteration to decide convergence.
+//  * Scalars (alpha, beta, dot products, the convergence flag) stay on the
+//    device.  Reductions are single-pass: fixed-size block partials, summed
+//    in block order by the last block to finish (deterministic).  The host
+//    never waits for the iteration it has just queued: it queues iteration
+//    k, then reads the scalars of iteration k-1 from pinned memory.  An
+//    iteration queued after convergence changes nothing, because the update
+//    kernels return when the device flag says the solve is done.
+//  * Work vectors and scalars are allocated once per handle and precision
+//    and kept with the preconditioner state.
 //  * Periodic DG SIPG has the constants as null space: with
 //    project_constant the right-hand side and every preconditioned residual
 //    are projected to mean zero.
@@ -34,27 +43,18 @@ constexpr int kBlocks = 1024; // fixed reduction grid: deterministic results
 
 struct Scalars {
   double rz, rz_old, pAp, rr, sum;
+  double tol2;        // the solve is done once rr <= tol2
+  int done;           // convergence or breakdown: update kernels return
+  int breakdown;      // non-positive curvature or non-finite residual
+  unsigned ticket;    // blocks finished in the running reduction
+  int pad;
 };
 
-int grid_for(long long n)
-{
-  long long g = (n + kThreads - 1) / kThreads;
-  if (g > 152 * 16) g = 152 * 16;
-  return (int)(g < 1 ? 1 : g);
-}
+int grid_for(long long n) { return stream_grid(n, kThreads, 16); }
 
-template <typename T>
-__global__ void dot2_partial(long long n, const T *__restrict__ r, const T *__restrict__ z,
-                             double *__restrict__ part)
+// block sum of two values per thread; the result is in s1[0], s2[0]
+__device__ __forceinline__ void block_sum2(double *s1, double *s2, double a, double b)
 {
-  __shared__ double s1[kThreads], s2[kThreads];
-  double a = 0, b = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const double ri = r[i];
-    a = fma(ri, double(z[i]), a);
-    b = fma(ri, ri, b);
-  }
   s1[threadIdx.x] = a;
   s2[threadIdx.x] = b;
   __syncthreads();
@@ -65,62 +65,78 @@ __global__ void dot2_partial(long long n, const T *__restrict__ r, const T *__re
     }
     __syncthreads();
   }
+}
+
+enum { RED_RZ = 0, RED_PAP = 1, RED_SUM = 2 };
+
+// single-pass reduction.  RED_RZ: rz = (a, b), rr = (a, a), convergence and
+// finiteness checks; RED_PAP: pAp = (a, b), curvature check; RED_SUM:
+// sum = sum(a).  The last block to finish sums the partials in block order.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kThreads) reduce_kernel(long long n, const T *__restrict__ a,
+                                                          const T *__restrict__ b, double *__restrict__ part,
+                                                          Scalars *sc)
+{
+  __shared__ double s1[kThreads], s2[kThreads];
+  __shared__ bool last;
+  double u = 0, v = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double ai = a[i];
+    if (MODE == RED_SUM) {
+      u += ai;
+    } else {
+      u = fma(ai, double(b[i]), u);
+      if (MODE == RED_RZ) v = fma(ai, ai, v);
+    }
+  }
+  block_sum2(s1, s2, u, v);
   if (threadIdx.x == 0) {
     part[2 * blockIdx.x] = s1[0];
     part[2 * blockIdx.x + 1] = s2[0];
+    __threadfence();
+    last = atomicAdd(&sc->ticket, 1u) == gridDim.x - 1;
   }
-}
-
-// slot: 0 -> rz (and rr), 1 -> pAp, 2 -> sum
-__global__ void dot2_final(const double *__restrict__ part, int nb, Scalars *sc, int slot)
-{
-  __shared__ double s1[kThreads], s2[kThreads];
-  double a = 0, b = 0;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    a += part[2 * i];
-    b += part[2 * i + 1];
-  }
-  s1[threadIdx.x] = a;
-  s2[threadIdx.x] = b;
   __syncthreads();
-  for (int w = kThreads / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) {
-      s1[threadIdx.x] += s1[threadIdx.x + w];
-      s2[threadIdx.x] += s2[threadIdx.x + w];
-    }
-    __syncthreads();
+  if (!last) return;
+  __threadfence();
+  u = 0;
+  v = 0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+    u += __ldcg(part + 2 * i);
+    v += __ldcg(part + 2 * i + 1);
   }
+  block_sum2(s1, s2, u, v);
   if (threadIdx.x == 0) {
-    if (slot == 0) {
+    if (MODE == RED_RZ) {
       sc->rz_old = sc->rz;
       sc->rz = s1[0];
       sc->rr = s2[0];
-    } else if (slot == 1) {
+      if (!isfinite(s2[0])) {
+        sc->breakdown = 1;
+        sc->done = 1;
+      } else if (s2[0] <= sc->tol2) {
+        sc->done = 1;
+      }
+    } else if (MODE == RED_PAP) {
       sc->pAp = s1[0];
+      if (!(s1[0] > 0.0)) {
+        sc->breakdown = 1;
+        sc->done = 1;
+      }
     } else {
       sc->sum = s1[0];
     }
+    sc->ticket = 0;
   }
 }
 
-template <typename T>
-__global__ void sum_partial(long long n, const T *__restrict__ x, double *__restrict__ part)
+__global__ void begin_solve_kernel(Scalars *sc, double tol2)
 {
-  __shared__ double s1[kThreads];
-  double a = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    a += double(x[i]);
-  s1[threadIdx.x] = a;
-  __syncthreads();
-  for (int w = kThreads / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) s1[threadIdx.x] += s1[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = s1[0];
-    part[2 * blockIdx.x + 1] = 0.0;
-  }
+  sc->tol2 = tol2;
+  sc->done = 0;
+  sc->breakdown = 0;
+  sc->ticket = 0;
 }
 
 template <typename T>
@@ -132,49 +148,56 @@ __global__ void subtract_mean(long long n, T *__restrict__ x, const Scalars *sc)
     x[i] -= m;
 }
 
-// x += alpha p, r -= alpha Ap with alpha = rz / pAp
-template <typename T>
-__global__ void update_xr(long long n, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
-                          const T *__restrict__ Ap, const Scalars *sc)
+enum { PC_NONE = 0, PC_JACOBI = 1, PC_CHEB = 2 };
+
+// x += alpha p, r -= alpha Ap (alpha = rz / pAp), then the first step of
+// the preconditioner on the new residual: z = D^-1 r (Jacobi) or z = s D^-1 r,
+// t = -z (first Chebyshev step from a zero start); nothing when done
+template <typename T, int PC>
+__global__ void update_xr_precond(long long n, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
+                                  const T *__restrict__ Ap, const T *__restrict__ dinv, T *__restrict__ z,
+                                  T *__restrict__ t, T s, const Scalars *sc)
 {
-  const double al = sc->rz / sc->pAp;
-  const T a = T(al);
+  if (sc->done) return;
+  const T a = T(sc->rz / sc->pAp);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     x[i] += a * p[i];
-    r[i] -= a * Ap[i];
+    const T ri = r[i] - a * Ap[i];
+    r[i] = ri;
+    if (PC == PC_JACOBI) z[i] = dinv[i] * ri;
+    if (PC == PC_CHEB) {
+      const T v = s * dinv[i] * ri;
+      z[i] = v;
+      t[i] = -v;
+    }
   }
 }
 
-// p = z + beta p, beta = rz / rz_old
+// p = z + beta p, beta = rz / rz_old; nothing when done
 template <typename T>
 __global__ void update_p(long long n, T *__restrict__ p, const T *__restrict__ z, const Scalars *sc)
 {
+  if (sc->done) return;
   const T be = T(sc->rz / sc->rz_old);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     p[i] = z[i] + be * p[i];
 }
 
-template <typename T>
-__global__ void mul_kernel(long long n, T *__restrict__ z, const T *__restrict__ d, const T *__restrict__ r,
-                           T s)
-{
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    z[i] = s * d[i] * r[i];
-}
-
-// z = s d r, t = -z (first Chebyshev step from a zero start)
-template <typename T>
-__global__ void cheb_first(long long n, T *__restrict__ z, T *__restrict__ t, const T *__restrict__ d,
-                           const T *__restrict__ r, T s)
+// first preconditioner step on a residual (outside the iteration)
+template <typename T, int PC>
+__global__ void precond_first(long long n, const T *__restrict__ r, const T *__restrict__ dinv, T *__restrict__ z,
+                              T *__restrict__ t, T s)
 {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const T v = s * d[i] * r[i];
-    z[i] = v;
-    t[i] = -v;
+    if (PC == PC_JACOBI) z[i] = dinv[i] * r[i];
+    if (PC == PC_CHEB) {
+      const T v = s * dinv[i] * r[i];
+      z[i] = v;
+      t[i] = -v;
+    }
   }
 }
 
@@ -186,17 +209,16 @@ __global__ void inverse_kernel(long long n, T *__restrict__ d)
     d[i] = d[i] != T(0) ? T(1) / d[i] : T(1);
 }
 
-// r = b - Ax  (FP64), also used to form scaled FP32 right-hand sides
-__global__ void residual_kernel(long long n, double *__restrict__ r, const double *__restrict__ b,
-                                const double *__restrict__ ax)
+template <typename T>
+__global__ void sub_kernel(long long n, T *__restrict__ r, const T *__restrict__ b, const T *__restrict__ ax)
 {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     r[i] = b[i] - ax[i];
 }
 
-__global__ void to_f32_scaled(long long n, float *__restrict__ y, const double *__restrict__ x,
-                              const Scalars *sc)
+// y = x / |r| in FP32 (the unit right-hand side of an inner solve)
+__global__ void to_f32_scaled(long long n, float *__restrict__ y, const double *__restrict__ x, const Scalars *sc)
 {
   const double s = 1.0 / sqrt(sc->rr);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -204,21 +226,20 @@ __global__ void to_f32_scaled(long long n, float *__restrict__ y, const double *
     y[i] = float(x[i] * s);
 }
 
-__global__ void add_f32_scaled(long long n, double *__restrict__ x, const float *__restrict__ d,
-                               const Scalars *sc)
+// x += scale d (scale = |r| of the outer step)
+__global__ void add_f32_scaled(long long n, double *__restrict__ x, const float *__restrict__ d, double scale)
 {
-  const double s = sqrt(sc->rr);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    x[i] += s * double(d[i]);
+    x[i] += scale * double(d[i]);
 }
 
 template <typename T>
-__global__ void sub_kernel(long long n, T *__restrict__ r, const T *__restrict__ b, const T *__restrict__ ax)
+__global__ void copy_kernel(long long n, T *__restrict__ y, const T *__restrict__ x)
 {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    r[i] = b[i] - ax[i];
+    y[i] = x[i];
 }
 
 template <typename T>
@@ -254,38 +275,82 @@ double tridiag_max_eig(const std::vector<double> &d, const std::vector<double> &
   return hi;
 }
 
+// CG work vectors of one precision
+struct Work {
+  DevBuf r, p, ap, z;
+  template <typename T>
+  int ensure(long long n)
+  {
+    const size_t b = sizeof(T) * (size_t)n;
+    int e;
+    if (r.bytes == b) return SF_OK;
+    if ((e = r.alloc(b)) || (e = p.alloc(b)) || (e = ap.alloc(b)) || (e = z.alloc(b))) return e;
+    return SF_OK;
+  }
+};
+
+// per-precision preconditioner state and work vectors, kept per handle
+struct PrecState {
+  DevBuf dinv, z2, t;
+  Work work;
+  double lambda_max = 0.0;
+  bool have_diag = false, have_eig = false;
+};
+
+// state of the solver kept per handle: preconditioners, work vectors,
+// device scalars, pinned host copies of the scalars
+struct SolverCache {
+  sf_op *op = nullptr;
+  PrecState st[2];
+  DevBuf part, scal, bcopy, r64, ax64, r32, d32;
+  Scalars *host = nullptr; // pinned ring of 2
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  ~SolverCache()
+  {
+    if (host) cudaFreeHost(host);
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  int init()
+  {
+    if (host) return SF_OK;
+    int r = part.alloc(sizeof(double) * 2 * kBlocks);
+    if (r) return r;
+    if ((r = scal.alloc(sizeof(Scalars)))) return r;
+    SF_CUDA_TRY(cudaMemset(scal.ptr, 0, sizeof(Scalars)));
+    for (auto &e : ev) SF_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    SF_CUDA_TRY(cudaMallocHost(&host, 2 * sizeof(Scalars)));
+    std::memset(host, 0, 2 * sizeof(Scalars));
+    return SF_OK;
+  }
+};
+
 struct Solver {
   sf_op *op;
   cudaStream_t st;
   long long n;
-  DevBuf part, scal;
+  SolverCache *cache;
   Scalars *sc = nullptr;
   double *part_d = nullptr;
-  Scalars *host_sc = nullptr; // pinned
   int applies = 0;
 
-  int init()
+  void bind()
   {
-    int r = part.alloc(sizeof(double) * 2 * kBlocks);
-    if (r) return r;
-    r = scal.alloc(sizeof(Scalars));
-    if (r) return r;
-    part_d = (double *)part.ptr;
-    sc = (Scalars *)scal.ptr;
-    SF_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(Scalars), st));
-    SF_CUDA_TRY(cudaMallocHost(&host_sc, sizeof(Scalars)));
-    return SF_OK;
-  }
-  ~Solver()
-  {
-    if (host_sc) cudaFreeHost(host_sc);
+    sc = (Scalars *)cache->scal.ptr;
+    part_d = (double *)cache->part.ptr;
   }
 
-  template <typename T>
-  int dot2(const T *r, const T *z, int slot)
+  template <typename T, int MODE>
+  int reduce(const T *a, const T *b)
   {
-    dot2_partial<T><<<kBlocks, kThreads, 0, st>>>(n, r, z, part_d);
-    dot2_final<<<1, kThreads, 0, st>>>(part_d, kBlocks, sc, slot);
+    reduce_kernel<T, MODE><<<kBlocks, kThreads, 0, st>>>(n, a, b, part_d, sc);
+    SF_CUDA_TRY(cudaGetLastError());
+    return SF_OK;
+  }
+
+  int begin(double tol2)
+  {
+    begin_solve_kernel<<<1, 1, 0, st>>>(sc, tol2);
     SF_CUDA_TRY(cudaGetLastError());
     return SF_OK;
   }
@@ -293,18 +358,35 @@ struct Solver {
   template <typename T>
   int project(T *x)
   {
-    sum_partial<T><<<kBlocks, kThreads, 0, st>>>(n, x, part_d);
-    dot2_final<<<1, kThreads, 0, st>>>(part_d, kBlocks, sc, 2);
+    int e = reduce<T, RED_SUM>(x, x);
+    if (e) return e;
     subtract_mean<T><<<grid_for(n), kThreads, 0, st>>>(n, x, sc);
     SF_CUDA_TRY(cudaGetLastError());
     return SF_OK;
   }
 
-  int read_scalars()
+  // queue a copy of the scalars into pinned slot `slot` and mark it
+  int post(int slot)
   {
-    SF_CUDA_TRY(cudaMemcpyAsync(host_sc, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
-    SF_CUDA_TRY(cudaStreamSynchronize(st));
+    SF_CUDA_TRY(cudaMemcpyAsync(cache->host + slot, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+    SF_CUDA_TRY(cudaEventRecord(cache->ev[slot], st));
     return SF_OK;
+  }
+
+  // wait for slot `slot` and return its scalars
+  int fetch(int slot, Scalars *out)
+  {
+    SF_CUDA_TRY(cudaEventSynchronize(cache->ev[slot]));
+    *out = cache->host[slot];
+    return SF_OK;
+  }
+
+  // synchronous read of the current scalars
+  int read(Scalars *out)
+  {
+    int e = post(0);
+    if (e) return e;
+    return fetch(0, out);
   }
 
   int vmult(int prec, const void *x, void *y)
@@ -312,13 +394,6 @@ struct Solver {
     ++applies;
     return sf_vmult(op, prec, x, y, st);
   }
-};
-
-// per-precision preconditioner state cached in the handle
-struct PrecState {
-  DevBuf dinv, z2, t;
-  double lambda_max = 0.0;
-  bool have_diag = false, have_eig = false;
 };
 
 template <typename T>
@@ -336,17 +411,19 @@ int ensure_diag(Solver &S, PrecState &P)
 }
 
 // lambda_max of D^-1 A from `steps` Jacobi-preconditioned CG iterations
+// (setup only: one host read per step)
 template <typename T>
 int ensure_eig(Solver &S, PrecState &P, int steps, bool proj)
 {
   if (P.have_eig) return SF_OK;
   const long long n = S.n;
-  DevBuf bx, rx, px, apx, zx;
   int e;
-  if ((e = bx.alloc(sizeof(T) * n)) || (e = rx.alloc(sizeof(T) * n)) || (e = px.alloc(sizeof(T) * n)) ||
-      (e = apx.alloc(sizeof(T) * n)) || (e = zx.alloc(sizeof(T) * n)))
-    return e;
-  T *r = (T *)rx.ptr, *p = (T *)px.ptr, *ap = (T *)apx.ptr, *z = (T *)zx.ptr, *x = (T *)bx.ptr;
+  if ((e = P.work.ensure<T>(n))) return e;
+  DevBuf bx;
+  if ((e = bx.alloc(sizeof(T) * n))) return e;
+  T *r = (T *)P.work.r.ptr, *p = (T *)P.work.p.ptr, *ap = (T *)P.work.ap.ptr, *z = (T *)P.work.z.ptr,
+    *x = (T *)bx.ptr;
+  const T *dinv = (const T *)P.dinv.ptr;
   // deterministic pseudo-random start vector: fractional parts of i * golden ratio
   {
     std::vector<T> h((size_t)std::min<long long>(n, 1 << 20));
@@ -358,29 +435,32 @@ int ensure_eig(Solver &S, PrecState &P, int steps, bool proj)
     SF_CUDA_TRY(cudaStreamSynchronize(S.st));
   }
   SF_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(T) * n, S.st));
+  if ((e = S.begin(0.0))) return e;
   if (proj && (e = S.project(r))) return e;
-  mul_kernel<T><<<grid_for(n), kThreads, 0, S.st>>>(n, z, (const T *)P.dinv.ptr, r, T(1));
+  precond_first<T, PC_JACOBI><<<grid_for(n), kThreads, 0, S.st>>>(n, r, dinv, z, nullptr, T(1));
   if (proj && (e = S.project(z))) return e;
-  SF_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(T) * n, cudaMemcpyDeviceToDevice, S.st));
-  if ((e = S.dot2(r, z, 0))) return e;
+  copy_kernel<T><<<grid_for(n), kThreads, 0, S.st>>>(n, p, z);
+  if ((e = S.reduce<T, RED_RZ>(r, z))) return e;
   std::vector<double> alpha, beta;
+  Scalars h;
   for (int it = 0; it < steps; ++it) {
     if ((e = S.vmult(prec_of<T>(), p, ap))) return e;
-    if ((e = S.dot2(p, ap, 1))) return e;
-    if ((e = S.read_scalars())) return e;
-    const double a = S.host_sc->rz / S.host_sc->pAp;
-    if (!(S.host_sc->pAp > 0) || !std::isfinite(a)) break;
+    if ((e = S.reduce<T, RED_PAP>(p, ap))) return e;
+    if ((e = S.read(&h))) return e;
+    const double a = h.rz / h.pAp;
+    if (h.done || !std::isfinite(a)) break;
     alpha.push_back(a);
-    update_xr<T><<<grid_for(n), kThreads, 0, S.st>>>(n, x, r, p, ap, S.sc);
-    mul_kernel<T><<<grid_for(n), kThreads, 0, S.st>>>(n, z, (const T *)P.dinv.ptr, r, T(1));
+    update_xr_precond<T, PC_JACOBI><<<grid_for(n), kThreads, 0, S.st>>>(n, x, r, p, ap, dinv, z, nullptr, T(1),
+                                                                         S.sc);
     if (proj && (e = S.project(z))) return e;
-    if ((e = S.dot2(r, z, 0))) return e;
-    if ((e = S.read_scalars())) return e;
-    const double b = S.host_sc->rz / S.host_sc->rz_old;
-    if (!std::isfinite(b) || S.host_sc->rz <= 0) break;
+    if ((e = S.reduce<T, RED_RZ>(r, z))) return e;
+    if ((e = S.read(&h))) return e;
+    const double b = h.rz / h.rz_old;
+    if (h.done || !std::isfinite(b) || h.rz <= 0) break;
     beta.push_back(b);
     update_p<T><<<grid_for(n), kThreads, 0, S.st>>>(n, p, z, S.sc);
   }
+  SF_CUDA_TRY(cudaGetLastError());
   if (alpha.empty()) {
     set_error("eigenvalue estimate failed (operator not positive)");
     return SF_ERR_BREAKDOWN;
@@ -397,113 +477,161 @@ int ensure_eig(Solver &S, PrecState &P, int steps, bool proj)
   return SF_OK;
 }
 
-// z = M r
-template <typename T>
-int apply_precond(Solver &S, PrecState &P, const sf_solve_opts &o, const T *r, T *z, bool proj)
+struct ChebCoef {
+  double theta, delta;
+};
+
+ChebCoef cheb_coef(const PrecState &P, const sf_solve_opts &o)
 {
-  const long long n = S.n;
-  int e;
-  if (o.precond == SF_PRECOND_NONE) {
-    SF_CUDA_TRY(cudaMemcpyAsync(z, r, sizeof(T) * n, cudaMemcpyDeviceToDevice, S.st));
-  } else if (o.precond == SF_PRECOND_JACOBI) {
-    mul_kernel<T><<<grid_for(n), kThreads, 0, S.st>>>(n, z, (const T *)P.dinv.ptr, r, T(1));
-  } else {
-    const double lmax = 1.2 * P.lambda_max, lmin = lmax / o.cheb_range;
-    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
-    T *t = (T *)P.t.ptr, *z2 = (T *)P.z2.ptr;
-    cheb_first<T><<<grid_for(n), kThreads, 0, S.st>>>(n, z, t, (const T *)P.dinv.ptr, r, T(1.0 / theta));
-    SF_CUDA_TRY(cudaGetLastError());
-    double rho_old = delta / theta;
-    T *cur = z, *nxt = z2;
-    for (int k = 1; k < o.cheb_degree; ++k) {
-      const double rho = 1.0 / (2.0 * theta / delta - rho_old);
-      ++S.applies;
-      e = sf_chebyshev_step(S.op, prec_of<T>(), r, P.dinv.ptr, cur, nxt, t, 2.0 * rho / delta,
-                            rho * rho_old, S.st);
-      if (e) return e;
-      rho_old = rho;
-      T *tmp = cur;
-      cur = nxt;
-      nxt = tmp;
-    }
-    if (cur != z) SF_CUDA_TRY(cudaMemcpyAsync(z, cur, sizeof(T) * n, cudaMemcpyDeviceToDevice, S.st));
-  }
-  SF_CUDA_TRY(cudaGetLastError());
-  if (proj) return S.project(z);
-  return SF_OK;
+  const double lmax = 1.2 * P.lambda_max, lmin = lmax / o.cheb_range;
+  return ChebCoef{0.5 * (lmax + lmin), 0.5 * (lmax - lmin)};
 }
 
-// CG work vectors of one precision
-struct Work {
-  DevBuf r, p, ap, z;
-  template <typename T>
-  int alloc(long long n)
-  {
-    int e;
-    if ((e = r.alloc(sizeof(T) * n)) || (e = p.alloc(sizeof(T) * n)) || (e = ap.alloc(sizeof(T) * n)) ||
-        (e = z.alloc(sizeof(T) * n)))
-      return e;
-    return SF_OK;
+// the Chebyshev steps after the first (which the caller fused into its
+// residual update): z = p_k(D^-1 A) D^-1 r
+template <typename T>
+int cheb_rest(Solver &S, PrecState &P, const sf_solve_opts &o, const T *r, T *z)
+{
+  const ChebCoef c = cheb_coef(P, o);
+  T *t = (T *)P.t.ptr, *z2 = (T *)P.z2.ptr;
+  double rho_old = c.delta / c.theta;
+  T *cur = z, *nxt = z2;
+  for (int k = 1; k < o.cheb_degree; ++k) {
+    const double rho = 1.0 / (2.0 * c.theta / c.delta - rho_old);
+    ++S.applies;
+    const int e = sf_chebyshev_step(S.op, prec_of<T>(), r, P.dinv.ptr, cur, nxt, t, 2.0 * rho / c.delta,
+                                    rho * rho_old, S.st);
+    if (e) return e;
+    rho_old = rho;
+    T *tmp = cur;
+    cur = nxt;
+    nxt = tmp;
   }
-};
+  if (cur != z) {
+    copy_kernel<T><<<grid_for(S.n), kThreads, 0, S.st>>>(S.n, z, cur);
+    SF_CUDA_TRY(cudaGetLastError());
+  }
+  return SF_OK;
+}
 
 // preconditioned CG on A x = b (vectors of type T, x holds the start);
-// stops when |r| <= tol_abs or after max_iter iterations
+// stops when |r| <= tol_abs or after max_iter iterations.  In FP32 the
+// recursively updated residual can stall above a tolerance close to the
+// precision: the inner solves of the refinement also stop once |r| has not
+// halved over kStall iterations (the outer step continues from there).
+constexpr int kStall = 100;
+
 template <typename T>
-int pcg(Solver &S, PrecState &P, Work &W, const sf_solve_opts &o, const T *b, T *x, double tol_abs,
-        int max_iter, bool proj, int &iters, double &rr_final)
+int pcg(Solver &S, PrecState &P, const sf_solve_opts &o, const T *b, T *x, double tol_abs, int max_iter,
+        bool proj, int &iters, double &rr_final)
 {
   const long long n = S.n;
+  const int g = grid_for(n);
   int e;
-  T *r = (T *)W.r.ptr, *p = (T *)W.p.ptr, *ap = (T *)W.ap.ptr, *z = (T *)W.z.ptr;
+  Work &W = P.work;
+  T *r = (T *)W.r.ptr, *p = (T *)W.p.ptr, *ap = (T *)W.ap.ptr;
+  T *z = o.precond == SF_PRECOND_NONE ? r : (T *)W.z.ptr;
+  T *t = (T *)P.t.ptr;
+  const T *dinv = (const T *)P.dinv.ptr;
+  const T s0 = o.precond == SF_PRECOND_CHEBYSHEV ? T(1.0 / cheb_coef(P, o).theta) : T(1);
+  if ((e = S.begin(tol_abs * tol_abs))) return e;
+  // r = b - A x, z = M r, p = z
   if ((e = S.vmult(prec_of<T>(), x, ap))) return e;
-  sub_kernel<T><<<grid_for(n), kThreads, 0, S.st>>>(n, r, b, ap);
-  SF_CUDA_TRY(cudaGetLastError());
+  sub_kernel<T><<<g, kThreads, 0, S.st>>>(n, r, b, ap);
   if (proj && (e = S.project(r))) return e;
-  if ((e = apply_precond<T>(S, P, o, r, z, proj))) return e;
-  SF_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(T) * n, cudaMemcpyDeviceToDevice, S.st));
-  if ((e = S.dot2(r, z, 0))) return e;
-  if ((e = S.read_scalars())) return e;
-  iters = 0;
-  rr_final = S.host_sc->rr;
-  while (iters < max_iter && std::sqrt(S.host_sc->rr) > tol_abs) {
-    if ((e = S.vmult(prec_of<T>(), p, ap))) return e;
-    if ((e = S.dot2(p, ap, 1))) return e;
-    update_xr<T><<<grid_for(n), kThreads, 0, S.st>>>(n, x, r, p, ap, S.sc);
-    if ((e = apply_precond<T>(S, P, o, r, z, proj))) return e;
-    if ((e = S.dot2(r, z, 0))) return e;
-    update_p<T><<<grid_for(n), kThreads, 0, S.st>>>(n, p, z, S.sc);
-    SF_CUDA_TRY(cudaGetLastError());
-    ++iters;
-    if ((e = S.read_scalars())) return e;
-    if (!(S.host_sc->pAp > 0) || !std::isfinite(S.host_sc->rr)) {
-      set_error("CG breakdown (non-positive curvature or non-finite residual)");
-      return SF_ERR_BREAKDOWN;
-    }
-    rr_final = S.host_sc->rr;
+  if (o.precond == SF_PRECOND_JACOBI)
+    precond_first<T, PC_JACOBI><<<g, kThreads, 0, S.st>>>(n, r, dinv, z, t, s0);
+  if (o.precond == SF_PRECOND_CHEBYSHEV) {
+    precond_first<T, PC_CHEB><<<g, kThreads, 0, S.st>>>(n, r, dinv, z, t, s0);
+    if ((e = cheb_rest<T>(S, P, o, r, z))) return e;
   }
+  if (proj && z != r && (e = S.project(z))) return e;
+  copy_kernel<T><<<g, kThreads, 0, S.st>>>(n, p, z);
+  if ((e = S.reduce<T, RED_RZ>(r, z))) return e;
+  Scalars h;
+  if ((e = S.read(&h))) return e;
+  iters = 0;
+  rr_final = h.rr;
+  if (h.breakdown) {
+    set_error("CG breakdown (non-finite residual)");
+    return SF_ERR_BREAKDOWN;
+  }
+  if (h.done) return SF_OK;
+  double best = h.rr;
+  int best_k = 0;
+  // iterations, queued one ahead of the host's convergence check
+  for (int k = 0; k < max_iter; ++k) {
+    if ((e = S.vmult(prec_of<T>(), p, ap))) return e;
+    if ((e = S.reduce<T, RED_PAP>(p, ap))) return e;
+    if (o.precond == SF_PRECOND_NONE)
+      update_xr_precond<T, PC_NONE><<<g, kThreads, 0, S.st>>>(n, x, r, p, ap, dinv, z, t, s0, S.sc);
+    else if (o.precond == SF_PRECOND_JACOBI)
+      update_xr_precond<T, PC_JACOBI><<<g, kThreads, 0, S.st>>>(n, x, r, p, ap, dinv, z, t, s0, S.sc);
+    else
+      update_xr_precond<T, PC_CHEB><<<g, kThreads, 0, S.st>>>(n, x, r, p, ap, dinv, z, t, s0, S.sc);
+    SF_CUDA_TRY(cudaGetLastError());
+    if (o.precond == SF_PRECOND_CHEBYSHEV && (e = cheb_rest<T>(S, P, o, r, z))) return e;
+    if (proj && z != r && (e = S.project(z))) return e;
+    if ((e = S.reduce<T, RED_RZ>(r, z))) return e;
+    update_p<T><<<g, kThreads, 0, S.st>>>(n, p, z, S.sc);
+    SF_CUDA_TRY(cudaGetLastError());
+    if ((e = S.post(k & 1))) return e;
+    if (k > 0) {
+      if ((e = S.fetch((k - 1) & 1, &h))) return e;
+      if (h.done) {
+        iters = k; // iteration k was queued after convergence and changed nothing
+        break;
+      }
+      if (h.rr < 0.25 * best) {
+        best = h.rr;
+        best_k = k;
+      } else if (sizeof(T) == 4 && k - best_k > kStall) {
+        iters = k + 1;
+        break;
+      }
+    }
+    iters = k + 1;
+  }
+  if ((e = S.read(&h))) return e;
+  if (h.breakdown) {
+    set_error("CG breakdown (non-positive curvature or non-finite residual)");
+    return SF_ERR_BREAKDOWN;
+  }
+  rr_final = h.rr;
   return SF_OK;
 }
 
-} // namespace
-
-// preconditioner caches live beside the handle (keyed by handle address)
-namespace {
-struct PrecCache {
-  sf_op *op;
-  PrecState st[2];
-};
-std::vector<PrecCache *> g_caches;
+// solver caches live beside the handle (keyed by handle address)
+std::vector<SolverCache *> g_caches;
 std::mutex g_cache_mutex;
 
-PrecState &prec_state(sf_op *op, int prec)
+SolverCache *solver_cache(sf_op *op)
 {
   std::lock_guard<std::mutex> lock(g_cache_mutex);
   for (auto *c : g_caches)
-    if (c->op == op) return c->st[prec];
-  g_caches.push_back(new PrecCache{op, {}});
-  return g_caches.back()->st[prec];
+    if (c->op == op) return c;
+  auto *c = new SolverCache();
+  c->op = op;
+  g_caches.push_back(c);
+  return c;
 }
+
+template <typename T>
+int prepare_precision(Solver &S, PrecState &P, const sf_solve_opts &o, bool proj)
+{
+  int e;
+  if ((e = P.work.ensure<T>(S.n))) return e;
+  if (o.precond != SF_PRECOND_NONE && (e = ensure_diag<T>(S, P))) return e;
+  if (o.precond == SF_PRECOND_CHEBYSHEV) {
+    if ((e = ensure_eig<T>(S, P, o.eig_iterations, proj))) return e;
+    const size_t b = sizeof(T) * (size_t)S.n;
+    if (P.t.bytes != b && ((e = P.t.alloc(b)) || (e = P.z2.alloc(b)))) return e;
+  }
+  return SF_OK;
+}
+
+int ensure_buf(DevBuf &d, size_t bytes) { return d.bytes == bytes ? SF_OK : d.alloc(bytes); }
+
 } // namespace
 
 void release_solver_cache(sf_op *op)
@@ -531,7 +659,7 @@ extern "C" void sf_solve_opts_default(sf_solve_opts *o)
   o->eig_iterations = 12;
   o->rtol = 1e-10;
   o->max_iter = 2000;
-  o->inner_rtol = 1e-3;
+  o->inner_rtol = 1e-6;
   o->project_constant = 0;
 }
 
@@ -549,7 +677,7 @@ extern "C" int sf_cg_solve(sf_op *op, const double *b, double *x, const sf_solve
   }
   if (o.precond < SF_PRECOND_NONE || o.precond > SF_PRECOND_CHEBYSHEV || o.cheb_degree < 1 ||
       o.cheb_degree > 64 || !(o.cheb_range > 1.0) || !(o.rtol > 0) || o.max_iter < 1 ||
-      o.eig_iterations < 2 || o.eig_iterations > 200) {
+      o.eig_iterations < 2 || o.eig_iterations > 200 || !(o.inner_rtol > 0 && o.inner_rtol < 1)) {
     set_error("invalid solver options");
     return SF_ERR_INVALID;
   }
@@ -567,98 +695,89 @@ extern "C" int sf_cg_solve(sf_op *op, const double *b, double *x, const sf_solve
   S.op = op;
   S.st = st;
   S.n = op->n_dofs;
-  int e = S.init();
+  S.cache = solver_cache(op);
+  int e = S.cache->init();
   if (e) return e;
+  S.bind();
   const bool proj = o.project_constant != 0;
   const long long n = S.n;
+  const int g = grid_for(n);
+  const bool mixed = o.mode == SF_SOLVE_MIXED;
+  PrecState &P = S.cache->st[mixed ? 1 : 0];
+  // buffers and preconditioner setup (cached per handle) before the clock
+  SolverCache &Cc = *S.cache;
+  if ((e = ensure_buf(Cc.bcopy, sizeof(double) * n)) || (e = ensure_buf(Cc.r64, sizeof(double) * n)) ||
+      (e = ensure_buf(Cc.ax64, sizeof(double) * n)))
+    return e;
+  if (mixed) {
+    if ((e = ensure_buf(Cc.r32, sizeof(float) * n)) || (e = ensure_buf(Cc.d32, sizeof(float) * n))) return e;
+    if ((e = prepare_precision<float>(S, P, o, proj))) return e;
+  } else {
+    if ((e = prepare_precision<double>(S, P, o, proj))) return e;
+  }
   SF_CUDA_TRY(cudaStreamSynchronize(st));
+  S.applies = 0;
   const auto t0 = std::chrono::steady_clock::now();
 
   // |b| (after projection of a copy when requested)
-  DevBuf bb;
-  if ((e = bb.alloc(sizeof(double) * n))) return e;
-  double *bp = (double *)bb.ptr;
+  double *bp = (double *)Cc.bcopy.ptr;
   SF_CUDA_TRY(cudaMemcpyAsync(bp, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  if ((e = S.begin(0.0))) return e;
   if (proj && (e = S.project(bp))) return e;
   if (proj && (e = S.project(x))) return e;
-  if ((e = S.dot2(bp, bp, 0))) return e;
-  if ((e = S.read_scalars())) return e;
-  const double bnorm = std::sqrt(S.host_sc->rr);
+  if ((e = S.reduce<double, RED_RZ>(bp, bp))) return e;
+  Scalars h;
+  if ((e = S.read(&h))) return e;
+  const double bnorm = std::sqrt(h.rr);
   int total_iters = 0, outer = 0;
   double relres = 0.0;
   if (bnorm == 0.0) {
     SF_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
-  } else if (o.mode == SF_SOLVE_FP64) {
-    PrecState &P = prec_state(op, 0);
-    if (o.precond != SF_PRECOND_NONE && (e = ensure_diag<double>(S, P))) return e;
-    if (o.precond == SF_PRECOND_CHEBYSHEV) {
-      if ((e = ensure_eig<double>(S, P, o.eig_iterations, proj))) return e;
-      if (P.t.bytes < sizeof(double) * n && ((e = P.t.alloc(sizeof(double) * n)) || (e = P.z2.alloc(sizeof(double) * n))))
-        return e;
-    }
+  } else if (!mixed) {
     double rr;
-    Work W;
-    if ((e = W.alloc<double>(n))) return e;
-    if ((e = pcg<double>(S, P, W, o, bp, x, o.rtol * bnorm, o.max_iter, proj, total_iters, rr))) return e;
+    if ((e = pcg<double>(S, P, o, bp, x, o.rtol * bnorm, o.max_iter, proj, total_iters, rr))) return e;
   } else {
-    PrecState &P = prec_state(op, 1);
-    if (o.precond != SF_PRECOND_NONE && (e = ensure_diag<float>(S, P))) return e;
-    if (o.precond == SF_PRECOND_CHEBYSHEV) {
-      if ((e = ensure_eig<float>(S, P, o.eig_iterations, proj))) return e;
-      if (P.t.bytes < sizeof(float) * n && ((e = P.t.alloc(sizeof(float) * n)) || (e = P.z2.alloc(sizeof(float) * n))))
-        return e;
-    }
-    DevBuf rb, axb, r32b, d32b;
-    if ((e = rb.alloc(sizeof(double) * n)) || (e = axb.alloc(sizeof(double) * n)) ||
-        (e = r32b.alloc(sizeof(float) * n)) || (e = d32b.alloc(sizeof(float) * n)))
-      return e;
-    double *r = (double *)rb.ptr, *ax = (double *)axb.ptr;
-    float *r32 = (float *)r32b.ptr, *d32 = (float *)d32b.ptr;
-    Work W;
-    if ((e = W.alloc<float>(n))) return e;
+    double *r = (double *)Cc.r64.ptr, *ax = (double *)Cc.ax64.ptr;
+    float *r32 = (float *)Cc.r32.ptr, *d32 = (float *)Cc.d32.ptr;
     const int max_outer = 60;
     while (outer < max_outer) {
       if ((e = S.vmult(SF_FP64, x, ax))) return e;
-      residual_kernel<<<grid_for(n), kThreads, 0, st>>>(n, r, bp, ax);
+      sub_kernel<double><<<g, kThreads, 0, st>>>(n, r, bp, ax);
       if (proj && (e = S.project(r))) return e;
-      if ((e = S.dot2(r, r, 0))) return e;
-      if ((e = S.read_scalars())) return e;
-      const double rn = std::sqrt(S.host_sc->rr);
+      if ((e = S.begin(0.0))) return e;
+      if ((e = S.reduce<double, RED_RZ>(r, r))) return e;
+      if ((e = S.read(&h))) return e;
+      const double rn = std::sqrt(h.rr);
       if (!std::isfinite(rn)) {
         set_error("non-finite residual");
         return SF_ERR_BREAKDOWN;
       }
       if (rn <= o.rtol * bnorm || total_iters >= o.max_iter) break;
-      to_f32_scaled<<<grid_for(n), kThreads, 0, st>>>(n, r32, r, S.sc);
+      to_f32_scaled<<<g, kThreads, 0, st>>>(n, r32, r, S.sc);
       SF_CUDA_TRY(cudaMemsetAsync(d32, 0, sizeof(float) * n, st));
-      // keep |r| for the back-scaling: stash it in sum slot via a tiny copy
-      Scalars keep = *S.host_sc;
+      // the inner solve reduces its unit residual as far as this outer
+      // step still needs (with a factor 2 of margin), not below inner_rtol
+      const double inner = std::fmax(o.inner_rtol, std::fmin(0.5, 0.5 * o.rtol * bnorm / rn));
       int it = 0;
       double rr32;
-      // inner tolerance relative to the unit right-hand side; never ask for
-      // more than FP32 can deliver
-      const double inner = std::fmax(o.inner_rtol, 1e-6);
-      if ((e = pcg<float>(S, P, W, o, r32, d32, inner, o.max_iter - total_iters, proj, it, rr32))) return e;
+      if ((e = pcg<float>(S, P, o, r32, d32, inner, o.max_iter - total_iters, proj, it, rr32))) return e;
       total_iters += it;
-      // restore |r|^2 into the device scalars for the back-scaling
-      SF_CUDA_TRY(cudaMemcpyAsync(&S.sc->rr, &keep.rr, sizeof(double), cudaMemcpyHostToDevice, st));
-      add_f32_scaled<<<grid_for(n), kThreads, 0, st>>>(n, x, d32, S.sc);
+      add_f32_scaled<<<g, kThreads, 0, st>>>(n, x, d32, rn);
       SF_CUDA_TRY(cudaGetLastError());
-      SF_CUDA_TRY(cudaStreamSynchronize(st));
       ++outer;
       if (it == 0) break; // no progress possible
     }
   }
   // final true residual in FP64
   {
-    DevBuf rb, axb;
-    if ((e = rb.alloc(sizeof(double) * n)) || (e = axb.alloc(sizeof(double) * n))) return e;
-    if ((e = S.vmult(SF_FP64, x, axb.ptr))) return e;
-    residual_kernel<<<grid_for(n), kThreads, 0, st>>>(n, (double *)rb.ptr, bp, (const double *)axb.ptr);
-    if (proj && (e = S.project((double *)rb.ptr))) return e;
-    if ((e = S.dot2((double *)rb.ptr, (double *)rb.ptr, 0))) return e;
-    if ((e = S.read_scalars())) return e;
-    relres = bnorm > 0 ? std::sqrt(S.host_sc->rr) / bnorm : 0.0;
+    double *r = (double *)Cc.r64.ptr, *ax = (double *)Cc.ax64.ptr;
+    if ((e = S.vmult(SF_FP64, x, ax))) return e;
+    sub_kernel<double><<<g, kThreads, 0, st>>>(n, r, bp, ax);
+    if (proj && (e = S.project(r))) return e;
+    if ((e = S.begin(0.0))) return e;
+    if ((e = S.reduce<double, RED_RZ>(r, r))) return e;
+    if ((e = S.read(&h))) return e;
+    relres = bnorm > 0 ? std::sqrt(h.rr) / bnorm : 0.0;
   }
   SF_CUDA_TRY(cudaStreamSynchronize(st));
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -666,7 +785,7 @@ extern "C" int sf_cg_solve(sf_op *op, const double *b, double *x, const sf_solve
     stats->iterations = total_iters;
     stats->outer_iterations = outer;
     stats->rel_residual = relres;
-    stats->lambda_max = prec_state(op, o.mode == SF_SOLVE_MIXED ? 1 : 0).lambda_max;
+    stats->lambda_max = P.lambda_max;
     stats->seconds = secs;
     stats->operator_applies = S.applies;
   }

@@ -8,21 +8,41 @@
 #include "sf_launch.h"
 
 #include <algorithm>
+#include <atomic>
 
 namespace sf {
+
+int device_sm_count()
+{
+  // cached per device ordinal (attribute queries are host-side only)
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (dev >= 0 && dev < 64) {
+    const int c = cache[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) return 1;
+  if (dev >= 0 && dev < 64) cache[dev].store(n, std::memory_order_relaxed);
+  return n;
+}
+
+int stream_grid(long long n, int threads, int per_sm)
+{
+  long long g = (n + threads - 1) / threads;
+  const long long cap = (long long)device_sm_count() * per_sm;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
 
 namespace {
 
 constexpr int kThreads = 256;
 
-int grid_for(long long n)
-{
-  // enough resident blocks to cover the 152 SMs several times over
-  long long g = (n + kThreads - 1) / kThreads;
-  if (g > 152 * 16) g = 152 * 16;
-  if (g < 1) g = 1;
-  return (int)g;
-}
+// enough resident blocks to cover the SMs several times over
+int grid_for(long long n) { return stream_grid(n, kThreads, 16); }
 
 template <typename S, typename D>
 __global__ void convert_kernel(long long n, const S *__restrict__ x, D *__restrict__ y)

@@ -26,7 +26,7 @@ OP_LAPLACE_FACES, OP_CONVECTION_FACES = 7, 8   # DO_FACES builds, cell-major vec
 BASIS_GLL, BASIS_HERMITE = 0, 1
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2
-KERNEL_AUTO, KERNEL_GENERIC, KERNEL_PAIR, KERNEL_CELL = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_GENERIC = 0, 1
 
 EXPORTS = [
     "sf_last_error", "sf_version", "sf_create", "sf_destroy", "sf_sizes", "sf_set_geometry",

@@ -73,12 +73,8 @@ def main(argv=None) -> None:
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--transpose", action="store_true", help="time the transposed apply")
-    ap.add_argument("--variant", choices=["auto", "pair", "cell"], default="auto",
-                    help="kernel variant of the continuous apply (sf_set_kernel_variant)")
     a = ap.parse_args(argv)
     op = make_operator(a.kind, a.degree, a.ncells)
-    if a.variant != "auto":
-        op.set_kernel_variant({"pair": sf.KERNEL_PAIR, "cell": sf.KERNEL_CELL}[a.variant])
     dt = torch.float32 if a.prec == "fp32" else torch.float64
     n = op.n_dofs
     g = torch.Generator(device="cuda").manual_seed(1)

@@ -96,9 +96,7 @@ def test_unstructured_single_cell(p):
     for dm in (None, d2):
         ref = O.unstructured_apply(p, O.BASIS_GLL, i2[None], g2[None], N, x, dm)
         op = sf.Operator.unstructured(p, i2[None], g2[None], N, dirichlet=dm)
-        for variant in (sf.KERNEL_AUTO, sf.KERNEL_CELL):
-            op.set_kernel_variant(variant)
-            _check(torch, op, x, ref, p)
+        _check(torch, op, x, ref, p)
 
 
 def test_batch_of_one_equals_single_apply():

@@ -128,8 +128,7 @@ def test_symmetry_and_boundary_rows_large():
 @pytest.mark.parametrize("case", ["deformed", "kappa", "affine", "neumann_odd"])
 def test_fp32_kernels_vs_fp64(p, case):
     """the packed FP32 line kernel (several cells per warp group, so odd and
-    unit cell counts leave partly filled groups) and the FP32x2 pair kernel
-    against the FP64 apply"""
+    unit cell counts leave partly filled groups) against the FP64 apply"""
     torch = torch_cuda()
     sf = _sf()
     nc = {"deformed": (7, 6, 5), "kappa": (5, 4, 6), "affine": (6, 5, 3), "neumann_odd": (1, 3, 5)}[case]
@@ -143,12 +142,10 @@ def test_fp32_kernels_vs_fp64(p, case):
     y64 = torch.empty_like(x64)
     op.vmult(x64, y64)
     x = x64.float()
-    for variant in (sf.KERNEL_AUTO, sf.KERNEL_PAIR):
-        op.set_kernel_variant(variant)
-        y = torch.full_like(x, float("nan"))
-        op.vmult(x, y)
-        torch.cuda.synchronize()
-        assert rel(to_np(y), to_np(y64)) < FP32_TOL[p], variant
+    y = torch.full_like(x, float("nan"))
+    op.vmult(x, y)
+    torch.cuda.synchronize()
+    assert rel(to_np(y), to_np(y64)) < FP32_TOL[p]
     assert op.device_status() == 0
 
 
@@ -163,32 +160,10 @@ def test_fp32_full_size_vs_fp64():
     y64 = torch.empty_like(x64)
     op.vmult(x64, y64)
     x32 = x64.float()
-    for variant in (sf.KERNEL_AUTO, sf.KERNEL_GENERIC, sf.KERNEL_PAIR):
+    for variant in (sf.KERNEL_AUTO, sf.KERNEL_GENERIC):
         op.set_kernel_variant(variant)
         for _ in range(2):
             y32 = torch.full_like(x32, float("nan"))
             op.vmult(x32, y32)
             assert float((y32.double() - y64).norm() / y64.norm()) < 3e-7
-    assert op.device_status() == 0
-
-
-@pytest.mark.parametrize("p", [5, 6, 7, 8])
-def test_fp32_pair_kernel_matches_generic_high_degree(p):
-    """paired FP32x2 kernel vs the line kernel for degrees 5..8 (odd cell
-    counts so that colours end with an unpaired cell), with kappa"""
-    torch = torch_cuda()
-    sf = _sf()
-    op = sf.Operator(sf.OP_LAPLACE, degree=p, n_cells=(5, 3, 3), deform=0.05)
-    rng = np.random.default_rng(p)
-    x = to_dev(torch, rng.uniform(-1, 1, op.n_dofs), torch.float32)
-    for kappa in (False, True):
-        if kappa:
-            op.set_coefficient(to_dev(torch, np.exp(0.5 * rng.standard_normal(op.n_cells * (p + 1) ** 3)),
-                                      torch.float64))
-        y_gen, y_pair = torch.empty_like(x), torch.empty_like(x)
-        op.set_kernel_variant(sf.KERNEL_GENERIC)
-        op.vmult(x, y_gen)
-        op.set_kernel_variant(sf.KERNEL_PAIR)
-        op.vmult(x, y_pair)
-        assert rel(to_np(y_pair), to_np(y_gen)) < 2e-6
     assert op.device_status() == 0

@@ -49,15 +49,13 @@ def test_unstructured_vs_oracle_and_structured(p):
     ref2 = O.unstructured_apply(p, O.BASIS_GLL, idx2, G2, N, x2, d2)
     op = sf.Operator.unstructured(p, idx2, G2, N, dirichlet=d2)
     st = sf.Operator(sf.OP_LAPLACE, degree=p, n_cells=(4, 3, 3), length=(1.0, 0.7, 0.9), deform=0.05)
-    for variant in (sf.KERNEL_AUTO, sf.KERNEL_CELL):   # line kernel with index arrays, cell pipeline
-        op.set_kernel_variant(variant)
-        for dtype, tol in ((torch.float64, FP64_TOL), (torch.float32, 2 * FP32_TOL[p])):
-            y = torch.full((N,), float("nan"), dtype=dtype, device="cuda:0")
-            op.vmult(to_dev(torch, x2, dtype), y)
-            assert rel(to_np(y), ref2) < tol, (variant, dtype)
-            ys = torch.empty(N, dtype=dtype, device="cuda:0")
-            st.vmult(to_dev(torch, x, dtype), ys)
-            assert rel(to_np(y)[perm], to_np(ys)) < tol, (variant, dtype)
+    for dtype, tol in ((torch.float64, FP64_TOL), (torch.float32, 2 * FP32_TOL[p])):
+        y = torch.full((N,), float("nan"), dtype=dtype, device="cuda:0")
+        op.vmult(to_dev(torch, x2, dtype), y)
+        assert rel(to_np(y), ref2) < tol, dtype
+        ys = torch.empty(N, dtype=dtype, device="cuda:0")
+        st.vmult(to_dev(torch, x, dtype), ys)
+        assert rel(to_np(y)[perm], to_np(ys)) < tol, dtype
     assert op.device_status() == 0
 
 
