@@ -168,18 +168,21 @@ int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, voi
                                void *stream);
 
 /* The transposed advection apply of sf_vmult_transpose_batched() for callers
- * that cannot allocate device memory while they run -- for example code
- * inside a stream capture, where cudaMalloc is not allowed, or code with its
- * own memory pool.  No counterpart in the reference.  The intermediate
+ * that cannot allocate device memory while they run: applications that hand
+ * out all device memory from their own pool or reserve a fixed budget up
+ * front, and loops that cannot take the device synchronisation an
+ * allocation implies.  No counterpart in the reference.  The intermediate
  * vector of the inverse-mass form comes from a 4 MiB array compiled into the
  * library (reserved on every GPU that loads it, until process exit) instead
  * of a cudaMalloc'd buffer; this function allocates nothing.  Only for
  * SF_OP_DG_ADVECT handles; nrhs * n_dofs * element size must not exceed
  * 4 MiB (SF_ERR_INVALID otherwise).  The first call on a device looks up the
- * array's device address once; make that first call before any stream
- * capture.  All calls share the array (nothing in it needs to start at
- * zero), so calls whose work overlaps on the GPU race: keep them on one
- * stream or synchronise between them. */
+ * array's device address once, and the first call with each degree and
+ * precision loads that kernel; make those first calls before any stream
+ * capture.  The address is not looked up again after cudaDeviceReset().
+ * All calls share the array (nothing in it needs to start at zero), so
+ * calls whose work overlaps on the GPU race: keep them on one stream or
+ * synchronise between them. */
 int sf_vmult_transpose_static(sf_op *op, int prec, int nrhs, const void *x, void *y,
                               void *stream);
 
@@ -280,6 +283,27 @@ void sf_solve_opts_default(sf_solve_opts *opts);
  * reference counterpart: the reference has no solver.  Synchronous. */
 int sf_cg_solve(sf_op *op, const double *b, double *x, const sf_solve_opts *opts,
                 sf_solve_stats *stats, void *stream);
+
+/* ---------------- design measurements ---------------- */
+/* The slab sweeps of the operator kernels in isolation: n_cells cells of
+ * (degree+1)^3 values (cell-major, x fastest) are loaded into shared memory,
+ * `rounds` times the interpolation matrix S (Gauss points of the GLL basis)
+ * is applied along x and then along y, and the result is written to out.
+ * method selects the arithmetic: SF_SWEEP_EO_FP32 / SF_SWEEP_EO_FP64 the
+ * CUDA-core even-odd contraction of the operator kernels (one thread per
+ * line), SF_SWEEP_MMA_TF32X3 the tensor cores (mma.sync m16n8k8, TF32
+ * operands split into high part and remainder, three products, FP32
+ * accumulation), SF_SWEEP_MMA_TF32 one TF32 product.  in/out are float
+ * (double for SF_SWEEP_EO_FP64).  No reference counterpart: it measures the
+ * choice between the two arithmetic units for matrix_vector_kernel.h:30-185. */
+typedef enum {
+  SF_SWEEP_EO_FP32 = 0,
+  SF_SWEEP_MMA_TF32X3 = 1,
+  SF_SWEEP_MMA_TF32 = 2,
+  SF_SWEEP_EO_FP64 = 3
+} sf_sweep_method;
+int sf_sweep_benchmark(int degree, int method, long long n_cells, int rounds, const void *in, void *out,
+                       void *stream);
 
 /* ---------------- utilities ---------------- */
 /* FP64 <-> FP32 vector conversion */

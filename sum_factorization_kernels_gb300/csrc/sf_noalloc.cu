@@ -4,13 +4,12 @@
 // K^T M^-1, runs in two passes and needs an intermediate vector between
 // them.  sf_vmult_transpose_batched() keeps that vector in a per-handle
 // device buffer that it allocates with cudaMalloc on first use.  Some
-// callers cannot allow that: code that runs while a stream is being
-// captured into a CUDA graph (cudaMalloc is not capturable), code whose
-// memory is handed out by its own pool and must not see a foreign
-// allocation appear mid-run, and real-time loops where an allocation's
-// implicit device synchronisation is not acceptable.  For them,
-// sf_vmult_transpose_static() takes the intermediate vector from a fixed
-// device array compiled into this library instead.
+// callers cannot allow that: applications that hand out all device memory
+// from their own pool or reserve a fixed budget up front, and must not see
+// a foreign allocation appear mid-run, and time-stepping loops where an
+// allocation's implicit device synchronisation is not acceptable.  For
+// them, sf_vmult_transpose_static() takes the intermediate vector from a
+// fixed device array compiled into this library instead.
 //
 // The array holds kStaticScratchBytes (4 MiB).  Every GPU that loads the
 // library reserves it until the process exits.  All calls share it and it
@@ -36,7 +35,10 @@ std::mutex g_scratch_mutex;
 void *g_scratch_ptr[kMaxDevices] = {};
 
 // device address of g_static_scratch on the current device; looked up once
-// per device (the name is only a host-side stand-in, not a device address)
+// per device (the name is only a host-side stand-in, not a device address).
+// The table is not refreshed after cudaDeviceReset(), which unloads the
+// library's module: a process that resets a device must not call this entry
+// point on that device again.
 int scratch_address(void **out)
 {
   int dev = 0;

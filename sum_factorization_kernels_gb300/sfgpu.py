@@ -27,6 +27,7 @@ BASIS_GLL, BASIS_HERMITE = 0, 1
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_CHEBYSHEV = 0, 1, 2
 KERNEL_AUTO, KERNEL_GENERIC = 0, 1
+SWEEP_EO_FP32, SWEEP_MMA_TF32X3, SWEEP_MMA_TF32, SWEEP_EO_FP64 = 0, 1, 2, 3
 
 EXPORTS = [
     "sf_last_error", "sf_version", "sf_create", "sf_destroy", "sf_sizes", "sf_set_geometry",
@@ -34,7 +35,7 @@ EXPORTS = [
     "sf_vmult_transpose_batched", "sf_chebyshev_step", "sf_vector_update", "sf_diagonal",
     "sf_kappa_gradient", "sf_solve_opts_default", "sf_cg_solve", "sf_convert", "sf_dot",
     "sf_shape_tables", "sf_set_kernel_variant", "sf_device_status", "sf_vmult_transpose_static",
-    "sf_rk_stage", "sf_lsrk_step", "sf_create_unstructured",
+    "sf_rk_stage", "sf_lsrk_step", "sf_create_unstructured", "sf_sweep_benchmark",
 ]
 
 
@@ -102,6 +103,7 @@ def lib():
         L.sf_device_status.argtypes = [vp, C.POINTER(i)]
         L.sf_rk_stage.argtypes = [vp, i, i, vp, vp, vp, vp, d, d, vp]
         L.sf_lsrk_step.argtypes = [vp, i, i, vp, vp, vp, d, vp]
+        L.sf_sweep_benchmark.argtypes = [i, i, ll, i, vp, vp, vp]
         _lib = L
     return _lib
 

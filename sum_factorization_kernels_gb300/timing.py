@@ -9,6 +9,11 @@ as cell-node index arrays and per-cell geometry) or ``faces`` /
 ``convection_faces`` (the DO_FACES cell operators on cell-major vectors).  Prints one line with the
 apply rate summed over the right-hand sides and the vector traffic it implies.
 Used to drive profiler captures of one kernel on a small case.
+
+KIND ``sweeps`` times the shared-memory slab sweeps alone (sf_sweep_benchmark)
+with the CUDA-core even-odd contraction in FP32 and FP64 and with the tensor
+cores (TF32 x3 and TF32), on ncells^3 cells of (degree+1)^3 values, and
+prints each rate and each FP32 path's relative error against the FP64 path.
 """
 from __future__ import annotations
 
@@ -62,10 +67,45 @@ def make_operator(kind: str, degree: int, ncells: int):
     raise ValueError("unknown operator kind %r" % kind)
 
 
+def sweeps(degree: int, ncells: int, rounds: int, reps: int, warmup: int) -> None:
+    n3 = (degree + 1) ** 3
+    cells = ncells ** 3
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x64 = torch.rand(cells * n3, device="cuda", dtype=torch.float64, generator=g) * 2 - 1
+    x32 = x64.float()
+    x64 = x32.double()
+    results = {}
+    for name, method, x in (("eo_fp64", sf.SWEEP_EO_FP64, x64), ("eo_fp32", sf.SWEEP_EO_FP32, x32),
+                            ("mma_tf32x3", sf.SWEEP_MMA_TF32X3, x32), ("mma_tf32", sf.SWEEP_MMA_TF32, x32)):
+        y = torch.empty_like(x)
+
+        def run():
+            sf.check(sf.lib().sf_sweep_benchmark(degree, method, cells, rounds, x.data_ptr(), y.data_ptr(),
+                                                 torch.cuda.current_stream().cuda_stream))
+
+        for _ in range(warmup):
+            run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            run()
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / reps
+        results[name] = (t, y)
+    ref = results["eo_fp64"][1]
+    for name, (t, y) in results.items():
+        err = float((y.double() - ref).norm() / ref.norm())
+        # values swept per second: every round sweeps all values along x and along y
+        print("sweeps p=%d %d^3 cells rounds=%d %-10s %.3f ms  %.1f G line-values/s  rel. error vs FP64 %.2e"
+              % (degree, ncells, rounds, name, t * 1e3, 2 * rounds * cells * n3 / t / 1e9, err))
+
+
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("kind", choices=["laplace", "sipg", "advect", "precomputed", "mass", "convection",
-                                     "unstructured", "faces", "convection_faces"])
+                                     "unstructured", "faces", "convection_faces", "sweeps"])
     ap.add_argument("--degree", type=int, default=4)
     ap.add_argument("--ncells", type=int, default=32, help="cells per direction")
     ap.add_argument("--prec", choices=["fp32", "fp64"], default="fp32")
@@ -73,7 +113,11 @@ def main(argv=None) -> None:
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--transpose", action="store_true", help="time the transposed apply")
+    ap.add_argument("--rounds", type=int, default=16, help="sweeps: x and y sweeps per round")
     a = ap.parse_args(argv)
+    if a.kind == "sweeps":
+        sweeps(a.degree, a.ncells, a.rounds, a.reps, a.warmup)
+        return
     op = make_operator(a.kind, a.degree, a.ncells)
     dt = torch.float32 if a.prec == "fp32" else torch.float64
     n = op.n_dofs

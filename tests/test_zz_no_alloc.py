@@ -1,7 +1,7 @@
 """sf_vmult_transpose_static: the transposed advection apply for callers that
-cannot allocate device memory while they run (stream capture, own memory
-pools).  Its intermediate vector lives in a fixed 4 MiB array inside the
-library.  The results must match sf_vmult_transpose_batched, which uses a
+cannot allocate device memory while they run (applications that hand out all
+device memory from their own pool or a fixed budget).  Its intermediate
+vector lives in a fixed 4 MiB array inside the library.  The results must match sf_vmult_transpose_batched, which uses a
 cudaMalloc'd buffer, on two calls in a row (the shared array keeps the
 previous call's contents), and sizes beyond the array must be refused.
 
