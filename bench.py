@@ -74,6 +74,15 @@ def measured_peaks():
 def host_cpu():
     model = platform.processor() or platform.machine()
     try:
+        import subprocess
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name:"):
+                return {"machine": platform.machine(), "model": line.split(":", 1)[1].strip(),
+                        "nproc": os.cpu_count()}
+    except (OSError, ValueError, subprocess.SubprocessError):
+        pass
+    try:
         with open("/proc/cpuinfo") as f:
             for line in f:
                 key = line.split(":")[0].strip().lower()

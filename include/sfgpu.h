@@ -231,11 +231,17 @@ int sf_diagonal(sf_op *op, int prec, void *diag, void *stream);
 int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void *dkappa,
                       void *stream);
 
-/* Kernel selection for the continuous Laplacian apply.  SF_KERNEL_AUTO and
- * SF_KERNEL_GENERIC: the packed line-ownership kernel (one thread per line
- * of a cell, several cells per warp group) for both precisions, structured
- * or unstructured.  Other values are rejected with SF_ERR_INVALID.  No
- * reference counterpart. */
+/* Kernel selection.  Continuous Laplacian: SF_KERNEL_AUTO and
+ * SF_KERNEL_GENERIC both select the packed line-ownership kernel (one
+ * thread per line of a cell, several cells per warp group), structured or
+ * unstructured.  SF_OP_DG_SIPG: SF_KERNEL_AUTO evaluates the operator in its
+ * tensor-product form (on these Cartesian meshes the SIPG bilinear form is
+ * exactly L (x) M (x) M + M (x) L (x) M + M (x) M (x) L with 1D stiffness-
+ * plus-face matrices L of penalty * (p+1)^2 and 1D mass matrices M: the
+ * kernel of SF_OP_DG_PRECOMPUTED), SF_KERNEL_GENERIC the cell-and-face
+ * kernel that follows the reference's EvaluationDGLaplacian step by step;
+ * both give the same operator to rounding.  Other values are rejected with
+ * SF_ERR_INVALID.  No reference counterpart. */
 typedef enum {
   SF_KERNEL_AUTO = 0,
   SF_KERNEL_GENERIC = 1

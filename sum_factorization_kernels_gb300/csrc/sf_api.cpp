@@ -66,6 +66,15 @@ int check_prec(const sf_op *op, int prec)
 
 bool is_cell_faces(int kind) { return kind == SF_OP_LAPLACE_FACES || kind == SF_OP_CONVECTION_FACES; }
 
+// operators evaluated by the tensor-product kernel: the precomputed SIPG
+// form, and the SIPG operator itself unless the cell-and-face kernel is
+// selected (the two are the same Kronecker sum on Cartesian meshes)
+bool tensor_form(const sf_op *op)
+{
+  return op->desc.kind == SF_OP_DG_PRECOMPUTED ||
+         (op->desc.kind == SF_OP_DG_SIPG && op->kernel_variant != SF_KERNEL_GENERIC);
+}
+
 bool is_continuous(int kind)
 {
   return kind == SF_OP_LAPLACE || kind == SF_OP_MASS || kind == SF_OP_CONVECTION ||
@@ -425,7 +434,7 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
   const Region region(op->region_mv);
   if (is_continuous(op->desc.kind)) return launch_cont_vmult(op, prec, x, y, st);
   if (is_cell_faces(op->desc.kind)) return launch_cell_faces(op, prec, 1, x, y, st);
-  if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
+  if (tensor_form(op))
     return launch_dg_precomputed(op, prec, 1, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
   return launch_dg_vmult(op, prec, 1, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
 }
@@ -457,7 +466,7 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
     return SF_OK;
   }
   if (is_cell_faces(op->desc.kind)) return launch_cell_faces(op, prec, nrhs, x, y, st);
-  if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
+  if (tensor_form(op))
     return launch_dg_precomputed(op, prec, nrhs, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
   return launch_dg_vmult(op, prec, nrhs, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
 }
@@ -500,10 +509,9 @@ int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv, 
     return fail(SF_ERR_UNSUPPORTED, "Chebyshev steps: not for the face-term operators");
   cudaStream_t st = (cudaStream_t)stream;
   const Region region(op->region_ch);
+  if (tensor_form(op)) return launch_dg_precomputed(op, prec, 1, x_old, x_new, b, diag_inv, t, c_np, c_tm, st);
   if (op->desc.kind == SF_OP_DG_SIPG || op->desc.kind == SF_OP_DG_ADVECT)
     return launch_dg_vmult(op, prec, 1, false, x_old, x_new, b, diag_inv, t, c_np, c_tm, st);
-  if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
-    return launch_dg_precomputed(op, prec, 1, x_old, x_new, b, diag_inv, t, c_np, c_tm, st);
   // continuous: operator into x_new, then the fused vector update in place
   SF_RET(launch_cont_vmult(op, prec, x_old, x_new, st));
   return launch_vector_update(op->n_dofs, prec, x_new, b, diag_inv, x_old, x_new, t, c_np, c_tm, st);
@@ -578,8 +586,7 @@ int sf_diagonal(sf_op *op, int prec, void *diag, void *stream)
       op->desc.kind == SF_OP_LAPLACE_UNSTRUCTURED || is_cell_faces(op->desc.kind))
     return fail(SF_ERR_UNSUPPORTED, "diagonal: structured Laplacian and DG operators only");
   if (op->desc.kind == SF_OP_LAPLACE) return launch_cont_diagonal(op, prec, diag, (cudaStream_t)stream);
-  if (op->desc.kind == SF_OP_DG_PRECOMPUTED)
-    return launch_dg_precomputed_diagonal(op, prec, diag, (cudaStream_t)stream);
+  if (tensor_form(op)) return launch_dg_precomputed_diagonal(op, prec, diag, (cudaStream_t)stream);
   return launch_dg_diagonal(op, prec, diag, (cudaStream_t)stream);
 }
 

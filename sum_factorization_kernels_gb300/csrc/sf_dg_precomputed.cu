@@ -13,6 +13,15 @@
 // evaluates iv0 and iv1 at swapped face points (which makes them vanish),
 // this library uses the couplings of the SIPG bilinear form.
 //
+// The general SIPG operator of SF_OP_DG_SIPG (sf_dg.cu, the reference's
+// EvaluationDGLaplacian with tau = penalty (p+1)^2 / h_d) is the same
+// Kronecker sum on these Cartesian meshes: its cell and face integrals are
+// exact in the tangential directions (Gauss quadrature with n points on
+// degree-p products), so they factor into 1D stiffness-plus-face matrices
+// and 1D mass matrices, with the 1D penalty penalty (p+1)^2 instead of
+// p(p+1).  SF_OP_DG_SIPG handles evaluate it with this kernel by default
+// (SF_KERNEL_AUTO); SF_KERNEL_GENERIC selects the cell-and-face kernel.
+//
 // GPU mapping as in sf_dg.cu: CPB consecutive cells per block, n^2 threads
 // per cell, z columns read and written straight from the cell-major vector,
 // three padded slabs per cell.  Five phases, four block barriers:
@@ -261,7 +270,7 @@ struct Matrices1D {
   double M[kMaxN][kMaxN], L[kMaxN][kMaxN], iv0, iv1;
 };
 
-Matrices1D precomputed_matrices(const Shape1D &s)
+Matrices1D precomputed_matrices(const Shape1D &s, double pen)
 {
   const int n = s.n;
   Matrices1D R{};
@@ -278,7 +287,6 @@ Matrices1D precomputed_matrices(const Shape1D &s)
       dq[q][i] = t;
     }
   }
-  const double pen = double(s.degree) * (s.degree + 1);
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) {
       double m = 0.0, l = 0.0;
@@ -296,12 +304,21 @@ Matrices1D precomputed_matrices(const Shape1D &s)
   return R;
 }
 
+// 1D penalty in reference coordinates: p(p+1) for the reference's
+// PrecomputedDGLaplacian, penalty (p+1)^2 for the SIPG operator
+double tensor_penalty(const sf_op *op)
+{
+  const double p = op->desc.degree;
+  if (op->desc.kind == SF_OP_DG_SIPG) return op->desc.penalty * (p + 1) * (p + 1);
+  return p * (p + 1);
+}
+
 template <int N, typename T>
 int precomputed_impl(const sf_op *op, int nrhs, const T *x, T *y, const T *cb, const T *cdinv, T *ct,
                      double c_np, double c_tm, cudaStream_t st)
 {
   using Cfg = PDGCfg<N, T>;
-  const Matrices1D mats = precomputed_matrices(op->shape);
+  const Matrices1D mats = precomputed_matrices(op->shape, tensor_penalty(op));
   PDGArgs<N, T> A{};
   A.M = make_eo<N, T>([&](int i, int j) { return mats.M[i][j]; });
   A.L = make_eo<N, T>([&](int i, int j) { return mats.L[i][j]; });
@@ -366,7 +383,7 @@ int launch_dg_precomputed(const sf_op *op, int prec, int nrhs, const void *x, vo
 // the diagonal), computed in FP64 on the host and broadcast to all cells
 int launch_dg_precomputed_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st)
 {
-  const Matrices1D m = precomputed_matrices(op->shape);
+  const Matrices1D m = precomputed_matrices(op->shape, tensor_penalty(op));
   const int n = op->n, n3 = n * n * n;
   const double vol = op->h[0] * op->h[1] * op->h[2];
   double c[3];

@@ -47,6 +47,43 @@ def test_sipg_chebyshev_golden(golden):
 
 
 @pytest.mark.parametrize("p", range(1, 9))
+@pytest.mark.parametrize("penalty", [1.0, 2.5])
+def test_sipg_tensor_form_equals_cell_face_kernel(p, penalty):
+    """SF_OP_DG_SIPG evaluated in tensor-product form (default) and by the
+    cell-and-face kernel: the same operator, the same Chebyshev step and
+    diagonal, both against the oracle (anisotropic cells, 1-cell-thick y)"""
+    torch = torch_cuda()
+    sf = _sf()
+    nc, h = (4, 1, 3), (0.3, 0.2, 0.45)
+    op = sf.Operator(sf.OP_DG_SIPG, degree=p, n_cells=nc, length=_lengths(nc, h), penalty=penalty)
+    g = O.dg(p, nc, h, penalty=penalty)
+    rng = np.random.default_rng(p)
+    x = rng.standard_normal(op.n_dofs)
+    y_ref = O.dg_sipg_apply(g, x)
+    d_ref = O.dg_sipg_diagonal(g)
+    out = {}
+    for variant in (sf.KERNEL_AUTO, sf.KERNEL_GENERIC):
+        op.set_kernel_variant(variant)
+        for dtype, tol in ((torch.float64, FP64_TOL), (torch.float32, 4 * FP32_TOL[p])):
+            xd = to_dev(torch, x, dtype)
+            y = torch.empty_like(xd)
+            op.vmult(xd, y)
+            assert rel(to_np(y), y_ref) < tol, (variant, dtype)
+            d = torch.empty_like(xd)
+            op.diagonal(d)
+            assert rel(to_np(d), d_ref) < tol, (variant, dtype)
+        b = to_dev(torch, rng.standard_normal(op.n_dofs), torch.float64)
+        dinv = 1.0 / to_dev(torch, d_ref, torch.float64)
+        t = to_dev(torch, rng.standard_normal(op.n_dofs), torch.float64)
+        xn = torch.empty_like(b)
+        op.chebyshev_step(b, dinv, to_dev(torch, x, torch.float64), xn, t, 0.7, 0.3)
+        out[variant] = (to_np(xn), to_np(t))
+    assert rel(out[sf.KERNEL_AUTO][0], out[sf.KERNEL_GENERIC][0]) < FP64_TOL
+    assert rel(out[sf.KERNEL_AUTO][1], out[sf.KERNEL_GENERIC][1]) < FP64_TOL
+    assert op.device_status() == 0
+
+
+@pytest.mark.parametrize("p", range(1, 9))
 def test_advect_golden(golden, p):
     torch = torch_cuda()
     sf = _sf()

@@ -171,3 +171,47 @@ def test_unstructured_equals_structured(p, basis):
     d2[perm_nodes] = dmask
     y2 = O.unstructured_apply(p, basis, idx2, G2, N, x2, d2)
     assert np.abs(y2[perm_nodes] - y).max() < 1e-13 * np.abs(y).max()
+
+
+@pytest.mark.parametrize("p", [1, 2, 5, 8])
+@pytest.mark.parametrize("penalty", [1.0, 2.5])
+def test_sipg_is_kronecker_sum(p, penalty):
+    """On a periodic Cartesian mesh the SIPG operator (tau = penalty (p+1)^2
+    / h_d) is L (x) M (x) M + M (x) L (x) M + M (x) M (x) L with 1D periodic
+    DG stiffness-plus-face matrices L of 1D penalty penalty (p+1)^2 and 1D
+    mass matrices M: the identity behind evaluating SF_OP_DG_SIPG with the
+    tensor-product kernel"""
+    n = p + 1
+    sh = O.shape_arrays(p, O.BASIS_HERMITE)
+    S, D, w = sh["S"], sh["D"], sh["wq"]
+    v0, v1 = sh["face_v"][0] @ S, sh["face_v"][1] @ S
+    d0, d1 = sh["face_d"][0] @ S, sh["face_d"][1] @ S
+    dq = D @ S
+    pen = penalty * (p + 1) ** 2
+    M = (S * w[:, None]).T @ S
+    L = ((dq * w[:, None]).T @ dq + pen * np.outer(v0, v0) + 0.5 * (np.outer(d0, v0) + np.outer(v0, d0))
+         + pen * np.outer(v1, v1) - 0.5 * (np.outer(d1, v1) + np.outer(v1, d1)))
+    C = -pen * np.outer(v0, v1) - 0.5 * np.outer(d0, v1) + 0.5 * np.outer(v0, d1)   # cell <- left neighbour
+    nc, h = (3, 4, 2), (1 / 3, 0.25, 0.5)
+
+    def lap1d(m, hh):
+        A = np.zeros((m * n, m * n))
+        for e in range(m):
+            l, r = (e - 1) % m, (e + 1) % m
+            A[e * n:(e + 1) * n, e * n:(e + 1) * n] += L / hh
+            A[e * n:(e + 1) * n, l * n:(l + 1) * n] += C / hh
+            A[e * n:(e + 1) * n, r * n:(r + 1) * n] += C.T / hh
+        return A
+
+    Ad = [lap1d(nc[d], h[d]) for d in range(3)]
+    Md = [np.kron(np.eye(nc[d]), M * h[d]) for d in range(3)]
+    x = np.random.default_rng(p).standard_normal(int(np.prod(nc)) * n ** 3)
+    T = x.reshape(nc[2], nc[1], nc[0], n, n, n).transpose(0, 3, 1, 4, 2, 5).reshape(nc[2] * n, nc[1] * n, nc[0] * n)
+
+    def app(Ax, Ay, Az):
+        return np.einsum("ai,zyi->zya", Ax, np.einsum("bj,zjx->zbx", Ay, np.einsum("ck,kyx->cyx", Az, T)))
+
+    Y = app(Ad[0], Md[1], Md[2]) + app(Md[0], Ad[1], Md[2]) + app(Md[0], Md[1], Ad[2])
+    y = Y.reshape(nc[2], n, nc[1], n, nc[0], n).transpose(0, 2, 4, 1, 3, 5).ravel()
+    ys = O.dg_sipg_apply(O.dg(p, nc, h, penalty=penalty), x)
+    assert np.linalg.norm(y - ys) / np.linalg.norm(ys) < 1e-13
