@@ -388,13 +388,28 @@ int launch_dg_precomputed_diagonal(const sf_op *op, int prec, void *diag, cudaSt
   const double vol = op->h[0] * op->h[1] * op->h[2];
   double c[3];
   for (int d = 0; d < 3; ++d) c[d] = vol / (op->h[d] * op->h[d]);
+  // 1D diagonals; a direction one cell thick is its own periodic neighbour,
+  // and at n = 2 the couplings with the neighbour's end layers then land on
+  // the diagonal (targets 0, 1, n-2, n-1 of the coupling terms)
+  double ld[3][kMaxN];
+  for (int d = 0; d < 3; ++d) {
+    for (int i = 0; i < n; ++i) ld[d][i] = m.L[i][i];
+    if (op->desc.n_cells[d] != 1) continue;
+    const struct {
+      int target, source;
+      double coef;
+    } cpl[6] = {{0, n - 1, m.iv0}, {0, n - 2, m.iv1}, {1, n - 1, m.iv1},
+                {n - 1, 0, m.iv0}, {n - 1, 1, m.iv1}, {n - 2, 0, m.iv1}};
+    for (const auto &e : cpl)
+      if (e.target == e.source) ld[d][e.target] += e.coef;
+  }
   double pat[kMaxN * kMaxN * kMaxN];
   float patf[kMaxN * kMaxN * kMaxN];
   for (int k = 0; k < n; ++k)
     for (int j = 0; j < n; ++j)
       for (int i = 0; i < n; ++i) {
-        const double v = c[0] * m.L[i][i] * m.M[j][j] * m.M[k][k] + c[1] * m.M[i][i] * m.L[j][j] * m.M[k][k] +
-                         c[2] * m.M[i][i] * m.M[j][j] * m.L[k][k];
+        const double v = c[0] * ld[0][i] * m.M[j][j] * m.M[k][k] + c[1] * m.M[i][i] * ld[1][j] * m.M[k][k] +
+                         c[2] * m.M[i][i] * m.M[j][j] * ld[2][k];
         pat[(k * n + j) * n + i] = v;
         patf[(k * n + j) * n + i] = float(v);
       }
