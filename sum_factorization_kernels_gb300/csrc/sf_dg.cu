@@ -755,7 +755,7 @@ int launch_dg_inverse_mass(const sf_op *op, int prec, int nrhs, const void *x, v
 //          + jf (ij phi_i'(0) phi_i(0) + tau phi_i(0)^2
 //                - ij phi_i'(1) phi_i(1) + tau phi_i(1)^2)
 // (the own-cell part of the face terms; neighbour couplings are off the
-// diagonal).  Computed on the host in FP64 and broadcast to all cells.
+// diagonal except along a direction one cell thick).  Computed on the host in FP64 and broadcast to all cells.
 // Advection has no diagonal preconditioner use; it gets the same formula's
 // analogue: sum_d of the cell-diagonal of M^-1 K along d is not provided.
 int launch_dg_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st)
@@ -791,6 +791,10 @@ int launch_dg_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st)
       const double ij = 1.0 / op->h[d], jf = jxw * ij;
       const double tau = op->desc.penalty * n * n * ij;
       K[d][i] = ij * ij * jxw * k + jf * (ij * d0 * v0 + tau * v0 * v0 - ij * d1 * v1 + tau * v1 * v1);
+      // a direction one cell thick is its own periodic neighbour on both
+      // faces: the couplings with the neighbour's end values (left: trial at
+      // 1, test at 0; right: the mirror) then contribute to the diagonal
+      if (op->desc.n_cells[d] == 1) K[d][i] += jf * (-2.0 * tau * v0 * v1 - ij * d0 * v1 + ij * v0 * d1);
     }
   }
   double pat[kMaxN * kMaxN * kMaxN];

@@ -13,9 +13,10 @@
 // The grid is persistent: a group walks a strided list of the colour's
 // cells, K consecutive ordinals per step.  The geometry is stored in the
 // order of that walk (a copy of the natural [cell][6][n^3] tensors made at
-// setup): per colour class, blocks of K ordinals, each block [6][n][K n^2]
-// so that lane t reads word c K n^2 + t of each component (consecutive
-// lanes, consecutive words: no bank conflicts).  The next step's block is
+// setup): per colour class, blocks of K ordinals, each block
+// [n][3][K n^2][2] (point, component pair, lane, pair member) so that lane
+// t reads three 2-wide words per point (consecutive lanes, consecutive
+// pairs: no bank conflicts).  The next step's block is
 // fetched by one TMA bulk copy right after the quadrature-point operation
 // of the current step (one mbarrier per group, bounded wait).  Summation: 8
 // colour launches, first-touch store / add, programmatic dependent launch
@@ -25,6 +26,8 @@
 // the strides of the three slabs come from a search of the shared-memory
 // bank conflicts of the access patterns for each (n, W, K); slab B2, read
 // and written only along y lines and z columns, has a layout of its own.
+#include <type_traits>
+
 #include "sf_cont_column.cuh"
 #include "sf_device.cuh"
 #include "sf_internal.h"
@@ -431,9 +434,12 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
         const T gx = B0[s], gy = B2[zc2 + L2.SZ * c];
         T tx, ty, tzc;
         if (DEFORMED) {
-          constexpr int GC = N * Cfg::KN2; // component stride of the block
-          const T *Gq = geo_s + c * Cfg::KN2 + tt;
-          const T g0 = Gq[0], g1 = Gq[GC], g2 = Gq[2 * GC], g3 = Gq[3 * GC], g4 = Gq[4 * GC], g5 = Gq[5 * GC];
+          // component pairs (xx, yy), (zz, xy), (xz, yz) of point c of lane tt:
+          // three 2-wide loads, consecutive lanes on consecutive pairs
+          using T2 = typename std::conditional<sizeof(T) == 8, double2, float2>::type;
+          const T2 *Gq = reinterpret_cast<const T2 *>(geo_s) + c * 3 * Cfg::KN2 + tt;
+          const T2 p0 = Gq[0], p1 = Gq[Cfg::KN2], p2 = Gq[2 * Cfg::KN2];
+          const T g0 = p0.x, g1 = p0.y, g2 = p1.x, g3 = p1.y, g4 = p2.x, g5 = p2.y;
           tx = gx * g0 + gy * g3 + gz[c] * g4;
           ty = gx * g3 + gy * g1 + gz[c] * g5;
           tzc = gx * g4 + gy * g5 + gz[c] * g2;
@@ -533,10 +539,10 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
   if (!y_ready) pdl_wait();
 }
 
-// walk-ordered copy of one colour's geometry: entry (blk, e, c, t) =
-// component e at point (l, c) of the colour's cell with ordinal blk K + k,
-// (k, l) the cell and line of lane t; zero past the colour's last cell and
-// in the block padding
+// walk-ordered copy of one colour's geometry: entry (blk, c, pr, t, h) =
+// component e = 2 pr + h at point (l, c) of the colour's cell with ordinal
+// blk K + k, (k, l) the cell and line of lane t; zero past the colour's
+// last cell and in the block padding
 template <int N, typename T>
 __global__ void line_pack_geometry_kernel(const double *__restrict__ G, long long gstride, T *__restrict__ out,
                                           long long total, long long count, int nc0, int nc1, int cx, int cy,
@@ -550,8 +556,9 @@ __global__ void line_pack_geometry_kernel(const double *__restrict__ G, long lon
     const int r = int(i - blk * Cfg::GB);
     T v = T(0);
     if (r < 6 * N * KN2) {
-      const int ec = r / KN2, tl = r - ec * KN2;
-      const int e = ec / N, c = ec - e * N;
+      // r = ((c 3 + pr) KN2 + tl) 2 + h holds component e = 2 pr + h
+      const int h = r & 1, tl = (r >> 1) % KN2, cp = (r >> 1) / KN2;
+      const int c = cp / 3, e = 2 * (cp - 3 * c) + h;
       const int k = Cfg::PP.INTER ? tl % Cfg::K : tl / N2, l = Cfg::PP.INTER ? tl / Cfg::K : tl % N2;
       const long long o = blk * Cfg::K + k;
       if (o < count) {
