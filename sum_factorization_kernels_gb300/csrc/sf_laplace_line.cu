@@ -131,6 +131,10 @@ long long line_color_geometry(const int (&nc)[3], int color, long long *count)
 template <int N, typename T>
 struct LineArgs {
   EOMat<N, T> S, ST, D, DT;
+  // the same tables as (e, o) pairs for packed FP32x2 arithmetic: S, ST, D, DT
+  struct {
+    float2 eo[N / 2 > 0 ? N / 2 : 1][N / 2 > 0 ? N / 2 : 1];
+  } P2[4];
   T w[N];
   const T *__restrict__ x;
   T *__restrict__ y;
@@ -155,6 +159,49 @@ struct LineArgs {
   // (mi, mj, mk) index space: no division inside the loop
   int step_i, step_j, step_k;
 };
+
+// out = M in.  In FP32 the even and odd products of output pair i,
+// (e[i][j] u+_j, o[i][j] u-_j), run as one packed FP32x2 FMA with the pair
+// table P2[WHICH]; the sums and the middle row stay scalar.  FP64 uses the
+// scalar even-odd contraction.
+template <int N, int SIGN, int WHICH, typename T, typename ARGS>
+__device__ __forceinline__ void eo_line(const ARGS &A, const EOMat<N, T> &M, const T (&in)[N], T (&out)[N])
+{
+  if constexpr (std::is_same<T, float>::value && N >= 2) {
+    constexpr int H = N / 2;
+    float up[H], um[H];
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+      up[j] = in[j] + in[N - 1 - j];
+      um[j] = in[j] - in[N - 1 - j];
+    }
+    float2 acc[H];
+#pragma unroll
+    for (int i = 0; i < H; ++i) acc[i] = make_float2((N % 2 == 1) ? M.mc[i] * in[H] : 0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+      const float2 u = make_float2(up[j], um[j]);
+#pragma unroll
+      for (int i = 0; i < H; ++i) acc[i] = __ffma2_rn(A.P2[WHICH].eo[i][j], u, acc[i]);
+    }
+    float res[N];
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      res[i] = acc[i].x + acc[i].y;
+      res[N - 1 - i] = SIGN > 0 ? acc[i].x - acc[i].y : acc[i].y - acc[i].x;
+    }
+    if (N % 2 == 1) {
+      float m = SIGN > 0 ? M.mm * in[H] : 0.f;
+#pragma unroll
+      for (int j = 0; j < H; ++j) m = fmaf(M.mr[j], SIGN > 0 ? up[j] : um[j], m);
+      res[H] = m;
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) out[i] = res[i];
+  } else {
+    eo_apply<N, SIGN>(M, in, out);
+  }
+}
 
 // cell operator of the apply: the Laplacian (div(kappa grad)), the mass
 // matrix or the convection form (u, b . grad v); the last two on affine
@@ -293,14 +340,14 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
       unstr_column<N, T>(A, used && o + step < A.count, o + step, l, nn, nmsk);
     }
     // ---- sweeps S_z (gathered column), S_x, S_y and D_y ----
-    eo_apply<N, 1>(A.S, xv, v);
+    eo_line<N, 1, 0>(A, A.S, xv, v);
 #pragma unroll
     for (int c = 0; c < N; ++c)
       if (used) B0[zc0 + L0.SZ * c] = v[c];
     cell_group_sync<W, Cfg::GROUPS>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B0[xl0 + L0.SX * m];
-    eo_apply<N, 1>(A.S, v, v);
+    eo_line<N, 1, 0>(A, A.S, v, v);
 #pragma unroll
     for (int m = 0; m < N; ++m)
       if (used) B0[xl0 + L0.SX * m] = v[m];
@@ -309,19 +356,19 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
       // ---- y lines: S_y, the weights JxW w at the Gauss points ----
 #pragma unroll
       for (int m = 0; m < N; ++m) v[m] = B0[yl0 + L0.SY * m];
-      eo_apply<N, 1>(A.S, v, v);
+      eo_line<N, 1, 0>(A, A.S, v, v);
       const T wxz = A.jxw * A.w[yx] * A.w[yz];
 #pragma unroll
       for (int m = 0; m < N; ++m) v[m] *= wxz * A.w[m];
       if constexpr (OPK == OP_MASS) {
-        eo_apply<N, 1>(A.ST, v, v);
+        eo_line<N, 1, 1>(A, A.ST, v, v);
 #pragma unroll
         for (int m = 0; m < N; ++m)
           if (used) B1[yl1 + L1.SY * m] = v[m];
       } else {
         // convection: r = u JxW w stays in B0 for the x and z lines; the y
         // term b_y / h_y D^T r goes to B1
-        eo_apply<N, -1>(A.DT, v, g);
+        eo_line<N, -1, 3>(A, A.DT, v, g);
 #pragma unroll
         for (int m = 0; m < N; ++m) {
           if (used) B0[yl0 + L0.SY * m] = v[m];
@@ -333,7 +380,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
         // ---- x lines: + b_x / h_x D^T r ----
 #pragma unroll
         for (int m = 0; m < N; ++m) v[m] = B0[xl0 + L0.SX * m];
-        eo_apply<N, -1>(A.DT, v, g);
+        eo_line<N, -1, 3>(A, A.DT, v, g);
 #pragma unroll
         for (int m = 0; m < N; ++m) {
           const T s = fma(A.conv[0], g[m], B1[xl1 + L1.SX * m]);
@@ -358,17 +405,17 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
         // ---- z columns: + b_z / h_z D^T r, then S_z^T ----
 #pragma unroll
         for (int m = 0; m < N; ++m) v[m] = B0[zc0 + L0.SZ * m];
-        eo_apply<N, -1>(A.DT, v, g);
+        eo_line<N, -1, 3>(A, A.DT, v, g);
 #pragma unroll
         for (int m = 0; m < N; ++m) v[m] = fma(A.conv[2], g[m], B1[zc1 + L1.SZ * m]);
-        eo_apply<N, 1>(A.ST, v, v);
+        eo_line<N, 1, 1>(A, A.ST, v, v);
 #pragma unroll
         for (int m = 0; m < N; ++m)
           if (used) B1[zc1 + L1.SZ * m] = v[m];
         cell_group_sync<W, Cfg::GROUPS>(grp);
 #pragma unroll
         for (int m = 0; m < N; ++m) v[m] = B1[yl1 + L1.SY * m];
-        eo_apply<N, 1>(A.ST, v, v);
+        eo_line<N, 1, 1>(A, A.ST, v, v);
 #pragma unroll
         for (int m = 0; m < N; ++m)
           if (used) B1[yl1 + L1.SY * m] = v[m];
@@ -377,7 +424,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
       // ---- x lines: S_x^T ----
 #pragma unroll
       for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
-      eo_apply<N, 1>(A.ST, v, v);
+      eo_line<N, 1, 1>(A, A.ST, v, v);
 #pragma unroll
       for (int m = 0; m < N; ++m)
         if (used) B1[xl1 + L1.SX * m] = v[m];
@@ -385,7 +432,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
       // ---- z column: S_z^T (mass), scatter ----
 #pragma unroll
       for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
-      if constexpr (OPK == OP_MASS) eo_apply<N, 1>(A.ST, v, v);
+      if constexpr (OPK == OP_MASS) eo_line<N, 1, 1>(A, A.ST, v, v);
       if (valid) store_column<N, T>(A.y + nb, A.x + nb, plane, msk.keep, v, yo);
       msk = nmsk;
       nb = nnb;
@@ -397,8 +444,8 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
     } else {
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B0[yl0 + L0.SY * m];
-    eo_apply<N, 1>(A.S, v, v);
-    eo_apply<N, -1>(A.D, v, g);
+    eo_line<N, 1, 0>(A, A.S, v, v);
+    eo_line<N, -1, 2>(A, A.D, v, g);
 #pragma unroll
     for (int m = 0; m < N; ++m) {
       if (used) B1[yl1 + L1.SY * m] = v[m];
@@ -408,13 +455,13 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
     // ---- D_x into B0; D_z stays in registers (same thread, same column) ----
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
-    eo_apply<N, -1>(A.D, v, g);
+    eo_line<N, -1, 2>(A, A.D, v, g);
 #pragma unroll
     for (int m = 0; m < N; ++m)
       if (used) B0[xl0 + L0.SX * m] = g[m];
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
-    eo_apply<N, -1>(A.D, v, gz);
+    eo_line<N, -1, 2>(A, A.D, v, gz);
     cell_group_sync<W, Cfg::GROUPS>(grp);
     // ---- quadrature points of column (a,b) ----
     const bool more = o0 + step < A.count;
@@ -460,7 +507,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
         if (used) B2[zc2 + L2.SZ * c] = ty;
         tz[c] = tzc;
       }
-      eo_apply<N, -1>(A.DT, tz, g);
+      eo_line<N, -1, 3>(A, A.DT, tz, g);
 #pragma unroll
       for (int c = 0; c < N; ++c)
         if (used) B1[zc1 + L1.SZ * c] = g[c];
@@ -490,7 +537,7 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
     }
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B0[xl0 + L0.SX * m];
-    eo_apply<N, -1>(A.DT, v, g);
+    eo_line<N, -1, 3>(A, A.DT, v, g);
 #pragma unroll
     for (int m = 0; m < N; ++m) {
       const T s = B1[xl1 + L1.SX * m] + g[m];
@@ -499,24 +546,24 @@ __global__ void __launch_bounds__(LineCfg<N, T>::GT * LineCfg<N, T>::GROUPS,
     cell_group_sync<W, Cfg::GROUPS>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B2[yl2 + L2.SY * m];
-    eo_apply<N, -1>(A.DT, v, g);
+    eo_line<N, -1, 3>(A, A.DT, v, g);
 #pragma unroll
     for (int m = 0; m < N; ++m) g[m] += B1[yl1 + L1.SY * m];
-    eo_apply<N, 1>(A.ST, g, v);
+    eo_line<N, 1, 1>(A, A.ST, g, v);
 #pragma unroll
     for (int m = 0; m < N; ++m)
       if (used) B1[yl1 + L1.SY * m] = v[m];
     cell_group_sync<W, Cfg::GROUPS>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[xl1 + L1.SX * m];
-    eo_apply<N, 1>(A.ST, v, v);
+    eo_line<N, 1, 1>(A, A.ST, v, v);
 #pragma unroll
     for (int m = 0; m < N; ++m)
       if (used) B1[xl1 + L1.SX * m] = v[m];
     cell_group_sync<W, Cfg::GROUPS>(grp);
 #pragma unroll
     for (int m = 0; m < N; ++m) v[m] = B1[zc1 + L1.SZ * m];
-    eo_apply<N, 1>(A.ST, v, v);
+    eo_line<N, 1, 1>(A, A.ST, v, v);
     // ---- scatter the z column: first colour stores, later ones add ----
     if constexpr (UNSTR) {
       if (valid) {
@@ -635,6 +682,16 @@ int line_unstr_pack_impl(sf_op *op, DevBuf &buf)
   return SF_OK;
 }
 
+// the (e, o) pair tables of the FP32 contractions
+template <int N, typename T>
+void fill_pairs(LineArgs<N, T> &A)
+{
+  const EOMat<N, T> *ms[4] = {&A.S, &A.ST, &A.D, &A.DT};
+  for (int w = 0; w < 4; ++w)
+    for (int i = 0; i < N / 2; ++i)
+      for (int j = 0; j < N / 2; ++j) A.P2[w].eo[i][j] = make_float2(float(ms[w]->e[i][j]), float(ms[w]->o[i][j]));
+}
+
 template <int N, typename T>
 int line_unstr_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
 {
@@ -646,6 +703,7 @@ int line_unstr_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
   A.ST = eo_of<N, T>(s.S, true);
   A.D = eo_of<N, T>(s.D, false);
   A.DT = eo_of<N, T>(s.D, true);
+  fill_pairs<N, T>(A);
   for (int i = 0; i < N; ++i) A.w[i] = T(s.wq[i]);
   A.x = x;
   A.y = y;
@@ -706,6 +764,7 @@ int line_vmult_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
   A.ST = eo_of<N, T>(s.S, true);
   A.D = eo_of<N, T>(s.D, false);
   A.DT = eo_of<N, T>(s.D, true);
+  fill_pairs<N, T>(A);
   for (int i = 0; i < N; ++i) A.w[i] = T(s.wq[i]);
   for (int d = 0; d < 3; ++d) A.nc[d] = op->desc.n_cells[d];
   A.Nx = (N - 1) * A.nc[0] + 1;
