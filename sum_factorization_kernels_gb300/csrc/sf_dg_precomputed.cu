@@ -29,7 +29,10 @@
 //   x:  B  = c_x (L_x x + x couplings);        Az = M_x Az
 //   y:  B  = M_y B;  Az = M_y Az;   X = c_y (L_y x + y couplings)
 //   x:  B += M_x X
-//   z:  y = M_z B + Az                       (or the fused Chebyshev step)
+//   z:  y = M_z B + Az                       (or the fused Chebyshev step,
+//                                             whose b and t arrive by
+//                                             asynchronous copies during the
+//                                             last two phases)
 #include "sf_device.cuh"
 #include "sf_dg_common.cuh"
 #include "sf_internal.h"
@@ -93,7 +96,24 @@ struct PDGCfg {
                        E2 = pdg_slab_end(N, CPB, S.B);
   static constexpr int WORDS = E0 > E1 ? (E0 > E2 ? E0 : E2) : (E1 > E2 ? E1 : E2);
   static constexpr size_t SMEM = size_t(WORDS) * sizeof(T);
+  // fused Chebyshev step: the b and t entries of each thread's column are
+  // staged by asynchronous copies during the last two phases (FP32; at n = 8
+  // and in FP64 the extra shared memory costs more residency than the hidden
+  // latency gains: measured 186 vs 182 us at p = 7, 2512 vs 2493 us for FP64
+  // p = 5, against 174 vs 224 us for FP32 p = 5)
+  static constexpr int THREADS = CPB * N * N;
+  static constexpr int STAGED = (sizeof(T) == 4 && N != 8) ? 2 : 0;
+  static constexpr int STAGE0 = (WORDS + 3) / 4 * 4;
+  static constexpr size_t SMEM_CHEB = (size_t(STAGE0) + STAGED * size_t(N) * THREADS) * sizeof(T);
 };
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *dst, const T *src)
+{
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src),
+               "n"((int)sizeof(T))
+               : "memory");
+}
 
 // line residual of the 1D operator L plus the couplings with the two
 // neighbours' end layers: lo1, lo2 = left neighbour's nodes n-1, n-2 of this
@@ -222,6 +242,17 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
 #pragma unroll
   for (int m = 0; m < N; ++m) X[ylX + LX.SY * m] = r[m];
   __syncthreads();
+  T *stage = smem + Cfg::STAGE0 + tid;
+  if (CHEB && Cfg::STAGED && valid) {
+    // b and t of the epilogue, in flight during the last two phases
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      const long long e = col + N2 * m;
+      cp_async_elem(stage + (0 * N + m) * Cfg::THREADS, A.cb + e);
+      cp_async_elem(stage + (1 * N + m) * Cfg::THREADS, A.ct + e);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
   // ---- x: B += M_x X ----
 #pragma unroll
   for (int m = 0; m < N; ++m) v[m] = X[xlX + LX.SX * m];
@@ -238,11 +269,14 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   if (valid) {
     T *dst = A.y + roff + col;
     if (CHEB) {
+      if (Cfg::STAGED) asm volatile("cp.async.wait_group 0;" ::: "memory");
 #pragma unroll
       for (int m = 0; m < N; ++m) {
         const long long e = col + N2 * m;
-        const T res = v[m] - A.cb[e];
-        const T tn = A.c_tm * A.ct[e] + A.c_np * A.cdinv[e] * res;
+        const T vb = Cfg::STAGED ? stage[(0 * N + m) * Cfg::THREADS] : A.cb[e];
+        const T vt = Cfg::STAGED ? stage[(1 * N + m) * Cfg::THREADS] : A.ct[e];
+        const T res = v[m] - vb;
+        const T tn = A.c_tm * vt + A.c_np * __ldg(A.cdinv + e) * res;
         A.ct[e] = tn;
         dst[N2 * m] = __ldg(x + e) - tn;
       }
@@ -341,11 +375,12 @@ int precomputed_impl(const sf_op *op, int nrhs, const T *x, T *y, const T *cb, c
   A.c_np = T(c_np);
   A.c_tm = T(c_tm);
   void (*kern)(const PDGArgs<N, T>) = cb ? dg_precomputed_kernel<N, T, true> : dg_precomputed_kernel<N, T, false>;
-  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
+  const size_t smem = cb ? Cfg::SMEM_CHEB : Cfg::SMEM;
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    cudaSharedmemCarveoutMaxShared));
   const long long blocks = (op->n_cells + Cfg::CPB - 1) / Cfg::CPB;
-  kern<<<dim3((unsigned)blocks, (unsigned)nrhs), dim3(Cfg::CPB * N * N), Cfg::SMEM, st>>>(A);
+  kern<<<dim3((unsigned)blocks, (unsigned)nrhs), dim3(Cfg::CPB * N * N), smem, st>>>(A);
   SF_CUDA_TRY(cudaGetLastError());
   return SF_OK;
 }

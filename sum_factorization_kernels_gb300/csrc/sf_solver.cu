@@ -15,7 +15,9 @@
 //    steps, range [lambda_max / range, 1.2 lambda_max].
 //  * Scalars (alpha, beta, dot products, the convergence flag) stay on the
 //    device.  Reductions are single-pass: fixed-size block partials, summed
-//    in block order by the last block to finish (deterministic).  The host
+//    in block order by the last block to finish (deterministic); FP32
+//    vectors are reduced four entries at a time in FP32 and accumulated in
+//    FP64.  The host
 //    never waits for the iteration it has just queued: it queues iteration
 //    k, then reads the scalars of iteration k-1 from pinned memory.  An
 //    iteration queued after convergence changes nothing, because the update
@@ -26,6 +28,7 @@
 //    project_constant the right-hand side and every preconditioned residual
 //    are projected to mean zero.
 #include <chrono>
+#include <cstdint>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -80,8 +83,30 @@ __global__ void __launch_bounds__(kThreads) reduce_kernel(long long n, const T *
   __shared__ double s1[kThreads], s2[kThreads];
   __shared__ bool last;
   double u = 0, v = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
+  const long long gs = (long long)gridDim.x * blockDim.x;
+  long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if constexpr (sizeof(T) == 4) {
+    // FP32 vectors: four products and their sum in FP32, accumulated in
+    // FP64 once per four entries (the FP64 pipe runs at 1/64 of FP32 rate
+    // and would bound a per-entry FP64 accumulation)
+    const bool aligned = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) == 0;
+    if (aligned) {
+      const long long n4 = n / 4;
+      const float4 *a4 = reinterpret_cast<const float4 *>(a), *b4 = reinterpret_cast<const float4 *>(b);
+      for (long long i = i0; i < n4; i += gs) {
+        const float4 x = a4[i];
+        if (MODE == RED_SUM) {
+          u += double((x.x + x.y) + (x.z + x.w));
+        } else {
+          const float4 y = b4[i];
+          u += double(fmaf(x.w, y.w, fmaf(x.z, y.z, fmaf(x.y, y.y, x.x * y.x))));
+          if (MODE == RED_RZ) v += double(fmaf(x.w, x.w, fmaf(x.z, x.z, fmaf(x.y, x.y, x.x * x.x))));
+        }
+      }
+      i0 += 4 * n4;
+    }
+  }
+  for (long long i = i0; i < n; i += gs) {
     const double ai = a[i];
     if (MODE == RED_SUM) {
       u += ai;
