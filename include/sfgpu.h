@@ -240,8 +240,13 @@ int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void 
  * plus-face matrices L of penalty * (p+1)^2 and 1D mass matrices M: the
  * kernel of SF_OP_DG_PRECOMPUTED), SF_KERNEL_GENERIC the cell-and-face
  * kernel that follows the reference's EvaluationDGLaplacian step by step;
- * both give the same operator to rounding.  Other values are rejected with
- * SF_ERR_INVALID.  No reference counterpart. */
+ * both give the same operator to rounding.  SF_OP_DG_ADVECT: SF_KERNEL_AUTO
+ * evaluates M^-1 A as a sum of 1D line operators, sum_d B_d (x) I (x) I
+ * with each line coupled to the upwind neighbour's end node (constant
+ * velocity, Cartesian cells), and A and A^T as M times such a sum;
+ * SF_KERNEL_GENERIC the cell-and-face kernel that follows the reference's
+ * EvaluationDGAdvection step by step; the same operator to rounding.  Other
+ * values are rejected with SF_ERR_INVALID.  No reference counterpart. */
 typedef enum {
   SF_KERNEL_AUTO = 0,
   SF_KERNEL_GENERIC = 1

@@ -75,6 +75,13 @@ bool tensor_form(const sf_op *op)
          (op->desc.kind == SF_OP_DG_SIPG && op->kernel_variant != SF_KERNEL_GENERIC);
 }
 
+// DG advection as a sum of one-dimensional line operators (constant
+// velocity, Cartesian cells) unless the cell-and-face kernel is selected
+bool advect_tensor(const sf_op *op)
+{
+  return op->desc.kind == SF_OP_DG_ADVECT && op->kernel_variant != SF_KERNEL_GENERIC;
+}
+
 bool is_continuous(int kind)
 {
   return kind == SF_OP_LAPLACE || kind == SF_OP_MASS || kind == SF_OP_CONVECTION ||
@@ -436,6 +443,9 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
   if (is_cell_faces(op->desc.kind)) return launch_cell_faces(op, prec, 1, x, y, st);
   if (tensor_form(op))
     return launch_dg_precomputed(op, prec, 1, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
+  if (advect_tensor(op))
+    return launch_dg_advect_tensor(op, prec, 1, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, nullptr,
+                                   nullptr, nullptr, st);
   return launch_dg_vmult(op, prec, 1, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
 }
 
@@ -468,6 +478,9 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
   if (is_cell_faces(op->desc.kind)) return launch_cell_faces(op, prec, nrhs, x, y, st);
   if (tensor_form(op))
     return launch_dg_precomputed(op, prec, nrhs, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
+  if (advect_tensor(op))
+    return launch_dg_advect_tensor(op, prec, nrhs, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, nullptr,
+                                   nullptr, nullptr, st);
   return launch_dg_vmult(op, prec, nrhs, false, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
 }
 
@@ -491,6 +504,9 @@ int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, voi
     SF_RET(launch_dg_inverse_mass(op, prec, nrhs, x, op->scratch.ptr, st));
     src = op->scratch.ptr;
   }
+  if (advect_tensor(op))
+    return launch_dg_advect_tensor(op, prec, nrhs, true, src, y, nullptr, nullptr, nullptr, 0.0, 0.0, nullptr,
+                                   nullptr, nullptr, st);
   return launch_dg_vmult(op, prec, nrhs, true, src, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
 }
 
@@ -510,6 +526,9 @@ int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv, 
   cudaStream_t st = (cudaStream_t)stream;
   const Region region(op->region_ch);
   if (tensor_form(op)) return launch_dg_precomputed(op, prec, 1, x_old, x_new, b, diag_inv, t, c_np, c_tm, st);
+  if (advect_tensor(op))
+    return launch_dg_advect_tensor(op, prec, 1, false, x_old, x_new, b, diag_inv, t, c_np, c_tm, nullptr, nullptr,
+                                   nullptr, st);
   if (op->desc.kind == SF_OP_DG_SIPG || op->desc.kind == SF_OP_DG_ADVECT)
     return launch_dg_vmult(op, prec, 1, false, x_old, x_new, b, diag_inv, t, c_np, c_tm, st);
   // continuous: operator into x_new, then the fused vector update in place
@@ -532,6 +551,9 @@ int sf_rk_stage(sf_op *op, int prec, int nrhs, const void *src, const void *upd,
     return fail(SF_ERR_INVALID, "src must not be an output vector");
   if (c_tm != 0.0 && vec_np == vec_tm) return fail(SF_ERR_INVALID, "vec_np and vec_tm must differ");
   const Region region(op->region_ch);
+  if (advect_tensor(op))
+    return launch_dg_advect_tensor(op, prec, nrhs, false, src, nullptr, nullptr, nullptr, nullptr, c_np, c_tm,
+                                   upd, vec_np, c_tm != 0.0 ? vec_tm : nullptr, (cudaStream_t)stream);
   return launch_dg_rk_stage(op, prec, nrhs, src, upd, vec_np, c_tm != 0.0 ? vec_tm : nullptr, c_np, c_tm,
                             (cudaStream_t)stream);
 }

@@ -36,6 +36,13 @@ int launch_dg_precomputed(const sf_op *op, int prec, int nrhs, const void *x, vo
                           const void *cheb_dinv, void *cheb_t, double c_np, double c_tm, cudaStream_t st);
 int launch_dg_precomputed_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
 
+// sf_dg_advect_tensor.cu: DG advection as a sum of 1D line operators; the
+// inverse-mass apply (forward with inverse_mass), otherwise the mass form;
+// rk_np non-null: fused Runge-Kutta stage (as launch_dg_rk_stage)
+int launch_dg_advect_tensor(const sf_op *op, int prec, int nrhs, bool transpose, const void *x, void *y,
+                            const void *cheb_b, const void *cheb_dinv, void *cheb_t, double c_np, double c_tm,
+                            const void *rk_upd, void *rk_np, void *rk_tm, cudaStream_t st);
+
 // sf_cell_faces.cu: the DO_FACES cell operators (block diagonal, cell-major)
 int launch_cell_faces(const sf_op *op, int prec, int nrhs, const void *x, void *y, cudaStream_t st);
 

@@ -118,6 +118,51 @@ def test_advect_forward_transpose_vs_oracle(p, invm):
     assert rel(to_np(y), O.dg_advect_apply_transpose(d, x)) < FP64_TOL
 
 
+@pytest.mark.parametrize("p", range(1, 9))
+def test_advect_line_operators_equal_cell_face_kernel(p):
+    """SF_OP_DG_ADVECT through the line-operator kernel (default) and the
+    cell-and-face kernel: forward and transpose with and without the inverse
+    mass, three right-hand sides in one launch, a Runge-Kutta stage and a
+    Chebyshev step; the applies against the oracle (anisotropic cells,
+    one-cell-thick y, a negative velocity component)"""
+    torch = torch_cuda()
+    sf = _sf()
+    nc, h, vel = (4, 1, 3), (0.3, 0.2, 0.45), (1.0, 0.5, -0.25)
+    rng = np.random.default_rng(40 + p)
+    for invm in (0, 1):
+        op = sf.Operator(sf.OP_DG_ADVECT, degree=p, n_cells=nc, length=_lengths(nc, h), velocity=vel,
+                         inverse_mass=invm)
+        g = O.dg(p, nc, h, velocity=vel, inverse_mass=invm)
+        N = op.n_dofs
+        x = rng.uniform(-1, 1, 3 * N)
+        refs = [O.dg_advect_apply(g, x[r * N:(r + 1) * N]) for r in range(3)]
+        refs_t = [O.dg_advect_apply_transpose(g, x[r * N:(r + 1) * N]) for r in range(3)]
+        b0, t0, d0 = rng.uniform(-1, 1, N), rng.uniform(-1, 1, N), rng.uniform(0.5, 1, N)
+        out = {}
+        for variant in (sf.KERNEL_AUTO, sf.KERNEL_GENERIC):
+            op.set_kernel_variant(variant)
+            for dtype, tol in ((torch.float64, FP64_TOL), (torch.float32, 4 * FP32_TOL[p])):
+                xd = to_dev(torch, x, dtype)
+                y = torch.empty_like(xd)
+                op.vmult_batched(xd, y, 3)
+                for r in range(3):
+                    assert rel(to_np(y[r * N:(r + 1) * N]), refs[r]) < tol, (variant, invm, dtype, r)
+                op.vmult_transpose_batched(xd, y, 3)
+                for r in range(3):
+                    assert rel(to_np(y[r * N:(r + 1) * N]), refs_t[r]) < tol, (variant, invm, dtype, r)
+            xd = to_dev(torch, x, torch.float64)
+            upd = to_dev(torch, b0, torch.float64).repeat(3)
+            vnp, vtm = torch.empty_like(xd), torch.empty_like(xd)
+            op.rk_stage(xd, upd, vnp, vtm, 0.3, -0.2, nrhs=3)
+            xn, t = torch.empty(N, dtype=torch.float64, device="cuda:0"), to_dev(torch, t0, torch.float64)
+            op.chebyshev_step(to_dev(torch, b0, torch.float64), to_dev(torch, d0, torch.float64),
+                              xd[:N].contiguous(), xn, t, 0.7, 0.3)
+            out[variant] = [to_np(v) for v in (vnp, vtm, xn, t)]
+        for a_, b_ in zip(out[sf.KERNEL_AUTO], out[sf.KERNEL_GENERIC]):
+            assert rel(a_, b_) < FP64_TOL, invm
+        assert op.device_status() == 0
+
+
 def test_advect_adjoint_dot_test_full_size():
     """<A x, y> = <x, A^T y> to 1e-12 (FP64) on the 48^3 p=4 mesh, 8 right-hand
     sides in one launch, with and without the inverse mass matrix"""

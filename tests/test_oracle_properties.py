@@ -215,3 +215,53 @@ def test_sipg_is_kronecker_sum(p, penalty):
     y = Y.reshape(nc[2], n, nc[1], n, nc[0], n).transpose(0, 2, 4, 1, 3, 5).ravel()
     ys = O.dg_sipg_apply(O.dg(p, nc, h, penalty=penalty), x)
     assert np.linalg.norm(y - ys) / np.linalg.norm(ys) < 1e-13
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_advect_is_sum_of_line_operators(p):
+    """On a periodic Cartesian mesh with constant velocity the upwind DG
+    advection operator (GLL nodes, Gauss points) separates by direction:
+    M^-1 A = sum_d B_d (x) I (x) I and A = M sum_d B_d (x) I (x) I, with
+    B_d = S^-1 W^-1 R_d S from the Gauss-point line residual R_d and each
+    line coupled to the upwind (transpose: downwind) neighbour's nodal end
+    value; M = jxw M1 (x) M1 (x) M1, M1 = S^T W S.  The identity behind the
+    line-operator advection kernel, checked for the forward operator (with
+    and without the inverse mass) and the transpose, on a mesh with a
+    one-cell-thick direction and a negative velocity component"""
+    n = p + 1
+    sh = O.shape_arrays(p)
+    S, D, Sinv, w, fv = sh["S"], sh["D"], sh["Sinv"], sh["wq"], sh["face_v"]
+    M1 = S.T @ np.diag(w) @ S
+    vel = (1.0, 0.5, -0.25)
+    for nc, h in (((3, 4, 2), (0.25, 0.2, 0.4)), ((4, 1, 3), (0.3, 0.2, 0.45))):
+        jxw = h[0] * h[1] * h[2]
+        # (the transpose with the inverse mass is A^T M^-1: the transpose
+        # case applied to M^-1 x)
+        for invm, tr in ((0, False), (0, True), (1, False)):
+            g = O.dg(p, nc, h, velocity=vel, inverse_mass=invm)
+            x = np.random.default_rng(p).uniform(-1, 1, O.dg_n_dofs(g))
+            inv = bool(invm)
+            P = Sinv / w[None, :] / (jxw if inv else 1.0)
+            X = x.reshape(nc[2], nc[1], nc[0], n, n, n)   # [cz][cy][cx][z][y][x]
+            Y = np.zeros_like(X)
+            for d, (cax, nax) in enumerate(((2, 5), (1, 4), (0, 3))):
+                ij, ad = 1 / h[d], vel[d]
+                c, jf = ad * ij * jxw, jxw * ij
+                R = c * np.diag(w) @ D if tr else D.T @ np.diag(c * w)
+                nb = []
+                for side in range(2):
+                    an = ad if side else -ad
+                    fa = -0.5 * ((an + abs(an)) if tr else an) * jf
+                    fb = -0.5 * abs(an) * jf
+                    R = R + (fa if tr else fa + fb) * np.outer(fv[side], fv[side])
+                    nb.append(P @ (fv[side] * (-fa if tr else fa - fb)))
+                B = P @ R @ S
+                lo = np.take(np.roll(X, 1, axis=cax), n - 1, axis=nax)
+                hi = np.take(np.roll(X, -1, axis=cax), 0, axis=nax)
+                Yd = np.moveaxis(X, nax, -1) @ B.T + lo[..., None] * nb[0] + hi[..., None] * nb[1]
+                Y += np.moveaxis(Yd, -1, nax)
+            if not inv:
+                for nax in (5, 4, 3):
+                    Y = np.moveaxis(np.moveaxis(Y, nax, -1) @ M1.T, -1, nax)
+            ref = O.dg_advect_apply_transpose(g, x) if tr else O.dg_advect_apply(g, x)
+            assert np.linalg.norm(Y.ravel() - ref) / np.linalg.norm(ref) < 1e-13, (nc, invm, tr)
