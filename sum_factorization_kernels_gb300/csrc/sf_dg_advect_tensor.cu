@@ -57,7 +57,7 @@ struct TAArgs {
   // may alias vec_np or vec_tm (read before written, element by element)
   const T *rk_upd;
   T *rk_np, *rk_tm;
-  int nc[3];
+  int nc[3], nrhs;
   FastDiv div_nx, div_ny;
   long long n_cells, n_dofs;
 };
@@ -76,7 +76,7 @@ struct TACfg {
   static constexpr int SLAB = L.P2 * N;
   static constexpr int RS = 3 * SLAB + L.SKEW;
   static constexpr TASlab X{1, L.P1, L.P2, RS, 0}, R1{1, L.P1, L.P2, RS, SLAB}, R2{1, L.P1, L.P2, RS, 2 * SLAB};
-  static constexpr size_t SMEM = size_t(CPB) * RS * sizeof(T);
+  static constexpr size_t SMEM = size_t(CPB) * RS * sizeof(T); // per right-hand side
 };
 
 // every entry of the three slabs of a cell has its own word inside RS
@@ -119,7 +119,10 @@ __device__ __forceinline__ void line_op(const TAArgs<N, T> &A, int d, const T (&
   }
 }
 
-template <int N, typename T, bool MASS, int EPI>
+// R right-hand sides per thread (blockIdx.y covers R of them): the cell's
+// neighbour and address arithmetic is shared and R times as many loads are in
+// flight; each right-hand side has slabs of its own
+template <int N, typename T, bool MASS, int EPI, int R>
 __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     dg_advect_tensor_kernel(const __grid_constant__ TAArgs<N, T> A)
 {
@@ -127,6 +130,7 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   constexpr int N2 = N * N, N3 = N * N * N;
   constexpr int CPB = Cfg::CPB;
   constexpr TASlab LX = Cfg::X, L1 = Cfg::R1, L2 = Cfg::R2;
+  constexpr int RSTRIDE = CPB * Cfg::RS; // slab words of one right-hand side
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
   const int tid = threadIdx.x;
@@ -143,8 +147,10 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   const int zc1 = L1.SX * a + L1.SY * b, xl1 = L1.SY * a + L1.SZ * b;
   const int zc2 = L2.SX * a + L2.SY * b, yl2 = L2.SX * a + L2.SZ * b;
   const long long col = cell * N3 + t;
-  const long long roff = (long long)blockIdx.y * A.n_dofs; // right-hand side offset
-  const T *__restrict__ x = A.x + roff;
+  const int r0 = (int)blockIdx.y * R;
+  bool on[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) on[k] = valid && r0 + k < A.nrhs;
 
   long long nb[3][2] = {{cell, cell}, {cell, cell}, {cell, cell}};
   if (valid) {
@@ -158,98 +164,126 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
       nb[d][1] = periodic_neighbour(A.nc, ix, iy, int(iz), d, 1);
     }
   }
-  const bool l0 = valid && (A.nbmask & 1), r0 = valid && (A.nbmask & 2);
-  const bool l1 = valid && (A.nbmask & 4), r1 = valid && (A.nbmask & 8);
-  const bool l2 = valid && (A.nbmask & 16), r2 = valid && (A.nbmask & 32);
+  // neighbour end values of this thread's z column, x line and y line:
+  // (a, b, n-1) / (a, b, 0), (n-1, a, b) / (0, a, b), (a, n-1, b) / (a, 0, b)
+  const long long off[3][2] = {{nb[0][0] * N3 + (N - 1) + N * a + N2 * b, nb[0][1] * N3 + N * a + N2 * b},
+                               {nb[1][0] * N3 + a + N * (N - 1) + N2 * b, nb[1][1] * N3 + a + N2 * b},
+                               {nb[2][0] * N3 + t + N2 * (N - 1), nb[2][1] * N3 + t}};
+  const bool use[3][2] = {{(A.nbmask & 1) != 0, (A.nbmask & 2) != 0},
+                          {(A.nbmask & 4) != 0, (A.nbmask & 8) != 0},
+                          {(A.nbmask & 16) != 0, (A.nbmask & 32) != 0}};
 
-  T v[N], r[N], rz[N];
-  // ---- every global read up front: the z column, the six neighbour end
-  // values of this thread's z column, x line and y line, and the
-  // Runge-Kutta update of the column ----
+  // ---- every global read up front: the z columns, the neighbour end
+  // values and the Runge-Kutta updates of the column ----
+  T v[R][N], rz[R][N], nbv[R][3][2];
+  T upd[R][EPI == TA_RK ? N : 1];
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = valid ? __ldg(x + col + N2 * m) : T(0);
-  // z column (a, b): neighbour nodes (a, b, n-1) and (a, b, 0)
-  const T zlo = l2 ? __ldg(x + nb[2][0] * N3 + t + N2 * (N - 1)) : T(0);
-  const T zhi = r2 ? __ldg(x + nb[2][1] * N3 + t) : T(0);
-  // x line (y, z) = (a, b): nodes (n-1, a, b) and (0, a, b)
-  const T xlo = l0 ? __ldg(x + nb[0][0] * N3 + (N - 1) + N * a + N2 * b) : T(0);
-  const T xhi = r0 ? __ldg(x + nb[0][1] * N3 + N * a + N2 * b) : T(0);
-  // y line (x, z) = (a, b): nodes (a, n-1, b) and (a, 0, b)
-  const T ylo = l1 ? __ldg(x + nb[1][0] * N3 + a + N * (N - 1) + N2 * b) : T(0);
-  const T yhi = r1 ? __ldg(x + nb[1][1] * N3 + a + N2 * b) : T(0);
-  T upd[EPI == TA_RK ? N : 1];
-  if (EPI == TA_RK) {
+  for (int k = 0; k < R; ++k) {
+    const T *__restrict__ x = A.x + (long long)(r0 + k) * A.n_dofs;
 #pragma unroll
-    for (int m = 0; m < N; ++m) upd[m] = valid ? A.rk_upd[roff + col + N2 * m] : T(0);
+    for (int m = 0; m < N; ++m) v[k][m] = on[k] ? __ldg(x + col + N2 * m) : T(0);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int sd = 0; sd < 2; ++sd) nbv[k][d][sd] = on[k] && use[d][sd] ? __ldg(x + off[d][sd]) : T(0);
+    if (EPI == TA_RK) {
+#pragma unroll
+      for (int m = 0; m < N; ++m)
+        upd[k][m] = on[k] ? A.rk_upd[(long long)(r0 + k) * A.n_dofs + col + N2 * m] : T(0);
+    }
   }
-  // ---- z column: copy to X, z line operator in registers ----
+  // ---- z columns: copy to X, z line operator in registers ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) X[zcX + LX.SZ * m] = v[m];
-  line_op<N, T>(A, 2, v, zlo, zhi, rz);
+  for (int k = 0; k < R; ++k) {
+#pragma unroll
+    for (int m = 0; m < N; ++m) X[k * RSTRIDE + zcX + LX.SZ * m] = v[k][m];
+    line_op<N, T>(A, 2, v[k], nbv[k][2][0], nbv[k][2][1], rz[k]);
+  }
   __syncthreads();
-  // ---- x line (y, z) = (a, b): node (m, a, b) at m + N a + N2 b ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = X[xlX + LX.SX * m];
-  line_op<N, T>(A, 0, v, xlo, xhi, r);
+  for (int k = 0; k < R; ++k) {
+    T u[N], r[N];
+    // ---- x line (y, z) = (a, b): node (m, a, b) at m + N a + N2 b ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) R1[xl1 + L1.SX * m] = r[m];
-  // ---- y line (x, z) = (a, b): node (a, m, b) at a + N m + N2 b ----
+    for (int m = 0; m < N; ++m) u[m] = X[k * RSTRIDE + xlX + LX.SX * m];
+    line_op<N, T>(A, 0, u, nbv[k][0][0], nbv[k][0][1], r);
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = X[ylX + LX.SY * m];
-  line_op<N, T>(A, 1, v, ylo, yhi, r);
+    for (int m = 0; m < N; ++m) R1[k * RSTRIDE + xl1 + L1.SX * m] = r[m];
+    // ---- y line (x, z) = (a, b): node (a, m, b) at a + N m + N2 b ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) R2[yl2 + L2.SY * m] = r[m];
+    for (int m = 0; m < N; ++m) u[m] = X[k * RSTRIDE + ylX + LX.SY * m];
+    line_op<N, T>(A, 1, u, nbv[k][1][0], nbv[k][1][1], r);
+#pragma unroll
+    for (int m = 0; m < N; ++m) R2[k * RSTRIDE + yl2 + L2.SY * m] = r[m];
+  }
   __syncthreads();
-  // ---- column sum of the three directions ----
+  // ---- column sums of the three directions ----
 #pragma unroll
-  for (int m = 0; m < N; ++m) v[m] = rz[m] + R1[zc1 + L1.SZ * m] + R2[zc2 + L2.SZ * m];
+  for (int k = 0; k < R; ++k)
+#pragma unroll
+    for (int m = 0; m < N; ++m)
+      v[k][m] = rz[k][m] + R1[k * RSTRIDE + zc1 + L1.SZ * m] + R2[k * RSTRIDE + zc2 + L2.SZ * m];
   if (MASS) {
     // M = M1 (x) M1 (x) M1: z in registers, then x and y lines in X (its
     // line reads ended at the barrier above)
-    eo_apply<N, 1>(A.M, v, v);
 #pragma unroll
-    for (int m = 0; m < N; ++m) X[zcX + LX.SZ * m] = v[m];
+    for (int k = 0; k < R; ++k) {
+      eo_apply<N, 1>(A.M, v[k], v[k]);
+#pragma unroll
+      for (int m = 0; m < N; ++m) X[k * RSTRIDE + zcX + LX.SZ * m] = v[k][m];
+    }
     __syncthreads();
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = X[xlX + LX.SX * m];
-    eo_apply<N, 1>(A.M, v, v);
+    for (int k = 0; k < R; ++k) {
+      T u[N];
 #pragma unroll
-    for (int m = 0; m < N; ++m) X[xlX + LX.SX * m] = v[m];
+      for (int m = 0; m < N; ++m) u[m] = X[k * RSTRIDE + xlX + LX.SX * m];
+      eo_apply<N, 1>(A.M, u, u);
+#pragma unroll
+      for (int m = 0; m < N; ++m) X[k * RSTRIDE + xlX + LX.SX * m] = u[m];
+    }
     __syncthreads();
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = X[ylX + LX.SY * m];
-    eo_apply<N, 1>(A.M, v, v);
+    for (int k = 0; k < R; ++k) {
+      T u[N];
 #pragma unroll
-    for (int m = 0; m < N; ++m) X[ylX + LX.SY * m] = v[m];
+      for (int m = 0; m < N; ++m) u[m] = X[k * RSTRIDE + ylX + LX.SY * m];
+      eo_apply<N, 1>(A.M, u, u);
+#pragma unroll
+      for (int m = 0; m < N; ++m) X[k * RSTRIDE + ylX + LX.SY * m] = u[m];
+    }
     __syncthreads();
 #pragma unroll
-    for (int m = 0; m < N; ++m) v[m] = X[zcX + LX.SZ * m];
+    for (int k = 0; k < R; ++k)
+#pragma unroll
+      for (int m = 0; m < N; ++m) v[k][m] = X[k * RSTRIDE + zcX + LX.SZ * m];
   }
-  // ---- store the z column (plain, fused Chebyshev or Runge-Kutta update) ----
-  if (valid) {
+  // ---- store the z columns (plain, fused Chebyshev or Runge-Kutta update) ----
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    if (!on[k]) continue;
+    const long long o = (long long)(r0 + k) * A.n_dofs + col;
     if (EPI == TA_RK) {
-      const long long o = roff + col;
 #pragma unroll
       for (int m = 0; m < N; ++m) {
         const long long e = o + N2 * m;
-        const T np = upd[m] + A.c_np * v[m];
+        const T np = upd[k][m] + A.c_np * v[k][m];
         A.rk_np[e] = np;
-        if (A.c_tm != T(0)) A.rk_tm[e] = np + A.c_tm * v[m];
+        if (A.c_tm != T(0)) A.rk_tm[e] = np + A.c_tm * v[k][m];
       }
     } else if (EPI == TA_CHEB) {
-      T *dst = A.y + roff + col;
+      // one right-hand side (the Chebyshev step of a single vector)
 #pragma unroll
       for (int m = 0; m < N; ++m) {
         const long long e = col + N2 * m;
-        const T res = v[m] - A.cb[e];
+        const T res = v[k][m] - A.cb[e];
         const T tn = A.c_tm * A.ct[e] + A.c_np * A.cdinv[e] * res;
         A.ct[e] = tn;
-        dst[N2 * m] = __ldg(x + e) - tn;
+        A.y[e] = __ldg(A.x + e) - tn;
       }
     } else {
-      T *dst = A.y + roff + col;
 #pragma unroll
-      for (int m = 0; m < N; ++m) dst[N2 * m] = v[m];
+      for (int m = 0; m < N; ++m) A.y[o + N2 * m] = v[k][m];
     }
   }
 }
@@ -364,19 +398,28 @@ int advect_tensor_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T 
   A.div_ny = make_fast_div((unsigned)A.nc[1]);
   A.n_cells = op->n_cells;
   A.n_dofs = op->n_dofs;
+  A.nrhs = nrhs;
   const bool rk = rk_np != nullptr, cheb = cb != nullptr;
+  // two right-hand sides per thread for batched FP32 applies (p = 4, 48^3,
+  // 8 right-hand sides: 258 against 301 us); not for the Runge-Kutta stage,
+  // whose prefetched updates make the pairs cost residency (1949 against
+  // 1737 us per LSRK step), nor in FP64, bound by the FP64 pipe
+  const int rps = (nrhs > 1 && sizeof(T) == 4 && !rk) ? 2 : 1;
   void (*kern)(const TAArgs<N, T>);
-  if (invmass)
-    kern = rk ? dg_advect_tensor_kernel<N, T, false, TA_RK>
-         : cheb ? dg_advect_tensor_kernel<N, T, false, TA_CHEB> : dg_advect_tensor_kernel<N, T, false, TA_STORE>;
+  if (rps == 2)
+    kern = invmass ? dg_advect_tensor_kernel<N, T, false, TA_STORE, 2> : dg_advect_tensor_kernel<N, T, true, TA_STORE, 2>;
+  else if (invmass)
+    kern = rk ? dg_advect_tensor_kernel<N, T, false, TA_RK, 1>
+         : cheb ? dg_advect_tensor_kernel<N, T, false, TA_CHEB, 1> : dg_advect_tensor_kernel<N, T, false, TA_STORE, 1>;
   else
-    kern = rk ? dg_advect_tensor_kernel<N, T, true, TA_RK>
-         : cheb ? dg_advect_tensor_kernel<N, T, true, TA_CHEB> : dg_advect_tensor_kernel<N, T, true, TA_STORE>;
-  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM));
+    kern = rk ? dg_advect_tensor_kernel<N, T, true, TA_RK, 1>
+         : cheb ? dg_advect_tensor_kernel<N, T, true, TA_CHEB, 1> : dg_advect_tensor_kernel<N, T, true, TA_STORE, 1>;
+  const size_t smem = Cfg::SMEM * rps;
+  SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    cudaSharedmemCarveoutMaxShared));
   const long long blocks = (op->n_cells + Cfg::CPB - 1) / Cfg::CPB;
-  kern<<<dim3((unsigned)blocks, (unsigned)nrhs), dim3(Cfg::CPB * N * N), Cfg::SMEM, st>>>(A);
+  kern<<<dim3((unsigned)blocks, (unsigned)((nrhs + rps - 1) / rps)), dim3(Cfg::CPB * N * N), smem, st>>>(A);
   SF_CUDA_TRY(cudaGetLastError());
   return SF_OK;
 }
