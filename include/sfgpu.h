@@ -245,8 +245,11 @@ int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void 
  * with each line coupled to the upwind neighbour's end node (constant
  * velocity, Cartesian cells), and A and A^T as M times such a sum;
  * SF_KERNEL_GENERIC the cell-and-face kernel that follows the reference's
- * EvaluationDGAdvection step by step; the same operator to rounding.  Other
- * values are rejected with SF_ERR_INVALID.  No reference counterpart. */
+ * EvaluationDGAdvection step by step; the same operator to rounding.
+ * SF_OP_CONVECTION_FACES: SF_KERNEL_AUTO evaluates the cell operator as
+ * sum_f L_f (x) M1 (x) M1 (1D convection-plus-own-face matrices L_f, 1D mass
+ * M1), SF_KERNEL_GENERIC the face-array kernel.  Other values are rejected
+ * with SF_ERR_INVALID.  No reference counterpart. */
 typedef enum {
   SF_KERNEL_AUTO = 0,
   SF_KERNEL_GENERIC = 1

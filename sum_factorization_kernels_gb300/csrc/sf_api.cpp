@@ -440,6 +440,8 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
   cudaStream_t st = (cudaStream_t)stream;
   const Region region(op->region_mv);
   if (is_continuous(op->desc.kind)) return launch_cont_vmult(op, prec, x, y, st);
+  if (is_cell_faces(op->desc.kind) && op->kernel_variant != SF_KERNEL_GENERIC)
+    return launch_faces_tensor(op, prec, 1, x, y, st);
   if (is_cell_faces(op->desc.kind)) return launch_cell_faces(op, prec, 1, x, y, st);
   if (tensor_form(op))
     return launch_dg_precomputed(op, prec, 1, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
@@ -475,6 +477,8 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
                                (char *)y + r * op->n_dofs * es, st));
     return SF_OK;
   }
+  if (is_cell_faces(op->desc.kind) && op->kernel_variant != SF_KERNEL_GENERIC)
+    return launch_faces_tensor(op, prec, nrhs, x, y, st);
   if (is_cell_faces(op->desc.kind)) return launch_cell_faces(op, prec, nrhs, x, y, st);
   if (tensor_form(op))
     return launch_dg_precomputed(op, prec, nrhs, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);

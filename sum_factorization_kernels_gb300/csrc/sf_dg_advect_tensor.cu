@@ -28,6 +28,7 @@
 // results go to two slabs of their own, so one barrier separates the line
 // phase from the column sum.
 #include <cmath>
+#include <utility>
 
 #include "sf_device.cuh"
 #include "sf_dg_common.cuh"
@@ -47,6 +48,9 @@ struct TAArgs {
   T cl[3][N], cr[3][N]; // couplings with the left neighbour's node n-1 / the right neighbour's node 0
   int nbmask;          // bit 2 d + side: the coupling of that side is nonzero
   EOMat<N, T> M;       // 1D mass matrix (plain apply and transpose)
+  // DO_FACES Laplacian: sum_f F2_f (x) Tp (x) Tp with F2_f = f2c[f] (e_p + e_0)^T
+  EOMat<N, T> Tp;
+  T f2c[3][N];
   const T *__restrict__ x;
   T *__restrict__ y;
   const T *__restrict__ cb;    // Chebyshev: rhs
@@ -77,6 +81,9 @@ struct TACfg {
   static constexpr int RS = 3 * SLAB + L.SKEW;
   static constexpr TASlab X{1, L.P1, L.P2, RS, 0}, R1{1, L.P1, L.P2, RS, SLAB}, R2{1, L.P1, L.P2, RS, 2 * SLAB};
   static constexpr size_t SMEM = size_t(CPB) * RS * sizeof(T); // per right-hand side
+  // DO_FACES Laplacian: three n x n face arrays per cell after the slabs
+  static constexpr int FW = 3 * N * N;
+  static constexpr size_t SMEM_F2 = size_t(CPB) * (RS + FW) * sizeof(T);
 };
 
 // every entry of the three slabs of a cell has its own word inside RS
@@ -122,15 +129,17 @@ __device__ __forceinline__ void line_op(const TAArgs<N, T> &A, int d, const T (&
 // R right-hand sides per thread (blockIdx.y covers R of them): the cell's
 // neighbour and address arithmetic is shared and R times as many loads are in
 // flight; each right-hand side has slabs of its own
-template <int N, typename T, bool MASS, int EPI, int R>
+template <int N, typename T, bool MASS, int EPI, int R, bool F2 = false>
 __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     dg_advect_tensor_kernel(const __grid_constant__ TAArgs<N, T> A)
 {
+  static_assert(!F2 || (MASS && EPI == TA_STORE), "face term: mass form, plain store");
   using Cfg = TACfg<N, T>;
   constexpr int N2 = N * N, N3 = N * N * N;
   constexpr int CPB = Cfg::CPB;
   constexpr TASlab LX = Cfg::X, L1 = Cfg::R1, L2 = Cfg::R2;
-  constexpr int RSTRIDE = CPB * Cfg::RS; // slab words of one right-hand side
+  // slab (and face array) words of one right-hand side
+  constexpr int RSTRIDE = CPB * (Cfg::RS + (F2 ? Cfg::FW : 0));
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
   const int tid = threadIdx.x;
@@ -142,6 +151,9 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   T *X = smem + LX.BASE + cs * LX.RS;
   T *R1 = smem + L1.BASE + cs * L1.RS;
   T *R2 = smem + L2.BASE + cs * L2.RS;
+  // face arrays of the F2 term: Fx over (y, z), Fy over (x, z), Fz over (x, y),
+  // entry (i, j) at i + N j
+  T *Fx = smem + CPB * Cfg::RS + cs * Cfg::FW, *Fy = Fx + N * N, *Fz = Fy + N * N;
   // z column (a, b), x line (y, z) = (a, b), y line (x, z) = (a, b)
   const int zcX = LX.SX * a + LX.SY * b, xlX = LX.SY * a + LX.SZ * b, ylX = LX.SX * a + LX.SZ * b;
   const int zc1 = L1.SX * a + L1.SY * b, xl1 = L1.SY * a + L1.SZ * b;
@@ -197,6 +209,7 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   for (int k = 0; k < R; ++k) {
 #pragma unroll
     for (int m = 0; m < N; ++m) X[k * RSTRIDE + zcX + LX.SZ * m] = v[k][m];
+    if (F2) Fz[k * RSTRIDE + a + N * b] = v[k][0] + v[k][N - 1];
     line_op<N, T>(A, 2, v[k], nbv[k][2][0], nbv[k][2][1], rz[k]);
   }
   __syncthreads();
@@ -206,12 +219,14 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     // ---- x line (y, z) = (a, b): node (m, a, b) at m + N a + N2 b ----
 #pragma unroll
     for (int m = 0; m < N; ++m) u[m] = X[k * RSTRIDE + xlX + LX.SX * m];
+    if (F2) Fx[k * RSTRIDE + a + N * b] = u[0] + u[N - 1];
     line_op<N, T>(A, 0, u, nbv[k][0][0], nbv[k][0][1], r);
 #pragma unroll
     for (int m = 0; m < N; ++m) R1[k * RSTRIDE + xl1 + L1.SX * m] = r[m];
     // ---- y line (x, z) = (a, b): node (a, m, b) at a + N m + N2 b ----
 #pragma unroll
     for (int m = 0; m < N; ++m) u[m] = X[k * RSTRIDE + ylX + LX.SY * m];
+    if (F2) Fy[k * RSTRIDE + a + N * b] = u[0] + u[N - 1];
     line_op<N, T>(A, 1, u, nbv[k][1][0], nbv[k][1][1], r);
 #pragma unroll
     for (int m = 0; m < N; ++m) R2[k * RSTRIDE + yl2 + L2.SY * m] = r[m];
@@ -225,12 +240,27 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
       v[k][m] = rz[k][m] + R1[k * RSTRIDE + zc1 + L1.SZ * m] + R2[k * RSTRIDE + zc2 + L2.SZ * m];
   if (MASS) {
     // M = M1 (x) M1 (x) M1: z in registers, then x and y lines in X (its
-    // line reads ended at the barrier above)
+    // line reads ended at the barrier above); with F2 the face arrays get
+    // Tp along their first and second coordinate in the same phases (3 n
+    // face lines per cell over its n^2 threads)
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       eo_apply<N, 1>(A.M, v[k], v[k]);
 #pragma unroll
       for (int m = 0; m < N; ++m) X[k * RSTRIDE + zcX + LX.SZ * m] = v[k][m];
+    }
+    for (int task = t; F2 && task < 3 * N; task += N * N) {
+      const int arr = task / N, j = task - arr * N;
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        T u[N];
+        T *Fa = Fx + k * RSTRIDE + arr * N * N + N * j;
+#pragma unroll
+        for (int i = 0; i < N; ++i) u[i] = Fa[i];
+        eo_apply<N, 1>(A.Tp, u, u);
+#pragma unroll
+        for (int i = 0; i < N; ++i) Fa[i] = u[i];
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -241,6 +271,19 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
       eo_apply<N, 1>(A.M, u, u);
 #pragma unroll
       for (int m = 0; m < N; ++m) X[k * RSTRIDE + xlX + LX.SX * m] = u[m];
+    }
+    for (int task = t; F2 && task < 3 * N; task += N * N) {
+      const int arr = task / N, i = task - arr * N;
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        T u[N];
+        T *Fa = Fx + k * RSTRIDE + arr * N * N + i;
+#pragma unroll
+        for (int j = 0; j < N; ++j) u[j] = Fa[N * j];
+        eo_apply<N, 1>(A.Tp, u, u);
+#pragma unroll
+        for (int j = 0; j < N; ++j) Fa[N * j] = u[j];
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -257,6 +300,21 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     for (int k = 0; k < R; ++k)
 #pragma unroll
       for (int m = 0; m < N; ++m) v[k][m] = X[k * RSTRIDE + zcX + LX.SZ * m];
+    if (F2) {
+      // node (a, b, m): the z face term at layer m, the x face term at layer
+      // a (face point (y, z) = (b, m)), the y face term at layer b ((x, z) = (a, m))
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const T tz = Fz[k * RSTRIDE + a + N * b];
+        const T cx = A.f2c[0][a], cy = A.f2c[1][b];
+#pragma unroll
+        for (int m = 0; m < N; ++m) {
+          T acc = fma(A.f2c[2][m], tz, v[k][m]);
+          acc = fma(cx, Fx[k * RSTRIDE + b + N * m], acc);
+          v[k][m] = fma(cy, Fy[k * RSTRIDE + a + N * m], acc);
+        }
+      }
+    }
   }
   // ---- store the z columns (plain, fused Chebyshev or Runge-Kutta update) ----
 #pragma unroll
@@ -300,7 +358,50 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
 // S^-1 W^-1 otherwise (the mass sweeps then use M1 = S^T W S without jxw).
 struct Tensor1D {
   double B[3][kMaxN][kMaxN], cl[3][kMaxN], cr[3][kMaxN], M1[kMaxN][kMaxN];
+  bool f2;                                    // DO_FACES Laplacian face term
+  double Tp[kMaxN][kMaxN], f2c[3][kMaxN];
 };
+
+// M1 = S^T W S
+void mass_1d(const Shape1D &s, double (&M1)[kMaxN][kMaxN])
+{
+  for (int i = 0; i < s.n; ++i)
+    for (int j = 0; j < s.n; ++j) {
+      double m = 0.0;
+      for (int q = 0; q < s.n; ++q) m += s.S[q][i] * s.wq[q] * s.S[q][j];
+      M1[i][j] = m;
+    }
+}
+
+// B = M1^-1 L by Gaussian elimination with partial pivoting (L is overwritten)
+void solve_mass(int n, const double (&M1)[kMaxN][kMaxN], double (&L)[kMaxN][kMaxN], double (&B)[kMaxN][kMaxN])
+{
+  double Mw[kMaxN][kMaxN];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) Mw[i][j] = M1[i][j];
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(Mw[r][c]) > std::fabs(Mw[piv][c])) piv = r;
+    for (int j = 0; j < n; ++j) {
+      std::swap(Mw[c][j], Mw[piv][j]);
+      std::swap(L[c][j], L[piv][j]);
+    }
+    for (int r = c + 1; r < n; ++r) {
+      const double fct = Mw[r][c] / Mw[c][c];
+      for (int j = 0; j < n; ++j) {
+        Mw[r][j] -= fct * Mw[c][j];
+        L[r][j] -= fct * L[c][j];
+      }
+    }
+  }
+  for (int c = n - 1; c >= 0; --c)
+    for (int j = 0; j < n; ++j) {
+      double v = L[c][j];
+      for (int k = c + 1; k < n; ++k) v -= Mw[c][k] * B[k][j];
+      B[c][j] = v / Mw[c][c];
+    }
+}
 
 Tensor1D advect_tensor_1d(const sf_op *op, bool transpose, bool invmass)
 {
@@ -311,12 +412,7 @@ Tensor1D advect_tensor_1d(const sf_op *op, bool transpose, bool invmass)
   double P[kMaxN][kMaxN];
   for (int i = 0; i < n; ++i)
     for (int q = 0; q < n; ++q) P[i][q] = s.Sinv[i][q] / s.wq[q] / (invmass ? jxw : 1.0);
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) {
-      double m = 0.0;
-      for (int q = 0; q < n; ++q) m += s.S[q][i] * s.wq[q] * s.S[q][j];
-      R.M1[i][j] = m;
-    }
+  mass_1d(s, R.M1);
   for (int d = 0; d < 3; ++d) {
     const double ij = 1.0 / op->h[d], jf = jxw * ij, ad = op->desc.velocity[d];
     const double c = ad * ij * jxw;
@@ -360,14 +456,115 @@ Tensor1D advect_tensor_1d(const sf_op *op, bool transpose, bool invmass)
   return R;
 }
 
+// The DO_FACES convection operator (cell-major, Hermite-like basis, each
+// cell's own faces at 0 and 1 as the two sides of one face,
+// evaluation_cell_laplacian.h:505-797) on Cartesian cells is
+// sum_f L_f (x) M1 (x) M1 with M1 = S^T W S and
+//   L_f = b_f ij_f jxw S^T D^T W S - jf (e_p - e_0) flux^T,
+//   flux = (b_f (e_p + e_0) + |b_f| (e_p - e_0)) / 2,
+// jf = jxw ij_f the face area (the value of the Hermite-like basis at a face
+// is its end coefficient).  Evaluated in the mass form with B_f = M1^-1 L_f
+// and no neighbour couplings.
+Tensor1D faces_convection_1d(const sf_op *op)
+{
+  const Shape1D &s = op->shape;
+  const int n = s.n, p = n - 1;
+  const double jxw = op->h[0] * op->h[1] * op->h[2];
+  Tensor1D R{};
+  mass_1d(s, R.M1);
+  for (int f = 0; f < 3; ++f) {
+    const double ij = 1.0 / op->h[f], jf = jxw * ij, bf = op->desc.velocity[f];
+    // L_f = b_f ij jxw S^T D^T W S, (D^T W S)[q][j] = sum_k D[k][q] w_k S[k][j]
+    double L[kMaxN][kMaxN];
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double acc = 0.0;
+        for (int q = 0; q < n; ++q) {
+          double ds = 0.0;
+          for (int k = 0; k < n; ++k) ds += s.D[k][q] * s.wq[k] * s.S[k][j];
+          acc += s.S[q][i] * ds;
+        }
+        L[i][j] = bf * ij * jxw * acc;
+      }
+    double flux[kMaxN] = {};
+    flux[p] += 0.5 * (bf + std::fabs(bf));
+    flux[0] += 0.5 * (bf - std::fabs(bf));
+    for (int j = 0; j < n; ++j) {
+      L[p][j] -= jf * flux[j];
+      L[0][j] += jf * flux[j];
+    }
+    solve_mass(n, R.M1, L, R.B[f]);
+  }
+  return R;
+}
+
+// The DO_FACES Laplacian (same source) on Cartesian cells is
+//   sum_f (K_f + F1_f) (x) M1 (x) M1 + sum_f F2_f (x) Tp (x) Tp,
+// K_f = jxw ij_f^2 (D S)^T W (D S), Tp = S W S (the reference interpolates
+// the derivative-test term of the face with S, not S^T), and with e_i the
+// unit vectors, sigma = n^2 ij_f, hd = phi_0'(0), jf = jxw ij_f:
+//   F1_f = jf (e_p - e_0) (sigma (e_p + e_0) - ij_f hd (e_{p-1} - e_p + e_1 - e_0) / 2)^T
+//   F2_f = -jf ij_f hd (-e_p + e_{p-1} - e_0 + e_1) (e_p + e_0)^T / 2.
+// The first sum runs in the mass form with B_f = M1^-1 (K_f + F1_f); the
+// second is rank one per direction: the sum of the two end layers, Tp along
+// both face directions, injected into layers 0, 1, p-1, p.
+Tensor1D faces_laplace_1d(const sf_op *op)
+{
+  const Shape1D &s = op->shape;
+  const int n = s.n, p = n - 1;
+  const double jxw = op->h[0] * op->h[1] * op->h[2], hd = s.hermite_d0;
+  Tensor1D R{};
+  R.f2 = true;
+  mass_1d(s, R.M1);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double m = 0.0;
+      for (int q = 0; q < n; ++q) m += s.S[i][q] * s.wq[q] * s.S[q][j];
+      R.Tp[i][j] = m;
+    }
+  double DS[kMaxN][kMaxN];
+  for (int q = 0; q < n; ++q)
+    for (int j = 0; j < n; ++j) {
+      double v = 0.0;
+      for (int k = 0; k < n; ++k) v += s.D[q][k] * s.S[k][j];
+      DS[q][j] = v;
+    }
+  for (int f = 0; f < 3; ++f) {
+    const double ij = 1.0 / op->h[f], jf = jxw * ij, sigma = double(n * n) * ij;
+    double L[kMaxN][kMaxN];
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double acc = 0.0;
+        for (int q = 0; q < n; ++q) acc += DS[q][i] * s.wq[q] * DS[q][j];
+        L[i][j] = jxw * ij * ij * acc;
+      }
+    double rowv[kMaxN] = {}, g[kMaxN] = {};
+    rowv[p] += sigma;
+    rowv[0] += sigma;
+    rowv[p - 1] -= 0.5 * ij * hd;
+    rowv[p] += 0.5 * ij * hd;
+    rowv[1] -= 0.5 * ij * hd;
+    rowv[0] += 0.5 * ij * hd;
+    for (int j = 0; j < n; ++j) {
+      L[p][j] += jf * rowv[j];
+      L[0][j] -= jf * rowv[j];
+    }
+    solve_mass(n, R.M1, L, R.B[f]);
+    g[p] -= 1.0;
+    g[p - 1] += 1.0;
+    g[0] -= 1.0;
+    g[1] += 1.0;
+    for (int i = 0; i < n; ++i) R.f2c[f][i] = -0.5 * jf * ij * hd * g[i];
+  }
+  return R;
+}
+
 template <int N, typename T>
-int advect_tensor_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T *y, const T *cb,
-                       const T *cdinv, T *ct, double c_np, double c_tm, const T *rk_upd, T *rk_np, T *rk_tm,
-                       cudaStream_t st)
+int line_sum_impl(const sf_op *op, const Tensor1D &R, bool invmass, int nrhs, const T *x, T *y, const T *cb,
+                  const T *cdinv, T *ct, double c_np, double c_tm, const T *rk_upd, T *rk_np, T *rk_tm,
+                  cudaStream_t st)
 {
   using Cfg = TACfg<N, T>;
-  const bool invmass = !transpose && op->desc.inverse_mass;
-  const Tensor1D R = advect_tensor_1d(op, transpose, invmass);
   TAArgs<N, T> A{};
   A.nbmask = 0;
   for (int d = 0; d < 3; ++d) {
@@ -384,6 +581,9 @@ int advect_tensor_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T 
     A.nc[d] = op->desc.n_cells[d];
   }
   A.M = make_eo<N, T>([&](int i, int j) { return R.M1[i][j]; });
+  A.Tp = make_eo<N, T>([&](int i, int j) { return R.Tp[i][j]; });
+  for (int d = 0; d < 3; ++d)
+    for (int i = 0; i < N; ++i) A.f2c[d][i] = T(R.f2c[d][i]);
   A.x = x;
   A.y = y;
   A.cb = cb;
@@ -406,7 +606,10 @@ int advect_tensor_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T 
   // 1737 us per LSRK step), nor in FP64, bound by the FP64 pipe
   const int rps = (nrhs > 1 && sizeof(T) == 4 && !rk) ? 2 : 1;
   void (*kern)(const TAArgs<N, T>);
-  if (rps == 2)
+  if (R.f2)
+    kern = rps == 2 ? dg_advect_tensor_kernel<N, T, true, TA_STORE, 2, true>
+                    : dg_advect_tensor_kernel<N, T, true, TA_STORE, 1, true>;
+  else if (rps == 2)
     kern = invmass ? dg_advect_tensor_kernel<N, T, false, TA_STORE, 2> : dg_advect_tensor_kernel<N, T, true, TA_STORE, 2>;
   else if (invmass)
     kern = rk ? dg_advect_tensor_kernel<N, T, false, TA_RK, 1>
@@ -414,7 +617,7 @@ int advect_tensor_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T 
   else
     kern = rk ? dg_advect_tensor_kernel<N, T, true, TA_RK, 1>
          : cheb ? dg_advect_tensor_kernel<N, T, true, TA_CHEB, 1> : dg_advect_tensor_kernel<N, T, true, TA_STORE, 1>;
-  const size_t smem = Cfg::SMEM * rps;
+  const size_t smem = (R.f2 ? Cfg::SMEM_F2 : Cfg::SMEM) * rps;
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    cudaSharedmemCarveoutMaxShared));
@@ -425,17 +628,34 @@ int advect_tensor_impl(const sf_op *op, int nrhs, bool transpose, const T *x, T 
 }
 
 template <int N>
-int advect_tensor_n(const sf_op *op, int prec, int nrhs, bool tr, const void *x, void *y, const void *cb,
-                    const void *cd, void *ct, double c_np, double c_tm, const void *upd, void *vnp, void *vtm,
-                    cudaStream_t st)
+int line_sum_n(const sf_op *op, const Tensor1D &R, bool invmass, int prec, int nrhs, const void *x, void *y,
+               const void *cb, const void *cd, void *ct, double c_np, double c_tm, const void *upd, void *vnp,
+               void *vtm, cudaStream_t st)
 {
   if (prec == SF_FP64)
-    return advect_tensor_impl<N, double>(op, nrhs, tr, (const double *)x, (double *)y, (const double *)cb,
-                                         (const double *)cd, (double *)ct, c_np, c_tm, (const double *)upd,
-                                         (double *)vnp, (double *)vtm, st);
-  return advect_tensor_impl<N, float>(op, nrhs, tr, (const float *)x, (float *)y, (const float *)cb,
-                                      (const float *)cd, (float *)ct, c_np, c_tm, (const float *)upd,
-                                      (float *)vnp, (float *)vtm, st);
+    return line_sum_impl<N, double>(op, R, invmass, nrhs, (const double *)x, (double *)y, (const double *)cb,
+                                    (const double *)cd, (double *)ct, c_np, c_tm, (const double *)upd,
+                                    (double *)vnp, (double *)vtm, st);
+  return line_sum_impl<N, float>(op, R, invmass, nrhs, (const float *)x, (float *)y, (const float *)cb,
+                                 (const float *)cd, (float *)ct, c_np, c_tm, (const float *)upd, (float *)vnp,
+                                 (float *)vtm, st);
+}
+
+int line_sum_dispatch(const sf_op *op, const Tensor1D &R, bool invmass, int prec, int nrhs, const void *x,
+                      void *y, const void *cb, const void *cd, void *ct, double c_np, double c_tm, const void *upd,
+                      void *vnp, void *vtm, cudaStream_t st)
+{
+  switch (op->desc.degree) {
+  case 1: return line_sum_n<2>(op, R, invmass, prec, nrhs, x, y, cb, cd, ct, c_np, c_tm, upd, vnp, vtm, st);
+  case 2: return line_sum_n<3>(op, R, invmass, prec, nrhs, x, y, cb, cd, ct, c_np, c_tm, upd, vnp, vtm, st);
+  case 3: return line_sum_n<4>(op, R, invmass, prec, nrhs, x, y, cb, cd, ct, c_np, c_tm, upd, vnp, vtm, st);
+  case 4: return line_sum_n<5>(op, R, invmass, prec, nrhs, x, y, cb, cd, ct, c_np, c_tm, upd, vnp, vtm, st);
+  case 5: return line_sum_n<6>(op, R, invmass, prec, nrhs, x, y, cb, cd, ct, c_np, c_tm, upd, vnp, vtm, st);
+  case 6: return line_sum_n<7>(op, R, invmass, prec, nrhs, x, y, cb, cd, ct, c_np, c_tm, upd, vnp, vtm, st);
+  case 7: return line_sum_n<8>(op, R, invmass, prec, nrhs, x, y, cb, cd, ct, c_np, c_tm, upd, vnp, vtm, st);
+  case 8: return line_sum_n<9>(op, R, invmass, prec, nrhs, x, y, cb, cd, ct, c_np, c_tm, upd, vnp, vtm, st);
+  default: set_error("unsupported degree"); return SF_ERR_UNSUPPORTED;
+  }
 }
 
 } // namespace
@@ -445,17 +665,18 @@ int launch_dg_advect_tensor(const sf_op *op, int prec, int nrhs, bool transpose,
                             const void *rk_upd, void *rk_np, void *rk_tm, cudaStream_t st)
 {
   if (op->desc.kind != SF_OP_DG_ADVECT) return SF_ERR_STATE;
-  switch (op->desc.degree) {
-  case 1: return advect_tensor_n<2>(op, prec, nrhs, transpose, x, y, cheb_b, cheb_dinv, cheb_t, c_np, c_tm, rk_upd, rk_np, rk_tm, st);
-  case 2: return advect_tensor_n<3>(op, prec, nrhs, transpose, x, y, cheb_b, cheb_dinv, cheb_t, c_np, c_tm, rk_upd, rk_np, rk_tm, st);
-  case 3: return advect_tensor_n<4>(op, prec, nrhs, transpose, x, y, cheb_b, cheb_dinv, cheb_t, c_np, c_tm, rk_upd, rk_np, rk_tm, st);
-  case 4: return advect_tensor_n<5>(op, prec, nrhs, transpose, x, y, cheb_b, cheb_dinv, cheb_t, c_np, c_tm, rk_upd, rk_np, rk_tm, st);
-  case 5: return advect_tensor_n<6>(op, prec, nrhs, transpose, x, y, cheb_b, cheb_dinv, cheb_t, c_np, c_tm, rk_upd, rk_np, rk_tm, st);
-  case 6: return advect_tensor_n<7>(op, prec, nrhs, transpose, x, y, cheb_b, cheb_dinv, cheb_t, c_np, c_tm, rk_upd, rk_np, rk_tm, st);
-  case 7: return advect_tensor_n<8>(op, prec, nrhs, transpose, x, y, cheb_b, cheb_dinv, cheb_t, c_np, c_tm, rk_upd, rk_np, rk_tm, st);
-  case 8: return advect_tensor_n<9>(op, prec, nrhs, transpose, x, y, cheb_b, cheb_dinv, cheb_t, c_np, c_tm, rk_upd, rk_np, rk_tm, st);
-  default: set_error("unsupported degree"); return SF_ERR_UNSUPPORTED;
-  }
+  const bool invmass = !transpose && op->desc.inverse_mass;
+  const Tensor1D R = advect_tensor_1d(op, transpose, invmass);
+  return line_sum_dispatch(op, R, invmass, prec, nrhs, x, y, cheb_b, cheb_dinv, cheb_t, c_np, c_tm, rk_upd, rk_np,
+                           rk_tm, st);
+}
+
+int launch_faces_tensor(const sf_op *op, int prec, int nrhs, const void *x, void *y, cudaStream_t st)
+{
+  if (op->desc.kind != SF_OP_CONVECTION_FACES && op->desc.kind != SF_OP_LAPLACE_FACES) return SF_ERR_STATE;
+  const Tensor1D R = op->desc.kind == SF_OP_LAPLACE_FACES ? faces_laplace_1d(op) : faces_convection_1d(op);
+  return line_sum_dispatch(op, R, false, prec, nrhs, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, nullptr, nullptr,
+                           nullptr, st);
 }
 
 } // namespace sf

@@ -42,6 +42,9 @@ int launch_dg_precomputed_diagonal(const sf_op *op, int prec, void *diag, cudaSt
 int launch_dg_advect_tensor(const sf_op *op, int prec, int nrhs, bool transpose, const void *x, void *y,
                             const void *cheb_b, const void *cheb_dinv, void *cheb_t, double c_np, double c_tm,
                             const void *rk_upd, void *rk_np, void *rk_tm, cudaStream_t st);
+// the DO_FACES operators in the same form: sum_f L_f (x) M1 (x) M1 (plus, for
+// the Laplacian, a rank-one face term per direction)
+int launch_faces_tensor(const sf_op *op, int prec, int nrhs, const void *x, void *y, cudaStream_t st);
 
 // sf_cell_faces.cu: the DO_FACES cell operators (block diagonal, cell-major)
 int launch_cell_faces(const sf_op *op, int prec, int nrhs, const void *x, void *y, cudaStream_t st);

@@ -65,6 +65,37 @@ def test_cell_faces_vs_oracle(p):
         assert op.device_status() == 0
 
 
+@pytest.mark.parametrize("p", range(1, 9))
+def test_cell_faces_line_operators_equal_face_kernel(p):
+    """SF_OP_LAPLACE_FACES and SF_OP_CONVECTION_FACES through the line-operator
+    kernel (default: sum_f L_f (x) M1 (x) M1, plus the rank-one face term of
+    the Laplacian) and through the face-array kernel: both against the oracle
+    and each other, two right-hand sides in one launch"""
+    torch = torch_cuda()
+    sf = _sf()
+    nc, length, b = (3, 2, 5), (0.9, 0.5, 1.3), (0.7, -1.3, 0.4)
+    h = tuple(L / n for L, n in zip(length, nc))
+    C = nc[0] * nc[1] * nc[2]
+    N = C * (p + 1) ** 3
+    X = np.random.default_rng(70 + p).uniform(-1, 1, 2 * N)
+    for kind, conv in _kinds(sf):
+        refs = [O.cell_faces_apply(p, conv, C, h, X[r * N:(r + 1) * N], b) for r in range(2)]
+        op = sf.Operator(kind, degree=p, n_cells=nc, length=length, velocity=b)
+        out = {}
+        for variant in (sf.KERNEL_AUTO, sf.KERNEL_GENERIC):
+            op.set_kernel_variant(variant)
+            for dtype, tol in ((torch.float64, FP64_TOL), (torch.float32, 2 * FP32_TOL[p])):
+                xd = to_dev(torch, X, dtype)
+                y = torch.full_like(xd, float("nan"))
+                op.vmult_batched(xd, y, 2)
+                for r in range(2):
+                    assert rel(to_np(y[r * N:(r + 1) * N]), refs[r]) < tol, (kind, variant, dtype, r)
+                if dtype == torch.float64:
+                    out[variant] = to_np(y)
+        assert rel(out[sf.KERNEL_AUTO], out[sf.KERNEL_GENERIC]) < FP64_TOL, kind
+        assert op.device_status() == 0
+
+
 def test_cell_faces_block_diagonal_48():
     """48^3 cells, p=4 (13.8 M entries): cells do not couple (changing one
     cell's input changes that cell's output only, bit for bit elsewhere), and

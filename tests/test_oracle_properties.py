@@ -265,3 +265,42 @@ def test_advect_is_sum_of_line_operators(p):
                     Y = np.moveaxis(np.moveaxis(Y, nax, -1) @ M1.T, -1, nax)
             ref = O.dg_advect_apply_transpose(g, x) if tr else O.dg_advect_apply(g, x)
             assert np.linalg.norm(Y.ravel() - ref) / np.linalg.norm(ref) < 1e-13, (nc, invm, tr)
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_cell_faces_are_kronecker_sums(p):
+    """The DO_FACES cell operators on a Cartesian cell (Hermite-like basis,
+    M1 = S^T W S): convection = sum_f L_f (x) M1 (x) M1 with
+    L_f = b_f ij_f jxw S^T D^T W S - jf (e_p - e_0) flux^T; Laplacian =
+    sum_f (K_f + F1_f) (x) M1 (x) M1 + sum_f F2_f (x) Tp (x) Tp with
+    Tp = S W S, K_f = jxw ij_f^2 (D S)^T W (D S) and rank-one face terms
+    F1_f, F2_f: the identities behind the line-operator evaluation of
+    SF_OP_CONVECTION_FACES and SF_OP_LAPLACE_FACES"""
+    n = p + 1
+    sh = O.shape_arrays(p, O.BASIS_HERMITE)
+    S, D, w, hd = sh["S"], sh["D"], sh["wq"], sh["hermite_d0"]
+    M1, Tp, DS = S.T @ np.diag(w) @ S, S @ np.diag(w) @ S, D @ S
+    h = (0.3, 0.2, 0.45)
+    ij, jxw = [1 / v for v in h], h[0] * h[1] * h[2]
+    b = (1.0, 0.5, -0.25)
+    E, n3 = np.eye(n), n ** 3
+    for conv in (True, False):
+        K = np.stack([O.cell_faces(p, conv, ij, jxw, b if conv else (0., 0., 0.), e) for e in np.eye(n3)], axis=1)
+        Kc = np.zeros_like(K)
+        for f in range(3):
+            jf = jxw * ij[f]
+            terms = []
+            if conv:
+                flux = 0.5 * (b[f] * (E[p] + E[0]) + abs(b[f]) * (E[p] - E[0]))
+                L = b[f] * ij[f] * jxw * S.T @ D.T @ np.diag(w) @ S - jf * np.outer(E[p] - E[0], flux)
+                terms.append((L, M1))
+            else:
+                rowv = n * n * ij[f] * (E[p] + E[0]) - 0.5 * ij[f] * hd * (E[p - 1] - E[p] + E[1] - E[0])
+                L = jxw * ij[f] ** 2 * DS.T @ np.diag(w) @ DS + jf * np.outer(E[p] - E[0], rowv)
+                F2 = -jf * ij[f] * hd * np.outer(-E[p] + E[p - 1] - E[0] + E[1], 0.5 * (E[p] + E[0]))
+                terms += [(L, M1), (F2, Tp)]
+            for A_f, T_t in terms:
+                mats = [T_t, T_t, T_t]
+                mats[f] = A_f
+                Kc += np.kron(mats[2], np.kron(mats[1], mats[0]))
+        assert np.abs(K - Kc).max() < 1e-13 * np.abs(K).max(), conv
