@@ -501,6 +501,10 @@ int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, voi
   if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
   cudaStream_t st = (cudaStream_t)stream;
   const Region region(op->region_mv);
+  // line operators: A^T, or A^T M^-1 in one launch
+  if (advect_tensor(op))
+    return launch_dg_advect_tensor(op, prec, nrhs, true, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, nullptr,
+                                   nullptr, nullptr, st);
   const void *src = x;
   if (op->desc.inverse_mass) {
     const size_t bytes = (size_t)nrhs * op->n_dofs * elem_size(prec);
@@ -508,9 +512,6 @@ int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, voi
     SF_RET(launch_dg_inverse_mass(op, prec, nrhs, x, op->scratch.ptr, st));
     src = op->scratch.ptr;
   }
-  if (advect_tensor(op))
-    return launch_dg_advect_tensor(op, prec, nrhs, true, src, y, nullptr, nullptr, nullptr, 0.0, 0.0, nullptr,
-                                   nullptr, nullptr, st);
   return launch_dg_vmult(op, prec, nrhs, true, src, y, nullptr, nullptr, nullptr, 0.0, 0.0, st);
 }
 

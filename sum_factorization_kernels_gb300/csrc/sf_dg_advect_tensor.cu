@@ -51,6 +51,9 @@ struct TAArgs {
   // DO_FACES Laplacian: sum_f F2_f (x) Tp (x) Tp with F2_f = f2c[f] (e_p + e_0)^T
   EOMat<N, T> Tp;
   T f2c[3][N];
+  // neighbour-line couplings (transpose with the inverse mass): the value of
+  // side s is sum_m wnb[s][m] u_m over the neighbour's whole line
+  T wnb[2][N];
   const T *__restrict__ x;
   T *__restrict__ y;
   const T *__restrict__ cb;    // Chebyshev: rhs
@@ -129,11 +132,12 @@ __device__ __forceinline__ void line_op(const TAArgs<N, T> &A, int d, const T (&
 // R right-hand sides per thread (blockIdx.y covers R of them): the cell's
 // neighbour and address arithmetic is shared and R times as many loads are in
 // flight; each right-hand side has slabs of its own
-template <int N, typename T, bool MASS, int EPI, int R, bool F2 = false>
+template <int N, typename T, bool MASS, int EPI, int R, bool F2 = false, bool NBL = false>
 __global__ void __launch_bounds__(DGCells<N>::value *N *N)
     dg_advect_tensor_kernel(const __grid_constant__ TAArgs<N, T> A)
 {
   static_assert(!F2 || (MASS && EPI == TA_STORE), "face term: mass form, plain store");
+  static_assert(!NBL || (!MASS && EPI == TA_STORE), "neighbour lines: line form, plain store");
   using Cfg = TACfg<N, T>;
   constexpr int N2 = N * N, N3 = N * N * N;
   constexpr int CPB = Cfg::CPB;
@@ -178,9 +182,13 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   }
   // neighbour end values of this thread's z column, x line and y line:
   // (a, b, n-1) / (a, b, 0), (n-1, a, b) / (0, a, b), (a, n-1, b) / (a, 0, b)
-  const long long off[3][2] = {{nb[0][0] * N3 + (N - 1) + N * a + N2 * b, nb[0][1] * N3 + N * a + N2 * b},
-                               {nb[1][0] * N3 + a + N * (N - 1) + N2 * b, nb[1][1] * N3 + a + N2 * b},
-                               {nb[2][0] * N3 + t + N2 * (N - 1), nb[2][1] * N3 + t}};
+  // (NBL: the start of the neighbour's line through the same face point,
+  // node stride 1, N, N^2 for x, y, z)
+  const long long off[3][2] =
+      {{nb[0][0] * N3 + (NBL ? 0 : N - 1) + N * a + N2 * b, nb[0][1] * N3 + N * a + N2 * b},
+       {nb[1][0] * N3 + a + (NBL ? 0 : N * (N - 1)) + N2 * b, nb[1][1] * N3 + a + N2 * b},
+       {nb[2][0] * N3 + t + (NBL ? 0 : N2 * (N - 1)), nb[2][1] * N3 + t}};
+  constexpr int lstride[3] = {1, N, N2};
   const bool use[3][2] = {{(A.nbmask & 1) != 0, (A.nbmask & 2) != 0},
                           {(A.nbmask & 4) != 0, (A.nbmask & 8) != 0},
                           {(A.nbmask & 16) != 0, (A.nbmask & 32) != 0}};
@@ -197,7 +205,18 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
 #pragma unroll
     for (int d = 0; d < 3; ++d)
 #pragma unroll
-      for (int sd = 0; sd < 2; ++sd) nbv[k][d][sd] = on[k] && use[d][sd] ? __ldg(x + off[d][sd]) : T(0);
+      for (int sd = 0; sd < 2; ++sd) {
+        if (NBL) {
+          T acc = T(0);
+          if (on[k] && use[d][sd]) {
+#pragma unroll
+            for (int m = 0; m < N; ++m) acc = fma(A.wnb[sd][m], __ldg(x + off[d][sd] + lstride[d] * m), acc);
+          }
+          nbv[k][d][sd] = acc;
+        } else {
+          nbv[k][d][sd] = on[k] && use[d][sd] ? __ldg(x + off[d][sd]) : T(0);
+        }
+      }
     if (EPI == TA_RK) {
 #pragma unroll
       for (int m = 0; m < N; ++m)
@@ -360,6 +379,8 @@ struct Tensor1D {
   double B[3][kMaxN][kMaxN], cl[3][kMaxN], cr[3][kMaxN], M1[kMaxN][kMaxN];
   bool f2;                                    // DO_FACES Laplacian face term
   double Tp[kMaxN][kMaxN], f2c[3][kMaxN];
+  bool nbline;                                // couplings through whole neighbour lines
+  double wnb[2][kMaxN];
 };
 
 // M1 = S^T W S
@@ -559,6 +580,57 @@ Tensor1D faces_laplace_1d(const sf_op *op)
   return R;
 }
 
+// The transpose with the inverse mass, A^T M^-1.  With A^T = M1^{x3}
+// (sum_d B'_d (x) I (x) I + couplings) from advect_tensor_1d(transpose, no
+// inverse mass) and M^-1 = (M1^-1)^{x3} / jxw, the tangential M1 and M1^-1
+// cancel:
+//   A^T M^-1 = sum_d C_d (x) I (x) I / jxw,  C_d = M1 B'_d M1^-1,
+// and the coupling of side s becomes (M1 c_s) times the dot product of row
+// n-1 (left neighbour) or row 0 (right neighbour) of M1^-1 with the
+// neighbour's whole line: one launch instead of an inverse-mass pass and the
+// transposed apply.
+Tensor1D advect_transpose_invmass_1d(const sf_op *op)
+{
+  const int n = op->shape.n;
+  const double jxw = op->h[0] * op->h[1] * op->h[2];
+  const Tensor1D T0 = advect_tensor_1d(op, true, false);
+  Tensor1D R{};
+  R.nbline = true;
+  double Minv[kMaxN][kMaxN], I[kMaxN][kMaxN] = {};
+  for (int i = 0; i < n; ++i) I[i][i] = 1.0;
+  solve_mass(n, T0.M1, I, Minv);
+  for (int m = 0; m < n; ++m) {
+    R.wnb[0][m] = Minv[n - 1][m];
+    R.wnb[1][m] = Minv[0][m];
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) R.M1[i][j] = T0.M1[i][j];
+  for (int d = 0; d < 3; ++d) {
+    double MB[kMaxN][kMaxN];
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double v = 0.0;
+        for (int k = 0; k < n; ++k) v += T0.M1[i][k] * T0.B[d][k][j];
+        MB[i][j] = v;
+      }
+    for (int i = 0; i < n; ++i) {
+      for (int j = 0; j < n; ++j) {
+        double v = 0.0;
+        for (int k = 0; k < n; ++k) v += MB[i][k] * Minv[k][j];
+        R.B[d][i][j] = v / jxw;
+      }
+      double l = 0.0, r = 0.0;
+      for (int k = 0; k < n; ++k) {
+        l += T0.M1[i][k] * T0.cl[d][k];
+        r += T0.M1[i][k] * T0.cr[d][k];
+      }
+      R.cl[d][i] = l / jxw;
+      R.cr[d][i] = r / jxw;
+    }
+  }
+  return R;
+}
+
 template <int N, typename T>
 int line_sum_impl(const sf_op *op, const Tensor1D &R, bool invmass, int nrhs, const T *x, T *y, const T *cb,
                   const T *cdinv, T *ct, double c_np, double c_tm, const T *rk_upd, T *rk_np, T *rk_tm,
@@ -584,6 +656,8 @@ int line_sum_impl(const sf_op *op, const Tensor1D &R, bool invmass, int nrhs, co
   A.Tp = make_eo<N, T>([&](int i, int j) { return R.Tp[i][j]; });
   for (int d = 0; d < 3; ++d)
     for (int i = 0; i < N; ++i) A.f2c[d][i] = T(R.f2c[d][i]);
+  for (int sd = 0; sd < 2; ++sd)
+    for (int i = 0; i < N; ++i) A.wnb[sd][i] = T(R.wnb[sd][i]);
   A.x = x;
   A.y = y;
   A.cb = cb;
@@ -609,6 +683,9 @@ int line_sum_impl(const sf_op *op, const Tensor1D &R, bool invmass, int nrhs, co
   if (R.f2)
     kern = rps == 2 ? dg_advect_tensor_kernel<N, T, true, TA_STORE, 2, true>
                     : dg_advect_tensor_kernel<N, T, true, TA_STORE, 1, true>;
+  else if (R.nbline)
+    kern = rps == 2 ? dg_advect_tensor_kernel<N, T, false, TA_STORE, 2, false, true>
+                    : dg_advect_tensor_kernel<N, T, false, TA_STORE, 1, false, true>;
   else if (rps == 2)
     kern = invmass ? dg_advect_tensor_kernel<N, T, false, TA_STORE, 2> : dg_advect_tensor_kernel<N, T, true, TA_STORE, 2>;
   else if (invmass)
@@ -665,6 +742,13 @@ int launch_dg_advect_tensor(const sf_op *op, int prec, int nrhs, bool transpose,
                             const void *rk_upd, void *rk_np, void *rk_tm, cudaStream_t st)
 {
   if (op->desc.kind != SF_OP_DG_ADVECT) return SF_ERR_STATE;
+  if (transpose && op->desc.inverse_mass) {
+    // A^T M^-1 in one launch (no Chebyshev or Runge-Kutta epilogue here)
+    if (cheb_b || rk_np) return SF_ERR_STATE;
+    const Tensor1D R = advect_transpose_invmass_1d(op);
+    return line_sum_dispatch(op, R, true, prec, nrhs, x, y, nullptr, nullptr, nullptr, 0.0, 0.0, nullptr, nullptr,
+                             nullptr, st);
+  }
   const bool invmass = !transpose && op->desc.inverse_mass;
   const Tensor1D R = advect_tensor_1d(op, transpose, invmass);
   return line_sum_dispatch(op, R, invmass, prec, nrhs, x, y, cheb_b, cheb_dinv, cheb_t, c_np, c_tm, rk_upd, rk_np,

@@ -227,7 +227,9 @@ def test_advect_is_sum_of_line_operators(p):
     value; M = jxw M1 (x) M1 (x) M1, M1 = S^T W S.  The identity behind the
     line-operator advection kernel, checked for the forward operator (with
     and without the inverse mass) and the transpose, on a mesh with a
-    one-cell-thick direction and a negative velocity component"""
+    one-cell-thick direction and a negative velocity component; and the
+    transpose with the inverse mass as one sum of line operators whose
+    couplings read the neighbour's whole line"""
     n = p + 1
     sh = O.shape_arrays(p)
     S, D, Sinv, w, fv = sh["S"], sh["D"], sh["Sinv"], sh["wq"], sh["face_v"]
@@ -265,6 +267,31 @@ def test_advect_is_sum_of_line_operators(p):
                     Y = np.moveaxis(np.moveaxis(Y, nax, -1) @ M1.T, -1, nax)
             ref = O.dg_advect_apply_transpose(g, x) if tr else O.dg_advect_apply(g, x)
             assert np.linalg.norm(Y.ravel() - ref) / np.linalg.norm(ref) < 1e-13, (nc, invm, tr)
+        # the transpose with the inverse mass, A^T M^-1 = sum_d C_d (x) I (x) I / jxw with
+        # C_d = M1 B'_d M1^-1, each coupling through a row of M1^-1 and the neighbour's line
+        g = O.dg(p, nc, h, velocity=vel, inverse_mass=1)
+        x = np.random.default_rng(p).uniform(-1, 1, O.dg_n_dofs(g))
+        Minv = np.linalg.inv(M1)
+        P = Sinv / w[None, :]
+        X = x.reshape(nc[2], nc[1], nc[0], n, n, n)
+        Y = np.zeros_like(X)
+        for d, (cax, nax) in enumerate(((2, 5), (1, 4), (0, 3))):
+            ij, ad = 1 / h[d], vel[d]
+            c, jf = ad * ij * jxw, jxw * ij
+            R = c * np.diag(w) @ D
+            nb = []
+            for side in range(2):
+                an = ad if side else -ad
+                fa = -0.5 * (an + abs(an)) * jf
+                R = R + fa * np.outer(fv[side], fv[side])
+                nb.append(M1 @ P @ (fv[side] * -fa) / jxw)
+            C = M1 @ (P @ R @ S) @ Minv / jxw
+            Xm = np.moveaxis(X, nax, -1)
+            lo = np.roll(Xm, 1, axis=cax) @ Minv[n - 1]
+            hi = np.roll(Xm, -1, axis=cax) @ Minv[0]
+            Y += np.moveaxis(Xm @ C.T + lo[..., None] * nb[0] + hi[..., None] * nb[1], -1, nax)
+        ref = O.dg_advect_apply_transpose(g, x)
+        assert np.linalg.norm(Y.ravel() - ref) / np.linalg.norm(ref) < 1e-13, (nc, "transpose, inverse mass")
 
 
 @pytest.mark.parametrize("p", range(1, 9))
