@@ -117,7 +117,11 @@ const char *sf_version(void);
  * (evaluation_cell_laplacian.h:34-101, evaluation_dg_laplacian.h:43-108,
  * evaluation_dg_advect.h:107-180, benchmark_loops.cc:1163-1200): builds the
  * shape tables and, for a deformed mesh, the per-quadrature-point geometry
- * on the device (FP64, plus an FP32 copy).  Synchronous. */
+ * on the device (FP64, plus an FP32 copy).  An affine continuous operator
+ * (SF_OP_LAPLACE with deform 0, SF_OP_MASS, SF_OP_CONVECTION) also gets the
+ * work vectors of its Kronecker passes: 2 (SF_OP_MASS: 1) vectors of n_dofs
+ * entries of the widest prepared precision, so that no apply allocates.
+ * Synchronous. */
 int sf_create(const sf_desc *desc, sf_op **op);
 int sf_destroy(sf_op *op);
 
@@ -231,10 +235,16 @@ int sf_diagonal(sf_op *op, int prec, void *diag, void *stream);
 int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void *dkappa,
                       void *stream);
 
-/* Kernel selection.  Continuous Laplacian: SF_KERNEL_AUTO and
- * SF_KERNEL_GENERIC both select the packed line-ownership kernel (one
- * thread per line of a cell, several cells per warp group), structured or
- * unstructured.  SF_OP_DG_SIPG: SF_KERNEL_AUTO evaluates the operator in its
+/* Kernel selection.  Continuous operators: SF_KERNEL_AUTO evaluates the
+ * affine structured ones without a coefficient (SF_OP_LAPLACE with deform 0
+ * and no sf_set_coefficient, SF_OP_MASS, SF_OP_CONVECTION) as Kronecker
+ * products of assembled 1D matrices (a pass along z, then x-y tiles of each
+ * node plane) in FP64, and in FP32 where that measured faster (degrees up
+ * to 5, the mass matrix up to 7); everything else (deformed, coefficient,
+ * unstructured, the remaining FP32 cases) runs on the packed
+ * line-ownership kernel (one thread per line of a cell, several cells per
+ * warp group); SF_KERNEL_GENERIC selects the line-ownership kernel for all
+ * of them.  Both give the same operator to rounding.  SF_OP_DG_SIPG: SF_KERNEL_AUTO evaluates the operator in its
  * tensor-product form (on these Cartesian meshes the SIPG bilinear form is
  * exactly L (x) M (x) M + M (x) L (x) M + M (x) M (x) L with 1D stiffness-
  * plus-face matrices L of penalty * (p+1)^2 and 1D mass matrices M: the

@@ -226,6 +226,15 @@ int sf_create(const sf_desc *desc, sf_op **out)
       return r;
     }
   }
+  if (kron_eligible(op)) {
+    // work vectors of the Kronecker passes, for the wider prepared precision
+    const size_t es = (d.precisions & 1) ? sizeof(double) : sizeof(float);
+    int r = op->kron.alloc(size_t(kron_work_vectors(op)) * size_t(op->n_dofs) * es);
+    if (r != SF_OK) {
+      delete op;
+      return r;
+    }
+  }
   *out = op;
   return SF_OK;
 }

@@ -86,6 +86,7 @@ struct sf_op {
   sf::DevBuf kap64, kap32;      // [cell][n^3] coefficient
   bool has_kappa = false;
   sf::DevBuf scratch;           // operator-private scratch (transpose, M^-1)
+  sf::DevBuf kron;              // work vectors of the Kronecker passes (affine continuous operators)
   sf::DevBuf geoLine64, geoLine32; // geometry in the line kernel's walk order
   std::unique_ptr<sf_unstructured> unstr; // SF_OP_LAPLACE_UNSTRUCTURED only
   sf::DevBuf dev_err;           // device error flags (bounded waits)

@@ -544,7 +544,9 @@ int cont_kgrad_n(const sf_op *op, int prec, const void *u, const void *l, void *
 
 int launch_cont_vmult(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
 {
-  // structured and unstructured meshes: the packed line-ownership kernel
+  // affine structured meshes without a coefficient: the Kronecker passes;
+  // otherwise (and with SF_KERNEL_GENERIC) the packed line-ownership kernel
+  if (kron_selected(op, prec)) return launch_cont_kron(op, prec, x, y, st);
   return launch_cont_vmult_line(op, prec, x, y, st);
 }
 

@@ -14,6 +14,14 @@ int launch_cont_kappa_grad(const sf_op *op, int prec, const void *u, const void 
 int launch_geometry(const sf_op *op, double *G, cudaStream_t st);
 int launch_cont_diagonal(const sf_op *op, int prec, void *diag, cudaStream_t st);
 
+// sf_cont_kron.cu: continuous Laplacian (affine, no coefficient), mass and
+// convection forms on structured meshes as Kronecker products of assembled
+// 1D matrices (a z pass and an x-y tile pass over the node grid)
+bool kron_eligible(const sf_op *op);
+int kron_work_vectors(const sf_op *op); // work vectors of n_dofs entries the passes need
+bool kron_selected(const sf_op *op, int prec); // the default apply of this precision uses them
+int launch_cont_kron(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st);
+
 // sf_laplace_line.cu (all degrees, FP64 and FP32)
 int launch_cont_vmult_line(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st);
 // walk-ordered copy of the FP64 geometry for the line kernel (geoLine64 / geoLine32)

@@ -116,3 +116,38 @@ def test_mass_cg_unpreconditioned():
         r = torch.empty_like(x)
         op.vmult(x, r)
         assert float((r - b).norm() / b.norm()) < 1e-9
+
+
+@pytest.mark.parametrize("basis", [0, 1])
+@pytest.mark.parametrize("p", range(1, 9))
+def test_affine_kronecker_passes_equal_line_kernel(p, basis):
+    """The affine continuous Laplacian, mass and convection forms through the
+    Kronecker passes (default) and the line-ownership kernel
+    (SF_KERNEL_GENERIC): both against the oracle and each other, GLL and
+    Hermite-like bases, with and without Dirichlet conditions, a
+    one-cell-thick mesh and two right-hand sides"""
+    torch = torch_cuda()
+    sf = _sf()
+    b = (0.7, -1.3, 0.4)
+    for nc, length, dirichlet in (((5, 3, 4), (1.0, 0.6, 0.9), 1), ((1, 3, 2), (0.5, 1.0, 0.8), 0),
+                                  ((2, 1, 3), (1.0, 0.4, 0.75), 1)):
+        m = O.mesh(p, nc, basis=basis, length=length, dirichlet=dirichlet)
+        N = O.cont_n_dofs(m)
+        X = np.random.default_rng(p + 3 * basis + sum(nc)).uniform(-1, 1, 2 * N)
+        for kind, okind in ((sf.OP_LAPLACE, None), (sf.OP_MASS, O.OP_MASS), (sf.OP_CONVECTION, O.OP_CONVECTION)):
+            refs = [O.cont_apply(m, None, X[r * N:(r + 1) * N]) if okind is None
+                    else O.cont_apply_op(m, okind, X[r * N:(r + 1) * N], b) for r in range(2)]
+            op = sf.Operator(kind, degree=p, n_cells=nc, length=length, dirichlet=dirichlet, velocity=b,
+                             basis=basis)
+            out = {}
+            for variant in (sf.KERNEL_AUTO, sf.KERNEL_GENERIC):
+                op.set_kernel_variant(variant)
+                for dtype, tol in ((torch.float64, FP64_TOL), (torch.float32, 4 * FP32_TOL[p])):
+                    y = torch.full((2 * N,), float("nan"), dtype=dtype, device="cuda:0")
+                    op.vmult_batched(to_dev(torch, X, dtype), y, 2)
+                    for r in range(2):
+                        assert rel(to_np(y[r * N:(r + 1) * N]), refs[r]) < tol, (kind, nc, variant, dtype, r)
+                    if dtype == torch.float64:
+                        out[variant] = to_np(y)
+            assert rel(out[sf.KERNEL_AUTO], out[sf.KERNEL_GENERIC]) < FP64_TOL, (kind, nc)
+            assert op.device_status() == 0

@@ -331,3 +331,52 @@ def test_cell_faces_are_kronecker_sums(p):
                 mats[f] = A_f
                 Kc += np.kron(mats[2], np.kron(mats[1], mats[0]))
         assert np.abs(K - Kc).max() < 1e-13 * np.abs(K).max(), conv
+
+
+@pytest.mark.parametrize("basis", [0, 1])
+@pytest.mark.parametrize("p", range(1, 9))
+def test_affine_continuous_operators_are_assembled_kronecker_products(p, basis):
+    """On a structured affine mesh the assembled continuous mass, Laplacian and
+    convection operators are M_z M_y M_x, sum_d K_d (x) M (x) M and
+    sum_d C_d (x) M (x) M with assembled banded 1D matrices (cell matrices
+    h M1, K1 / h, b C1); with Dirichlet conditions every 1D matrix loses its
+    boundary rows and columns and the boundary rows become y = x: the
+    identity behind the Kronecker passes of the affine continuous apply"""
+    sh = O.shape_arrays(p, basis)
+    S, D, w = sh["S"], sh["D"], sh["wq"]
+    M1 = S.T @ np.diag(w) @ S
+    K1 = (D @ S).T @ np.diag(w) @ (D @ S)
+    C1 = S.T @ D.T @ np.diag(w) @ S
+    b = (0.7, -1.3, 0.4)
+
+    def assembled(A1, nc):
+        G = np.zeros((nc * p + 1, nc * p + 1))
+        for c in range(nc):
+            G[c * p:c * p + p + 1, c * p:c * p + p + 1] += A1
+        return G
+
+    def app(Az, Ay, Ax, X):
+        return np.einsum("ck,kyx->cyx", Az, np.einsum("bj,zjx->zbx", Ay, np.einsum("ai,zyi->zya", Ax, X)))
+
+    for nc, length, dirichlet in (((3, 2, 4), (0.9, 0.5, 1.3), 1), ((2, 1, 3), (1.0, 0.4, 0.75), 0),
+                                  ((1, 3, 2), (0.5, 1.0, 0.8), 1)):
+        h = [length[d] / nc[d] for d in range(3)]
+        m = O.mesh(p, nc, basis=basis, length=length, dirichlet=dirichlet)
+        x = np.random.default_rng(p).uniform(-1, 1, O.cont_n_dofs(m))
+        nn = [nc[d] * p + 1 for d in range(3)]
+        Pd = [np.diag(np.r_[1 - dirichlet, np.ones(nn[d] - 2), 1 - dirichlet]) for d in range(3)]
+        Md = [Pd[d] @ assembled(h[d] * M1, nc[d]) @ Pd[d] for d in range(3)]
+        Kd = [Pd[d] @ assembled(K1 / h[d], nc[d]) @ Pd[d] for d in range(3)]
+        Cd = [Pd[d] @ assembled(b[d] * C1, nc[d]) @ Pd[d] for d in range(3)]
+        X = x.reshape(nn[2], nn[1], nn[0])
+        bnd = np.zeros_like(X, dtype=bool)
+        if dirichlet:
+            bnd[0] = bnd[-1] = bnd[:, 0] = bnd[:, -1] = bnd[:, :, 0] = bnd[:, :, -1] = True
+        cases = (("mass", O.cont_apply_op(m, O.OP_MASS, x, b), app(Md[2], Md[1], Md[0], X)),
+                 ("convection", O.cont_apply_op(m, O.OP_CONVECTION, x, b),
+                  app(Md[2], Md[1], Cd[0], X) + app(Md[2], Cd[1], Md[0], X) + app(Cd[2], Md[1], Md[0], X)),
+                 ("laplacian", O.cont_apply(m, None, x),
+                  app(Md[2], Md[1], Kd[0], X) + app(Md[2], Kd[1], Md[0], X) + app(Kd[2], Md[1], Md[0], X)))
+        for name, ref, Y in cases:
+            Y = np.where(bnd, X, Y).ravel()
+            assert np.linalg.norm(Y - ref) / np.linalg.norm(ref) < 1e-13, (name, nc)
