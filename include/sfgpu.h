@@ -175,15 +175,19 @@ int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, voi
  * that cannot allocate device memory while they run: applications that hand
  * out all device memory from their own pool or reserve a fixed budget up
  * front, and loops that cannot take the device synchronisation an
- * allocation implies.  No counterpart in the reference.  The intermediate
- * vector of the inverse-mass form comes from a 4 MiB array compiled into the
- * library (reserved on every GPU that loads it, until process exit) instead
- * of a cudaMalloc'd buffer; this function allocates nothing.  Only for
- * SF_OP_DG_ADVECT handles; nrhs * n_dofs * element size must not exceed
- * 4 MiB (SF_ERR_INVALID otherwise).  The first call on a device looks up the
+ * allocation implies.  No counterpart in the reference.  (The default
+ * line-operator path of sf_vmult_transpose_batched() applies K^T M^-1 in one
+ * launch and needs no intermediate vector; its cell-and-face path,
+ * SF_KERNEL_GENERIC, allocates one per handle on first use.)  This function
+ * always runs the cell-and-face two-pass form, with the intermediate vector
+ * of the inverse-mass form in a 4 MiB array compiled into the library
+ * (reserved on every GPU that loads it, until process exit) instead of a
+ * cudaMalloc'd buffer; it allocates nothing.  Only for SF_OP_DG_ADVECT
+ * handles; nrhs * n_dofs * element size must not exceed 4 MiB
+ * (SF_ERR_INVALID otherwise).  The first call on a device looks up the
  * array's device address once, and the first call with each degree and
- * precision loads that kernel; make those first calls before any stream
- * capture.  The address is not looked up again after cudaDeviceReset().
+ * precision loads that kernel.  The address is not looked up again after
+ * cudaDeviceReset().
  * All calls share the array (nothing in it needs to start at zero), so
  * calls whose work overlaps on the GPU race: keep them on one stream or
  * synchronise between them. */

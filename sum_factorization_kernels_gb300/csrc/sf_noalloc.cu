@@ -1,9 +1,11 @@
 // sf_noalloc.cu -- transposed DG advection apply that allocates nothing.
 //
 // The transpose of the inverse-mass advection operator, (M^-1 K)^T =
-// K^T M^-1, runs in two passes and needs an intermediate vector between
-// them.  sf_vmult_transpose_batched() keeps that vector in a per-handle
-// device buffer that it allocates with cudaMalloc on first use.  Some
+// K^T M^-1, runs in two passes in the cell-and-face form and needs an
+// intermediate vector between them.  sf_vmult_transpose_batched() with that
+// form (SF_KERNEL_GENERIC) keeps the vector in a per-handle device buffer
+// that it allocates with cudaMalloc on first use (its default line-operator
+// form needs none).  This entry point always runs the two-pass form.  Some
 // callers cannot allow that: applications that hand out all device memory
 // from their own pool or reserve a fixed budget up front, and must not see
 // a foreign allocation appear mid-run, and time-stepping loops where an
