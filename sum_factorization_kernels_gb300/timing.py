@@ -1,7 +1,8 @@
 """Time single operator applies through the C ABI (CUDA events, inputs in
 device memory): ``python -m sum_factorization_kernels_gb300.timing KIND ...``.
 
-KIND is ``laplace`` (continuous, deformed mesh), ``sipg`` (DG SIPG),
+KIND is ``laplace`` (continuous, the deformed mesh; ``--deform 0`` for the
+affine one), ``sipg`` (DG SIPG),
 ``advect`` (DG upwind advection with inverse mass), ``precomputed`` (DG
 SIPG in tensor-product form with precomputed 1D matrices), ``mass`` /
 ``convection`` (continuous, affine), ``unstructured`` (the affine box given
@@ -43,7 +44,7 @@ def unstructured_box(degree: int, ncells: int):
     return idx, geo, Nx ** 3
 
 
-def make_operator(kind: str, degree: int, ncells: int):
+def make_operator(kind: str, degree: int, ncells: int, deform: float = 0.05):
     n = (ncells,) * 3
     if kind == "mass":
         return sf.Operator(sf.OP_MASS, degree=degree, n_cells=n)
@@ -53,7 +54,7 @@ def make_operator(kind: str, degree: int, ncells: int):
         idx, geo, nn = unstructured_box(degree, ncells)
         return sf.Operator.unstructured(degree, idx, geo, nn)
     if kind == "laplace":
-        return sf.Operator(sf.OP_LAPLACE, degree=degree, n_cells=n, deform=0.05)
+        return sf.Operator(sf.OP_LAPLACE, degree=degree, n_cells=n, deform=deform)
     if kind == "sipg":
         return sf.Operator(sf.OP_DG_SIPG, degree=degree, n_cells=n)
     if kind == "advect":
@@ -114,11 +115,12 @@ def main(argv=None) -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--transpose", action="store_true", help="time the transposed apply")
     ap.add_argument("--rounds", type=int, default=16, help="sweeps: x and y sweeps per round")
+    ap.add_argument("--deform", type=float, default=0.05, help="laplace: mapping amplitude (0: affine)")
     a = ap.parse_args(argv)
     if a.kind == "sweeps":
         sweeps(a.degree, a.ncells, a.rounds, a.reps, a.warmup)
         return
-    op = make_operator(a.kind, a.degree, a.ncells)
+    op = make_operator(a.kind, a.degree, a.ncells, a.deform)
     dt = torch.float32 if a.prec == "fp32" else torch.float64
     n = op.n_dofs
     g = torch.Generator(device="cuda").manual_seed(1)
