@@ -547,6 +547,28 @@ def secondary_configs(stream, peak):
                      # the reference's memory model (test_dg_advect.cc:111-113)
                      "lsrk_step_gdofs_total_8rhs": round(8 * N / ts / 1e9, 3),
                      "lsrk_step_hbm_frac": round(20 * dt.itemsize * 8 * N / ts / 1e9 / peak, 4)}
+    # the cell-and-face kernel (SF_KERNEL_GENERIC) on the same FP32 batch
+    op.set_kernel_variant(sfgpu.KERNEL_GENERIC)
+    xx = (torch.rand(8 * N, device="cuda", dtype=torch.float64) * 2 - 1).to(torch.float32)
+    yy = torch.empty_like(xx)
+    for _ in range(3):
+        op.vmult_batched(xx, yy, 8, stream=stream)
+        op.vmult_transpose_batched(xx, yy, 8, stream=stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record(stream)
+    for _ in range(10):
+        op.vmult_batched(xx, yy, 8, stream=stream)
+    ev[1].record(stream)
+    for _ in range(10):
+        op.vmult_transpose_batched(xx, yy, 8, stream=stream)
+    ev[2].record(stream)
+    torch.cuda.synchronize()
+    check_status(op, "config 5 cell-and-face kernel")
+    res["fp32"]["cell_face_kernel"] = {
+        "forward_gdofs_total_8rhs": round(8 * N / (ev[0].elapsed_time(ev[1]) / 1e4) / 1e9, 3),
+        "transpose_gdofs_total_8rhs": round(8 * N / (ev[1].elapsed_time(ev[2]) / 1e4) / 1e9, 3)}
+    op.set_kernel_variant(sfgpu.KERNEL_AUTO)
+    del xx, yy
     x64 = torch.rand(8 * N, device="cuda", dtype=torch.float64) * 2 - 1
     y64 = torch.rand(8 * N, device="cuda", dtype=torch.float64) * 2 - 1
     ax, aty = torch.empty_like(x64), torch.empty_like(y64)
@@ -564,24 +586,33 @@ def secondary_configs(stream, peak):
     torch.cuda.empty_cache()
     # ---- the cell operator's DO_MASS_MATRIX / DO_CONVECTION variants:
     # continuous mass matrix and convection form, p=4, affine 64^3, FP32
-    # (vectors only: 2 s N algorithmic bytes) ----
+    # (vectors only: 2 s N algorithmic bytes); default kernel (assembled
+    # Kronecker products) and the line-ownership kernel (SF_KERNEL_GENERIC) ----
     res = {}
     for name, kind in (("mass", sfgpu.OP_MASS), ("convection", sfgpu.OP_CONVECTION)):
         op = sfgpu.Operator(kind, degree=4, n_cells=(64, 64, 64), velocity=(1.0, 2.0, 3.0))
         x = torch.rand(op.n_dofs, device="cuda", dtype=torch.float32) * 2 - 1
         y = torch.empty_like(x)
         t = time_apply(op, x, y, 30, 5, stream, name)
-        res[name] = {"gdofs": round(op.n_dofs / t / 1e9, 3), "hbm_frac": round(8 * op.n_dofs / t / 1e9 / peak, 4)}
+        op.set_kernel_variant(sfgpu.KERNEL_GENERIC)
+        tg = time_apply(op, x, y, 30, 5, stream, name + " (line kernel)")
+        res[name] = {"gdofs": round(op.n_dofs / t / 1e9, 3), "hbm_frac": round(8 * op.n_dofs / t / 1e9 / peak, 4),
+                     "kernel": "assembled Kronecker products (z pass + x-y tiles)",
+                     "line_kernel_gdofs": round(op.n_dofs / tg / 1e9, 3)}
         del op, x, y
     # the DO_FACES builds on the cell-major vector of the same 64^3 cells
-    # (n^3 entries per cell; 2 s C n^3 algorithmic bytes)
+    # (n^3 entries per cell; 2 s C n^3 algorithmic bytes); default kernel
+    # (sums of 1D line operators) and the face-array kernel
     for name, kind in (("laplace_faces", sfgpu.OP_LAPLACE_FACES), ("convection_faces", sfgpu.OP_CONVECTION_FACES)):
         op = sfgpu.Operator(kind, degree=4, n_cells=(64, 64, 64), velocity=(1.0, 2.0, 3.0))
         x = torch.rand(op.n_dofs, device="cuda", dtype=torch.float32) * 2 - 1
         y = torch.empty_like(x)
         t = time_apply(op, x, y, 30, 5, stream, name)
+        op.set_kernel_variant(sfgpu.KERNEL_GENERIC)
+        tg = time_apply(op, x, y, 30, 5, stream, name + " (face-array kernel)")
         res[name] = {"gdofs": round(op.n_dofs / t / 1e9, 3), "hbm_frac": round(8 * op.n_dofs / t / 1e9 / peak, 4),
-                     "n_dofs": op.n_dofs}
+                     "n_dofs": op.n_dofs, "kernel": "sums of 1D line operators",
+                     "face_array_kernel_gdofs": round(op.n_dofs / tg / 1e9, 3)}
         del op, x, y
     out["cell_variants_p4_64c_affine_fp32"] = res
     # ---- unstructured hexahedral input: the 48^3 p=4 box given as cell-node
