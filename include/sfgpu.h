@@ -243,8 +243,9 @@ int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void 
  * affine structured ones without a coefficient (SF_OP_LAPLACE with deform 0
  * and no sf_set_coefficient, SF_OP_MASS, SF_OP_CONVECTION) as Kronecker
  * products of assembled 1D matrices (a pass along z, then x-y tiles of each
- * node plane) in FP64, and in FP32 where that measured faster (degrees up
- * to 5, the mass matrix up to 7); everything else (deformed, coefficient,
+ * node plane) in FP64, and in FP32 where that measured faster (the
+ * Laplacian and mass matrix at every degree, convection up to degree 5);
+ * everything else (deformed, coefficient,
  * unstructured, the remaining FP32 cases) runs on the packed
  * line-ownership kernel (one thread per line of a cell, several cells per
  * warp group); SF_KERNEL_GENERIC selects the line-ownership kernel for all

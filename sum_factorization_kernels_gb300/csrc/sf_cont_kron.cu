@@ -32,6 +32,7 @@
 #include "sf_device.cuh"
 #include "sf_internal.h"
 #include "sf_launch.h"
+#include "sf_tables.h"
 
 namespace sf {
 
@@ -42,6 +43,8 @@ struct KronArgs {
   // cell-local 1D matrices of this pass: out_o = sum_i A[o][i] in_i, A[o][i]
   // = mat[sel[o][i] - 1] (sel 0: no term)
   T mat[4][N][N];      // z pass: mat[0..1]; x-y tile: M_x, K_x, M_y, K_y
+  EOMat<N, T> eo[4];   // the same matrices in even-odd form (M and the Laplacian's
+                       // K centro-symmetric, the convection C anti-centro-symmetric)
   const T *in0, *in1;
   T *out0, *out1;
   const T *x;          // last pass: the Dirichlet rows y = x
@@ -52,6 +55,45 @@ struct KronArgs {
   FastDiv div_a, div_b; // task decomposition (see kron_pass)
 };
 
+// row p of a cell matrix times the left cell's nodes (the left cell's share
+// of the segment's vertex)
+template <int N, typename T, typename U>
+__device__ __forceinline__ T last_row(const T (&M)[N][N], const U &u, int off)
+{
+  T v = T(0);
+#pragma unroll
+  for (int j = 0; j < N; ++j) v = fma(M[N - 1][j], u[off + j], v);
+  return v;
+}
+
+// all rows of a cell matrix times the right cell's nodes u[off .. off + p]:
+// the even-odd form (symmetry SIGN), or the dense rows for FP64 below n = 7,
+// where the even-odd form's additions (on the same FP64 pipe) cost more than
+// its saved products (measured: p = 2 Laplacian 162 vs 213 us, p = 4 1.67 vs
+// 1.80 ms; p = 8 3.06 vs 3.77 ms the other way)
+// (ROWS: the rows the caller uses; the dense form computes only those)
+template <int N, int SIGN, typename T, typename U, int ROWS = N>
+__device__ __forceinline__ void cell_rows(const EOMat<N, T> &E, const T (&M)[N][N], const U &u, int off,
+                                          T (&out)[N])
+{
+  T in[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) in[j] = u[off + j];
+  if constexpr (sizeof(T) == 8 && N < 7) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) out[i] = T(0);
+#pragma unroll
+    for (int i = 0; i < ROWS; ++i) {
+      T v = M[i][0] * in[0];
+#pragma unroll
+      for (int j = 1; j < N; ++j) v = fma(M[i][j], in[j], v);
+      out[i] = v;
+    }
+  } else {
+    eo_apply<N, SIGN>(E, in, out);
+  }
+}
+
 // segments per thread: a thread walks G consecutive cell segments of its
 // line and loads each node once ((G + 1) p + 1 inputs per G p outputs)
 template <int N>
@@ -61,11 +103,13 @@ struct KronG {
 
 // the z pass: out_o = sum_i A[o][i] in_i along the z lines, SEL[o][i] in
 // {0, 1, 2} picking no term / mat[0] / mat[1]
-template <int N, typename T, int NIN, int NOUT, int S00, int S01, int S10, int S11>
+template <int N, typename T, int NIN, int NOUT, int S00, int S01, int S10, int S11, int KS>
 __global__ void __launch_bounds__(256) kron_pass(const __grid_constant__ KronArgs<N, T> A)
 {
   constexpr int DIR = 2;
   constexpr int P = N - 1;
+  // dense rows for FP64 below n = 7 (see cell_rows), even-odd otherwise
+  constexpr bool DENSE = sizeof(T) == 8 && N < 7;
   constexpr int G = KronG<N>::value;
   constexpr int W = (G + 1) * P + 1; // window: nodes s0 p - p .. (s0 + G) p
   constexpr int SEL[2][2] = {{S00, S01}, {S10, S11}};
@@ -100,39 +144,65 @@ __global__ void __launch_bounds__(256) kron_pass(const __grid_constant__ KronArg
         }
       }
     }
+    // segment g's left cell is segment g - 1's right cell: in the even-odd
+    // form its last row is carried along the chain (computed directly for
+    // the first segment); the dense form (FP64 below n = 7) takes the left
+    // cell's last row and the right cell's rows 0 .. p - 1 directly
+    T carry[NOUT];
+#pragma unroll
+    for (int o = 0; o < NOUT; ++o) carry[o] = T(0);
 #pragma unroll
     for (int g = 0; g < G; ++g) {
       const int s = s0 + g;
       if (s > nc) break;
       const bool left = s > 0, right = s < nc;
-      // window offset of node s p - p: g p
+      // window offsets: left cell g p .. g p + p, right cell g p + p .. g p + 2p
       T r[NOUT][P];
 #pragma unroll
       for (int o = 0; o < NOUT; ++o) {
 #pragma unroll
         for (int q = 0; q < P; ++q) r[o][q] = T(0);
+        if constexpr (DENSE) {
 #pragma unroll
-        for (int i = 0; i < NIN; ++i) {
-          if (SEL[o][i] == 0) continue;
-          const T(&M)[N][N] = A.mat[SEL[o][i] - 1];
-          // vertex s p: last row of the left cell, first row of the right cell
-          T v = r[o][0];
-          if (left) {
+          for (int i = 0; i < NIN; ++i) {
+            if (SEL[o][i] == 0) continue;
+            const T(&M)[N][N] = A.mat[SEL[o][i] - 1];
+            T v = r[o][0];
+            if (left) {
 #pragma unroll
-            for (int j = 0; j < N; ++j) v = fma(M[P][j], u[i][g * P + j], v);
+              for (int j = 0; j < N; ++j) v = fma(M[P][j], u[i][g * P + j], v);
+            }
+            if (right) {
+#pragma unroll
+              for (int j = 0; j < N; ++j) v = fma(M[0][j], u[i][g * P + P + j], v);
+#pragma unroll
+              for (int q = 1; q < P; ++q) {
+                T w = r[o][q];
+#pragma unroll
+                for (int j = 0; j < N; ++j) w = fma(M[q][j], u[i][g * P + P + j], w);
+                r[o][q] = w;
+              }
+            }
+            r[o][0] = v;
           }
-          if (right) {
+        } else {
+          T v = g > 0 ? carry[o] : T(0), next = T(0);
 #pragma unroll
-            for (int j = 0; j < N; ++j) v = fma(M[0][j], u[i][g * P + P + j], v);
+          for (int i = 0; i < NIN; ++i) {
+            if (SEL[o][i] == 0) continue;
+            const int k = SEL[o][i] - 1;
+            if (g == 0 && left) v += last_row<N, T>(A.mat[k], u[i], 0);
+            if (right) {
+              T pr[N];
+              if (k == 0) cell_rows<N, 1, T>(A.eo[0], A.mat[0], u[i], g * P + P, pr);
+              else cell_rows<N, KS, T>(A.eo[1], A.mat[1], u[i], g * P + P, pr);
 #pragma unroll
-            for (int q = 1; q < P; ++q) {
-              T w = r[o][q];
-#pragma unroll
-              for (int j = 0; j < N; ++j) w = fma(M[q][j], u[i][g * P + P + j], w);
-              r[o][q] = w;
+              for (int q = 0; q < P; ++q) r[o][q] += pr[q];
+              next += pr[P];
             }
           }
-          r[o][0] = v;
+          r[o][0] += left ? v : T(0);
+          carry[o] = next;
         }
       }
       // store nodes s p .. s p + p - 1 (the final vertex alone), projected
@@ -178,13 +248,14 @@ struct KronTile {
   static constexpr int THREADS = 256;
 };
 
-template <int N, typename T, int NIN>
+template <int N, typename T, int NIN, int KS>
 __global__ void __launch_bounds__(KronTile<N>::THREADS) kron_xy(const __grid_constant__ KronArgs<N, T> A)
 {
   using TL = KronTile<N>;
   constexpr int P = N - 1, CX = TL::CX, CY = TL::CY, TX = TL::TX;
   constexpr int IC = TL::IC, IR = TL::IR, OC = TL::OC;
   constexpr int NQ = NIN == 1 ? 1 : 2; // x-sweep results per node
+  constexpr bool DENSE = sizeof(T) == 8 && N < 7; // dense rows (see cell_rows)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *in = reinterpret_cast<T *>(smem_raw);   // [NIN][IR][IC]
   T *qx = in + NIN * IR * IC;                // [NQ][IR][OC]
@@ -245,31 +316,70 @@ __global__ void __launch_bounds__(KronTile<N>::THREADS) kron_xy(const __grid_con
       for (int k = 0; k < 2 * P + 1; ++k) u[i][k] = in[(i * IR + r) * IC + sl * P + k];
     // q0 = (K_x a + M_x b) or M_x a (NIN = 1), q1 = M_x a
     T q0[P], q1[P];
+    if constexpr (DENSE) {
 #pragma unroll
-    for (int q = 0; q < P; ++q) q0[q] = q1[q] = T(0);
+      for (int q = 0; q < P; ++q) q0[q] = q1[q] = T(0);
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-      const T a_l = u[0][j], a_r = u[0][P + j];
-      if (NIN == 1) {
-        if (left) q0[0] = fma(Mx[P][j], a_l, q0[0]);
-        if (right) {
+      for (int j = 0; j < N; ++j) {
+        const T a_l = u[0][j], a_r = u[0][P + j];
+        if (NIN == 1) {
+          if (left) q0[0] = fma(Mx[P][j], a_l, q0[0]);
+          if (right) {
 #pragma unroll
-          for (int q = 0; q < P; ++q) q0[q] = fma(Mx[q][j], a_r, q0[q]);
-        }
-      } else {
-        const T b_l = u[NIN - 1][j], b_r = u[NIN - 1][P + j];
-        if (left) {
-          q0[0] = fma(Kx[P][j], a_l, fma(Mx[P][j], b_l, q0[0]));
-          q1[0] = fma(Mx[P][j], a_l, q1[0]);
-        }
-        if (right) {
+            for (int q = 0; q < P; ++q) q0[q] = fma(Mx[q][j], a_r, q0[q]);
+          }
+        } else {
+          const T b_l = u[NIN - 1][j], b_r = u[NIN - 1][P + j];
+          if (left) {
+            q0[0] = fma(Kx[P][j], a_l, fma(Mx[P][j], b_l, q0[0]));
+            q1[0] = fma(Mx[P][j], a_l, q1[0]);
+          }
+          if (right) {
 #pragma unroll
-          for (int q = 0; q < P; ++q) {
-            q0[q] = fma(Kx[q][j], a_r, fma(Mx[q][j], b_r, q0[q]));
-            q1[q] = fma(Mx[q][j], a_r, q1[q]);
+            for (int q = 0; q < P; ++q) {
+              q0[q] = fma(Kx[q][j], a_r, fma(Mx[q][j], b_r, q0[q]));
+              q1[q] = fma(Mx[q][j], a_r, q1[q]);
+            }
           }
         }
       }
+    } else {
+      // the right cell's rows by even-odd products, the vertex's left-cell
+      // row directly
+    {
+      const T(&ua)[2 * P + 1] = u[0];
+      const T(&ub)[2 * P + 1] = u[NIN - 1];
+      T la = T(0), lb = T(0);
+      if (left) {
+        la = last_row<N, T>(NIN == 1 ? Mx : Kx, ua, 0);
+        if (NIN == 2) {
+          la += last_row<N, T>(Mx, ub, 0);
+          lb = last_row<N, T>(Mx, ua, 0);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < P; ++q) q0[q] = q1[q] = T(0);
+      if (right) {
+        T pr[N];
+        if (NIN == 1) {
+          cell_rows<N, 1, T, decltype(ua), N - 1>(A.eo[0], Mx, ua, P, pr);
+#pragma unroll
+          for (int q = 0; q < P; ++q) q0[q] = pr[q];
+        } else {
+          cell_rows<N, KS, T, decltype(ua), N - 1>(A.eo[1], Kx, ua, P, pr);
+#pragma unroll
+          for (int q = 0; q < P; ++q) q0[q] = pr[q];
+          cell_rows<N, 1, T, decltype(ub), N - 1>(A.eo[0], Mx, ub, P, pr);
+#pragma unroll
+          for (int q = 0; q < P; ++q) q0[q] += pr[q];
+          cell_rows<N, 1, T, decltype(ua), N - 1>(A.eo[0], Mx, ua, P, pr);
+#pragma unroll
+          for (int q = 0; q < P; ++q) q1[q] = pr[q];
+        }
+      }
+      q0[0] += la;
+      q1[0] += lb;
+    }
     }
     const int cnt = right ? P : 1;
 #pragma unroll
@@ -303,22 +413,42 @@ __global__ void __launch_bounds__(KronTile<N>::THREADS) kron_xy(const __grid_con
 #pragma unroll
       for (int o = 0; o < NQ; ++o) v[o][k] = yb ? T(0) : qx[(o * IR + tl * P + k) * OC + c];
     }
+    // y = M_y q0 (+ K_y q1)
     T y[P];
 #pragma unroll
     for (int q = 0; q < P; ++q) y[q] = T(0);
+    if constexpr (DENSE) {
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-      if (left) {
-        y[0] = fma(My[P][j], v[0][j], y[0]);
-        if (NQ == 2) y[0] = fma(Ky[P][j], v[1][j], y[0]);
-      }
-      if (right) {
+      for (int j = 0; j < N; ++j) {
+        if (left) {
+          y[0] = fma(My[P][j], v[0][j], y[0]);
+          if (NQ == 2) y[0] = fma(Ky[P][j], v[1][j], y[0]);
+        }
+        if (right) {
 #pragma unroll
-        for (int q = 0; q < P; ++q) {
-          y[q] = fma(My[q][j], v[0][P + j], y[q]);
-          if (NQ == 2) y[q] = fma(Ky[q][j], v[1][P + j], y[q]);
+          for (int q = 0; q < P; ++q) {
+            y[q] = fma(My[q][j], v[0][P + j], y[q]);
+            if (NQ == 2) y[q] = fma(Ky[q][j], v[1][P + j], y[q]);
+          }
         }
       }
+    } else {
+      // right cell by even-odd products, the vertex's left-cell row directly
+    if (right) {
+      T pr[N];
+      cell_rows<N, 1, T, decltype(v[0]), N - 1>(A.eo[2], My, v[0], P, pr);
+#pragma unroll
+      for (int q = 0; q < P; ++q) y[q] = pr[q];
+      if (NQ == 2) {
+        cell_rows<N, KS, T, decltype(v[NQ - 1]), N - 1>(A.eo[3], Ky, v[NQ - 1], P, pr);
+#pragma unroll
+        for (int q = 0; q < P; ++q) y[q] += pr[q];
+      }
+    }
+    if (left) {
+      y[0] += last_row<N, T>(My, v[0], 0);
+      if (NQ == 2) y[0] += last_row<N, T>(Ky, v[NQ - 1], 0);
+    }
     }
     const int cnt = right ? P : 1;
     const bool xzb = dir && (X == 0 || X == nx - 1 || Z == 0 || Z == nz - 1);
@@ -359,7 +489,7 @@ void kron_mats(const sf_op *op, int d, double (&M)[kMaxN][kMaxN], double (&K)[kM
     }
 }
 
-template <int N, typename T, int NIN, int NOUT, int S00, int S01, int S10, int S11>
+template <int N, typename T, int NIN, int NOUT, int S00, int S01, int S10, int S11, int KS>
 int launch_zpass(const sf_op *op, const T *in0, T *out0, T *out1, cudaStream_t st)
 {
   KronArgs<N, T> A{};
@@ -370,6 +500,8 @@ int launch_zpass(const sf_op *op, const T *in0, T *out0, T *out1, cudaStream_t s
       A.mat[0][i][j] = T(M[i][j]);
       A.mat[1][i][j] = T(K[i][j]);
     }
+  A.eo[0] = make_eo<N, T>([&](int i, int j) { return M[i][j]; });
+  A.eo[1] = make_eo<N, T>([&](int i, int j) { return K[i][j]; });
   for (int d = 0; d < 3; ++d) {
     A.nc[d] = op->desc.n_cells[d];
     A.nn[d] = (N - 1) * A.nc[d] + 1;
@@ -390,12 +522,12 @@ int launch_zpass(const sf_op *op, const T *in0, T *out0, T *out1, cudaStream_t s
   const int threads = 256;
   const long long want = (A.tasks + threads - 1) / threads;
   const long long cap = (long long)device_sm_count() * 16;
-  kron_pass<N, T, NIN, NOUT, S00, S01, S10, S11><<<(unsigned)(want < cap ? want : cap), threads, 0, st>>>(A);
+  kron_pass<N, T, NIN, NOUT, S00, S01, S10, S11, KS><<<(unsigned)(want < cap ? want : cap), threads, 0, st>>>(A);
   SF_CUDA_TRY(cudaGetLastError());
   return SF_OK;
 }
 
-template <int N, typename T, int NIN>
+template <int N, typename T, int NIN, int KS>
 int launch_xy(const sf_op *op, const T *a, const T *b, T *y, const T *x, cudaStream_t st)
 {
   using TL = KronTile<N>;
@@ -408,6 +540,8 @@ int launch_xy(const sf_op *op, const T *a, const T *b, T *y, const T *x, cudaStr
         A.mat[2 * d][i][j] = T(M[i][j]);
         A.mat[2 * d + 1][i][j] = T(K[i][j]);
       }
+    A.eo[2 * d] = make_eo<N, T>([&](int i, int j) { return M[i][j]; });
+    A.eo[2 * d + 1] = make_eo<N, T>([&](int i, int j) { return K[i][j]; });
   }
   for (int d = 0; d < 3; ++d) {
     A.nc[d] = op->desc.n_cells[d];
@@ -420,14 +554,14 @@ int launch_xy(const sf_op *op, const T *a, const T *b, T *y, const T *x, cudaStr
   A.dirichlet = op->desc.dirichlet;
   constexpr int NQ = NIN == 1 ? 1 : 2;
   const size_t smem = size_t(NIN * TL::IR * TL::IC + NQ * TL::IR * TL::OC) * sizeof(T);
-  SF_CUDA_TRY(cudaFuncSetAttribute(kron_xy<N, T, NIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SF_CUDA_TRY(cudaFuncSetAttribute(kron_xy<N, T, NIN, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const dim3 grid((unsigned)((A.nc[0] + TL::CX - 1) / TL::CX), (unsigned)((A.nc[1] + TL::CY - 1) / TL::CY),
                   (unsigned)A.nn[2]);
   if (A.nn[2] > 65535) {
     set_error("Kronecker passes: more than 65535 node planes");
     return SF_ERR_UNSUPPORTED;
   }
-  kron_xy<N, T, NIN><<<grid, TL::THREADS, smem, st>>>(A);
+  kron_xy<N, T, NIN, KS><<<grid, TL::THREADS, smem, st>>>(A);
   SF_CUDA_TRY(cudaGetLastError());
   return SF_OK;
 }
@@ -443,13 +577,19 @@ int kron_impl(const sf_op *op, const T *x, T *y, cudaStream_t st)
   }
   if (op->desc.kind == SF_OP_MASS) {
     // a = M_z x; y = M_y M_x a
-    SF_RET_IF((launch_zpass<N, T, 1, 1, 1, 0, 0, 0>(op, x, w, nullptr, st)));
-    return launch_xy<N, T, 1>(op, w, nullptr, y, x, st);
+    SF_RET_IF((launch_zpass<N, T, 1, 1, 1, 0, 0, 0, 1>(op, x, w, nullptr, st)));
+    return launch_xy<N, T, 1, 1>(op, w, nullptr, y, x, st);
   }
   // a = M_z x, b = K_z x; y = M_y (K_x a + M_x b) + K_y (M_x a)
   T *a = w, *b = w + n;
-  SF_RET_IF((launch_zpass<N, T, 1, 2, 1, 0, 2, 0>(op, x, a, b, st)));
-  return launch_xy<N, T, 2>(op, a, b, y, x, st);
+  // K: the Laplacian's stiffness is centro-symmetric, the convection matrix
+  // anti-centro-symmetric
+  if (op->desc.kind == SF_OP_CONVECTION) {
+    SF_RET_IF((launch_zpass<N, T, 1, 2, 1, 0, 2, 0, -1>(op, x, a, b, st)));
+    return launch_xy<N, T, 2, -1>(op, a, b, y, x, st);
+  }
+  SF_RET_IF((launch_zpass<N, T, 1, 2, 1, 0, 2, 0, 1>(op, x, a, b, st)));
+  return launch_xy<N, T, 2, 1>(op, a, b, y, x, st);
 }
 
 template <int N>
@@ -469,19 +609,18 @@ bool kron_eligible(const sf_op *op)
 
 int kron_work_vectors(const sf_op *op) { return op->desc.kind == SF_OP_MASS ? 1 : 2; }
 
-// FP64: always (the FP64 pipe favours the banded 1D products: 2-4x the
-// line kernel at p = 2..8).  FP32: where measured faster than the line
-// kernel (64^3 at p <= 4, 48^3, 40^3, 36^3, 32^3 at p = 5..8): every operator
-// up to p = 5 (p = 4 Laplacian 158 vs 196 us, mass 106 vs 152), the mass
-// matrix up to p = 7 (117 vs 131 us); the Laplacian and convection forms at
-// p >= 6 and everything at p = 8 stay with the line kernel (p = 8
-// Laplacian 274 vs 229 us: its (p+1)^2 / p multiply-adds per node and
-// product lose to the even-odd sweeps).
+// FP64: always (1.3-2.4x the line kernel at p = 2..8; convection at p = 7
+// within 3 %).  FP32: where measured faster than the line kernel (64^3 at
+// p = 4, 48^3, 40^3, 36^3, 32^3 at p = 5..8): the Laplacian and the mass
+// matrix at every degree (p = 4 Laplacian 148 vs 197 us, mass 94 vs 153;
+// p = 8 187 vs 230 and 100 vs 143 us), convection up to p = 5 (141 vs 179
+// us at p = 4); convection from p = 6 on stays with the line kernel (136 vs
+// 139 us at p = 6, 165 vs 180 at p = 7).
 bool kron_selected(const sf_op *op, int prec)
 {
   if (!kron_eligible(op) || op->kernel_variant == SF_KERNEL_GENERIC || !op->kron.ptr) return false;
   if (prec == SF_FP64) return true;
-  return op->desc.degree <= 5 || (op->desc.kind == SF_OP_MASS && op->desc.degree <= 7);
+  return op->desc.kind != SF_OP_CONVECTION || op->desc.degree <= 5;
 }
 
 int launch_cont_kron(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
