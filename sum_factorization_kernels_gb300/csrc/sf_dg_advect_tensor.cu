@@ -20,6 +20,14 @@
 // same tables as the cell-and-face kernel (sf_dg.cu), which remains
 // selectable (SF_KERNEL_GENERIC) and agrees to rounding.
 //
+// The same kernel evaluates the DO_FACES cell operators of
+// evaluation_cell_laplacian.h:505-797 (each Cartesian cell's own faces at 0
+// and 1 as the two sides of one face): convection as sum_f L_f (x) M1 (x) M1
+// with B_f = M1^-1 L_f and no neighbour coupling, the Laplacian the same way
+// plus a rank-one face term per direction (faces_laplace_1d below), and the
+// transpose with the inverse mass, A^T M^-1, with couplings through whole
+// neighbour lines (advect_transpose_invmass_1d).
+//
 // GPU mapping as in the tensor-form SIPG kernel: a block holds CPB
 // consecutive cells with n^2 threads each; the thread of z column (a, b)
 // reads and writes that column of the cell-major vector (runs of n^2
