@@ -131,16 +131,18 @@ __global__ void __launch_bounds__(256) kron_pass(const __grid_constant__ KronArg
     T u[NIN][W];
 #pragma unroll
     for (int i = 0; i < NIN; ++i) {
-      const T *src = (i == 0 ? A.in0 : A.in1) + base + w0 * stride;
+      const T *src = i == 0 ? A.in0 : A.in1;
       if (!edge) {
+        // w0 >= p here: the window lies inside the line
+        const T *w = src + base + w0 * stride;
 #pragma unroll
-        for (int k = 0; k < W; ++k) u[i][k] = __ldg(src + k * stride);
+        for (int k = 0; k < W; ++k) u[i][k] = __ldg(w + k * stride);
       } else {
 #pragma unroll
         for (int k = 0; k < W; ++k) {
           const long long pos = w0 + k;
           const bool ok = pos >= 0 && pos < nd && !(A.dirichlet && (pos == 0 || pos == nd - 1));
-          u[i][k] = ok ? __ldg(src + k * stride) : T(0);
+          u[i][k] = ok ? __ldg(src + (base + pos * stride)) : T(0);
         }
       }
     }
@@ -279,15 +281,16 @@ __global__ void __launch_bounds__(KronTile<N>::THREADS) kron_xy(const __grid_con
   }
 #pragma unroll
   for (int i = 0; i < NIN; ++i) {
-    const T *src = (i == 0 ? A.in0 : A.in1) + zoff + (X0 - P);
+    const T *src = i == 0 ? A.in0 : A.in1;
     T stage[RW][CW];
 #pragma unroll
     for (int k = 0; k < RW; ++k) {
       const int r = warp + WARPS * k, Y = Y0 - P + r;
       const bool rok = r < IR && Y >= 0 && Y < ny && !(dir && (Y == 0 || Y == ny - 1));
-      const T *row = src + (long long)Y * nx;
+      // node (X0 - p + c, Y) of plane Z, formed only for loaded (in-mesh) nodes
+      const long long row = zoff + (long long)Y * nx + (X0 - P);
 #pragma unroll
-      for (int j = 0; j < CW; ++j) stage[k][j] = (rok && cok[j]) ? __ldg(row + lane + 32 * j) : T(0);
+      for (int j = 0; j < CW; ++j) stage[k][j] = (rok && cok[j]) ? __ldg(src + (row + lane + 32 * j)) : T(0);
     }
 #pragma unroll
     for (int k = 0; k < RW; ++k) {
