@@ -292,15 +292,17 @@ typedef struct {
   int eig_iterations;    /* Lanczos steps for lambda_max (default 12)            */
   double rtol;           /* relative residual target |b - A x| / |b|             */
   int max_iter;          /* total inner iterations allowed                       */
-  double inner_rtol;     /* SF_SOLVE_MIXED: floor of the inner solves' relative
-                            tolerance (1e-6); each stops at max(inner_rtol,
-                            rtol |b| / (2 |r|)) for the outer residual r    */
+  double inner_rtol;     /* SF_SOLVE_MIXED: reliable-update factor (0.03): the
+                            FP32 CG replaces its residual by the true FP64
+                            residual b - A x whenever the recursive one has
+                            dropped by this factor since the last replacement */
   int project_constant;  /* 1: remove the mean from b and x (periodic SIPG)      */
 } sf_solve_opts;
 
 typedef struct {
   int iterations;        /* CG iterations (inner, for SF_SOLVE_MIXED)            */
-  int outer_iterations;  /* refinement steps (SF_SOLVE_MIXED)                    */
+  int outer_iterations;  /* SF_SOLVE_MIXED: FP64 true-residual updates of the
+                            iterate (reliable updates and refinement steps)  */
   double rel_residual;   /* final |b - A x| / |b| in FP64                        */
   double lambda_max;     /* estimate used by the Chebyshev preconditioner        */
   double seconds;        /* wall time of the solve (device synchronised)         */

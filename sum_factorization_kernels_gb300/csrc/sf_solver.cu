@@ -2,12 +2,17 @@
 // counterpart: the reference times operator applications only).
 //
 //  * SF_SOLVE_FP64: preconditioned CG with FP64 vectors and the FP64 operator.
-//  * SF_SOLVE_MIXED: FP64 iterative refinement.  Each outer step forms the
-//    true residual r = b - A x with the FP64 operator, solves A d = r / |r|
-//    approximately with an FP32 preconditioned CG (FP32 operator, FP32
-//    vectors, FP64 reductions) and updates x += |r| d in FP64.  Each inner
-//    solve stops at the relative residual the outer iteration still needs
-//    (half of rtol |b| / |r|), but not below inner_rtol.
+//  * SF_SOLVE_MIXED: FP32 preconditioned CG (FP32 operator, FP32 vectors,
+//    FP64 reductions) on the correction A d = r / |r| of an FP64 iterate,
+//    with reliable updates (residual replacement): whenever the recursive
+//    FP32 residual has dropped by a factor inner_rtol since the last
+//    replacement, the correction is added to the FP64 iterate, the true
+//    residual b - A x is formed with the FP64 operator and becomes the FP32
+//    residual, and the iteration continues with the same search direction.
+//    The Krylov space is not restarted, so the FP32 solve needs about as many
+//    iterations as the FP64 one.  The solve targets the outer tolerance
+//    directly; an FP64 refinement step around it (the true residual, then
+//    another FP32 solve) only follows if the FP32 solve stalls.
 //  * Preconditioners: none, Jacobi (inverse diagonal) or a Chebyshev
 //    polynomial of D^-1 A (the smoother form of the reference's fused
 //    Chebyshev step, evaluation_dg_laplacian.h:485-502) with lambda_max from
@@ -246,6 +251,14 @@ __global__ void sub_kernel(long long n, T *__restrict__ r, const T *__restrict__
 __global__ void to_f32_scaled(long long n, float *__restrict__ y, const double *__restrict__ x, const Scalars *sc)
 {
   const double s = 1.0 / sqrt(sc->rr);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = float(x[i] * s);
+}
+
+// y = x * s in FP32 (a replaced residual in the scale of the running solve)
+__global__ void to_f32_times(long long n, float *__restrict__ y, const double *__restrict__ x, double s)
+{
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] = float(x[i] * s);
@@ -539,6 +552,17 @@ int cheb_rest(Solver &S, PrecState &P, const sf_solve_opts &o, const T *r, T *z)
   return SF_OK;
 }
 
+// reliable updates of an FP32 correction solve inside the FP64 refinement:
+// the FP64 iterate, right-hand side and work vectors, and the scale of the
+// FP32 system (|r| of the outer step: the FP32 right-hand side is r / rn)
+struct Reliable {
+  double *x64;
+  const double *b64;
+  double *r64, *ax64;
+  double rn;
+  int replacements = 0;
+};
+
 // preconditioned CG on A x = b (vectors of type T, x holds the start);
 // stops when |r| <= tol_abs or after max_iter iterations.  In FP32 the
 // recursively updated residual can stall above a tolerance close to the
@@ -548,7 +572,7 @@ constexpr int kStall = 100;
 
 template <typename T>
 int pcg(Solver &S, PrecState &P, const sf_solve_opts &o, const T *b, T *x, double tol_abs, int max_iter,
-        bool proj, int &iters, double &rr_final)
+        bool proj, int &iters, double &rr_final, Reliable *rel = nullptr)
 {
   const long long n = S.n;
   const int g = grid_for(n);
@@ -584,6 +608,7 @@ int pcg(Solver &S, PrecState &P, const sf_solve_opts &o, const T *b, T *x, doubl
   if (h.done) return SF_OK;
   double best = h.rr;
   int best_k = 0;
+  double rr_ref = h.rr; // recursive residual at the start or the last replacement
   // iterations, queued one ahead of the host's convergence check
   for (int k = 0; k < max_iter; ++k) {
     if ((e = S.vmult(prec_of<T>(), p, ap))) return e;
@@ -606,6 +631,31 @@ int pcg(Solver &S, PrecState &P, const sf_solve_opts &o, const T *b, T *x, doubl
       if (h.done) {
         iters = k; // iteration k was queued after convergence and changed nothing
         break;
+      }
+      if constexpr (sizeof(T) == 4) if (rel && h.rr < o.inner_rtol * o.inner_rtol * rr_ref) {
+        // residual replacement after the queued iteration k: fold the FP32
+        // correction into the FP64 iterate, form the true residual in FP64,
+        // take it (in the FP32 system's scale) as the residual, precondition
+        // it and continue with the same search direction p
+        add_f32_scaled<<<g, kThreads, 0, S.st>>>(n, rel->x64, x, rel->rn);
+        SF_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(T) * n, S.st));
+        if ((e = S.vmult(SF_FP64, rel->x64, rel->ax64))) return e;
+        sub_kernel<double><<<g, kThreads, 0, S.st>>>(n, rel->r64, rel->b64, rel->ax64);
+        if (proj && (e = S.project(rel->r64))) return e;
+        to_f32_times<<<g, kThreads, 0, S.st>>>(n, r, rel->r64, 1.0 / rel->rn);
+        if (o.precond == SF_PRECOND_JACOBI)
+          precond_first<T, PC_JACOBI><<<g, kThreads, 0, S.st>>>(n, r, dinv, z, t, s0);
+        if (o.precond == SF_PRECOND_CHEBYSHEV) {
+          precond_first<T, PC_CHEB><<<g, kThreads, 0, S.st>>>(n, r, dinv, z, t, s0);
+          if ((e = cheb_rest<T>(S, P, o, r, z))) return e;
+        }
+        if (proj && z != r && (e = S.project(z))) return e;
+        if ((e = S.reduce<T, RED_RZ>(r, z))) return e;
+        SF_CUDA_TRY(cudaGetLastError());
+        ++rel->replacements;
+        rr_ref = h.rr;
+        best = h.rr;
+        best_k = k;
       }
       if (h.rr < 0.25 * best) {
         best = h.rr;
@@ -684,7 +734,7 @@ extern "C" void sf_solve_opts_default(sf_solve_opts *o)
   o->eig_iterations = 12;
   o->rtol = 1e-10;
   o->max_iter = 2000;
-  o->inner_rtol = 1e-6;
+  o->inner_rtol = 0.03;
   o->project_constant = 0;
 }
 
@@ -754,7 +804,7 @@ extern "C" int sf_cg_solve(sf_op *op, const double *b, double *x, const sf_solve
   Scalars h;
   if ((e = S.read(&h))) return e;
   const double bnorm = std::sqrt(h.rr);
-  int total_iters = 0, outer = 0;
+  int total_iters = 0, outer = 0, replacements = 0;
   double relres = 0.0;
   if (bnorm == 0.0) {
     SF_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
@@ -780,13 +830,15 @@ extern "C" int sf_cg_solve(sf_op *op, const double *b, double *x, const sf_solve
       if (rn <= o.rtol * bnorm || total_iters >= o.max_iter) break;
       to_f32_scaled<<<g, kThreads, 0, st>>>(n, r32, r, S.sc);
       SF_CUDA_TRY(cudaMemsetAsync(d32, 0, sizeof(float) * n, st));
-      // the inner solve reduces its unit residual as far as this outer
-      // step still needs (with a factor 2 of margin), not below inner_rtol
-      const double inner = std::fmax(o.inner_rtol, std::fmin(0.5, 0.5 * o.rtol * bnorm / rn));
+      // the FP32 solve, with reliable updates, reduces its unit residual as
+      // far as the outer tolerance needs (with a factor 2 of margin)
+      const double inner = std::fmin(0.5, 0.5 * o.rtol * bnorm / rn);
       int it = 0;
       double rr32;
-      if ((e = pcg<float>(S, P, o, r32, d32, inner, o.max_iter - total_iters, proj, it, rr32))) return e;
+      Reliable rel{x, bp, r, ax, rn};
+      if ((e = pcg<float>(S, P, o, r32, d32, inner, o.max_iter - total_iters, proj, it, rr32, &rel))) return e;
       total_iters += it;
+      replacements += rel.replacements;
       add_f32_scaled<<<g, kThreads, 0, st>>>(n, x, d32, rn);
       SF_CUDA_TRY(cudaGetLastError());
       ++outer;
@@ -808,7 +860,7 @@ extern "C" int sf_cg_solve(sf_op *op, const double *b, double *x, const sf_solve
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (stats) {
     stats->iterations = total_iters;
-    stats->outer_iterations = outer;
+    stats->outer_iterations = outer + replacements;
     stats->rel_residual = relres;
     stats->lambda_max = P.lambda_max;
     stats->seconds = secs;
