@@ -1,7 +1,7 @@
 """Shared-memory bank model of the sweep kernels and the layout search behind
 their slab tables (``pack_params`` in ``csrc/sf_laplace_line.cu``,
 ``dg_slabs`` and ``dg_inv_layout`` in ``csrc/sf_dg.cu``, ``faces_layout`` in
-``csrc/sf_cell_faces.cu``).
+``csrc/sf_cell_faces.cu``, ``ta_slabs`` in ``csrc/sf_dg_advect_tensor.cu``).
 
 Model: shared memory has 32 banks of 4 bytes.  One warp-wide access takes as
 many wavefronts as the largest number of distinct 4-byte words that its

@@ -78,50 +78,96 @@ struct TAArgs {
 };
 
 // slabs X (input copy, and the mass sweeps), R1 (x line results), R2 (y line
-// results): entry (x, y, z) of cell cs at BASE + cs RS + SX x + SY y + SZ z,
-// the padded layout of dg_layout with the three slabs of a cell side by side
+// results), each in a region of its own: entry (x, y, z) of cell cs at
+// BASE + cs RS + SX x + SY y + SZ z.  FP32: strides from the bank-conflict
+// model of the kernel's accesses over the lanes of each warp (X: z column
+// stores, x and y line loads; R1: x line stores, z column loads; R2: y line
+// stores, z column loads; p = 4: 190 weighted wavefronts per cell group
+// against 220 for the padded layout); FP64: the padded layout of dg_layout.
 struct TASlab {
   int SX, SY, SZ, RS, BASE;
 };
+struct TASlabs {
+  TASlab X, R1, R2;
+};
+
+constexpr TASlabs ta_slabs3(TASlab x, TASlab r1, TASlab r2, int cpb)
+{
+  return TASlabs{{x.SX, x.SY, x.SZ, x.RS, 0}, {r1.SX, r1.SY, r1.SZ, r1.RS, cpb * x.RS},
+                 {r2.SX, r2.SY, r2.SZ, r2.RS, cpb * (x.RS + r1.RS)}};
+}
+
+constexpr TASlabs ta_slabs(int n, int elem, int cpb)
+{
+  if (elem == 4) {
+    switch (n) {
+    case 2: return ta_slabs3({5, 1, 2, 12, 0}, {5, 2, 1, 12, 0}, {2, 5, 1, 12, 0}, cpb);
+    case 3: return ta_slabs3({3, 1, 9, 27, 0}, {3, 9, 1, 27, 0}, {11, 33, 1, 99, 0}, cpb);
+    case 4: return ta_slabs3({19, 4, 1, 80, 0}, {17, 4, 1, 80, 0}, {4, 1, 17, 80, 0}, cpb);
+    case 5: return ta_slabs3({26, 1, 5, 153, 0}, {26, 1, 5, 153, 0}, {1, 5, 37, 185, 0}, cpb);
+    case 6: return ta_slabs3({37, 1, 6, 228, 0}, {37, 1, 6, 228, 0}, {1, 6, 38, 228, 0}, cpb);
+    case 7: return ta_slabs3({1, 52, 7, 369, 0}, {1, 7, 49, 343, 0}, {7, 49, 1, 343, 0}, cpb);
+    case 8: return ta_slabs3({67, 1, 8, 533, 0}, {68, 1, 8, 540, 0}, {1, 72, 8, 568, 0}, cpb);
+    case 9: return ta_slabs3({1, 9, 81, 729, 0}, {1, 9, 81, 729, 0}, {1, 9, 105, 945, 0}, cpb);
+    default: break;
+    }
+  }
+  const DGLayout L = dg_layout(n, elem);
+  const int slab = L.P2 * n, rs = 3 * slab + L.SKEW;
+  return TASlabs{{1, L.P1, L.P2, rs, 0}, {1, L.P1, L.P2, rs, slab}, {1, L.P1, L.P2, rs, 2 * slab}};
+}
+
+constexpr int ta_slab_end(int n, int cpb, TASlab S)
+{
+  return S.BASE + (cpb - 1) * S.RS + (n - 1) * (S.SX + S.SY + S.SZ) + 1;
+}
 
 template <int N, typename T>
 struct TACfg {
   static constexpr int CPB = DGCells<N>::value;
-  static constexpr DGLayout L = dg_layout(N, (int)sizeof(T));
-  static constexpr int SLAB = L.P2 * N;
-  static constexpr int RS = 3 * SLAB + L.SKEW;
-  static constexpr TASlab X{1, L.P1, L.P2, RS, 0}, R1{1, L.P1, L.P2, RS, SLAB}, R2{1, L.P1, L.P2, RS, 2 * SLAB};
-  static constexpr size_t SMEM = size_t(CPB) * RS * sizeof(T); // per right-hand side
+  static constexpr TASlabs S = ta_slabs(N, (int)sizeof(T), CPB);
+  static constexpr TASlab X = S.X, R1 = S.R1, R2 = S.R2;
+  static constexpr int E0 = ta_slab_end(N, CPB, X), E1 = ta_slab_end(N, CPB, R1), E2 = ta_slab_end(N, CPB, R2);
+  static constexpr int WORDS = E0 > E1 ? (E0 > E2 ? E0 : E2) : (E1 > E2 ? E1 : E2); // slabs of one right-hand side
+  static constexpr size_t SMEM = size_t(WORDS) * sizeof(T);                        // per right-hand side
   // DO_FACES Laplacian: three n x n face arrays per cell after the slabs
   static constexpr int FW = 3 * N * N;
-  static constexpr size_t SMEM_F2 = size_t(CPB) * (RS + FW) * sizeof(T);
+  static constexpr size_t SMEM_F2 = (size_t(WORDS) + size_t(CPB) * FW) * sizeof(T);
 };
 
-// every entry of the three slabs of a cell has its own word inside RS
-constexpr bool ta_slabs_fit(int n, DGLayout L)
+// every entry of the three slabs of every cell of a block has its own word
+constexpr bool ta_slabs_fit(int n, int cpb, TASlabs S)
 {
-  bool seen[8192] = {};
-  const int slab = L.P2 * n, rs = 3 * slab + L.SKEW;
-  if (rs > 8192) return false;
+  bool seen[16384] = {};
+  const TASlab L[3] = {S.X, S.R1, S.R2};
   for (int s = 0; s < 3; ++s)
-    for (int z = 0; z < n; ++z)
-      for (int y = 0; y < n; ++y)
-        for (int x = 0; x < n; ++x) {
-          const int i = s * slab + x + L.P1 * y + L.P2 * z;
-          if (i >= rs || seen[i]) return false;
-          seen[i] = true;
-        }
+    for (int c = 0; c < cpb; ++c)
+      for (int z = 0; z < n; ++z)
+        for (int y = 0; y < n; ++y)
+          for (int x = 0; x < n; ++x) {
+            const int i = L[s].BASE + c * L[s].RS + L[s].SX * x + L[s].SY * y + L[s].SZ * z;
+            if (i < 0 || i >= 16384 || seen[i]) return false;
+            seen[i] = true;
+          }
   return true;
 }
-static_assert(ta_slabs_fit(2, dg_layout(2, 4)) && ta_slabs_fit(3, dg_layout(3, 4)) && ta_slabs_fit(4, dg_layout(4, 4)) &&
-                  ta_slabs_fit(5, dg_layout(5, 4)) && ta_slabs_fit(6, dg_layout(6, 4)) &&
-                  ta_slabs_fit(7, dg_layout(7, 4)) && ta_slabs_fit(8, dg_layout(8, 4)) &&
-                  ta_slabs_fit(9, dg_layout(9, 4)),
+static_assert(ta_slabs_fit(2, DGCells<2>::value, ta_slabs(2, 4, DGCells<2>::value)) &&
+                  ta_slabs_fit(3, DGCells<3>::value, ta_slabs(3, 4, DGCells<3>::value)) &&
+                  ta_slabs_fit(4, DGCells<4>::value, ta_slabs(4, 4, DGCells<4>::value)) &&
+                  ta_slabs_fit(5, DGCells<5>::value, ta_slabs(5, 4, DGCells<5>::value)) &&
+                  ta_slabs_fit(6, DGCells<6>::value, ta_slabs(6, 4, DGCells<6>::value)) &&
+                  ta_slabs_fit(7, DGCells<7>::value, ta_slabs(7, 4, DGCells<7>::value)) &&
+                  ta_slabs_fit(8, DGCells<8>::value, ta_slabs(8, 4, DGCells<8>::value)) &&
+                  ta_slabs_fit(9, DGCells<9>::value, ta_slabs(9, 4, DGCells<9>::value)),
               "FP32 slab entries overlap");
-static_assert(ta_slabs_fit(2, dg_layout(2, 8)) && ta_slabs_fit(3, dg_layout(3, 8)) && ta_slabs_fit(4, dg_layout(4, 8)) &&
-                  ta_slabs_fit(5, dg_layout(5, 8)) && ta_slabs_fit(6, dg_layout(6, 8)) &&
-                  ta_slabs_fit(7, dg_layout(7, 8)) && ta_slabs_fit(8, dg_layout(8, 8)) &&
-                  ta_slabs_fit(9, dg_layout(9, 8)),
+static_assert(ta_slabs_fit(2, DGCells<2>::value, ta_slabs(2, 8, DGCells<2>::value)) &&
+                  ta_slabs_fit(3, DGCells<3>::value, ta_slabs(3, 8, DGCells<3>::value)) &&
+                  ta_slabs_fit(4, DGCells<4>::value, ta_slabs(4, 8, DGCells<4>::value)) &&
+                  ta_slabs_fit(5, DGCells<5>::value, ta_slabs(5, 8, DGCells<5>::value)) &&
+                  ta_slabs_fit(6, DGCells<6>::value, ta_slabs(6, 8, DGCells<6>::value)) &&
+                  ta_slabs_fit(7, DGCells<7>::value, ta_slabs(7, 8, DGCells<7>::value)) &&
+                  ta_slabs_fit(8, DGCells<8>::value, ta_slabs(8, 8, DGCells<8>::value)) &&
+                  ta_slabs_fit(9, DGCells<9>::value, ta_slabs(9, 8, DGCells<9>::value)),
               "FP64 slab entries overlap");
 
 // r = B_d u + cl_d lo + cr_d hi
@@ -151,7 +197,7 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   constexpr int CPB = Cfg::CPB;
   constexpr TASlab LX = Cfg::X, L1 = Cfg::R1, L2 = Cfg::R2;
   // slab (and face array) words of one right-hand side
-  constexpr int RSTRIDE = CPB * (Cfg::RS + (F2 ? Cfg::FW : 0));
+  constexpr int RSTRIDE = Cfg::WORDS + (F2 ? CPB * Cfg::FW : 0);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
   const int tid = threadIdx.x;
@@ -165,7 +211,7 @@ __global__ void __launch_bounds__(DGCells<N>::value *N *N)
   T *R2 = smem + L2.BASE + cs * L2.RS;
   // face arrays of the F2 term: Fx over (y, z), Fy over (x, z), Fz over (x, y),
   // entry (i, j) at i + N j
-  T *Fx = smem + CPB * Cfg::RS + cs * Cfg::FW, *Fy = Fx + N * N, *Fz = Fy + N * N;
+  T *Fx = smem + Cfg::WORDS + cs * Cfg::FW, *Fy = Fx + N * N, *Fz = Fy + N * N;
   // z column (a, b), x line (y, z) = (a, b), y line (x, z) = (a, b)
   const int zcX = LX.SX * a + LX.SY * b, xlX = LX.SY * a + LX.SZ * b, ylX = LX.SX * a + LX.SZ * b;
   const int zc1 = L1.SX * a + L1.SY * b, xl1 = L1.SY * a + L1.SZ * b;

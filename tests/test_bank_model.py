@@ -88,3 +88,32 @@ def test_faces_layouts():
             assert B.faces_cost(n, elem, L, conv) <= B.faces_cost(n, elem, pad, conv), (elem, n, conv)
     assert abs(B.faces_cost(5, 4, B.faces_padded(5)) - 532) < 0.04 * 532
     assert round(B.faces_cost(5, 4, t[(4, 5)])) == 382
+
+
+def test_line_operator_kernel_layouts():
+    """The FP32 slab table of the line-operator kernel (ta_slabs in
+    csrc/sf_dg_advect_tensor.cu), parsed from the source: per degree its
+    weighted wavefronts (X: z stores, x and y loads; R1: x stores, z loads;
+    R2: y stores, z loads; cell-major lanes) beat the padded layout of
+    dg_layout it replaced, and p = 4 costs the 190 the search found"""
+    import os
+    import re
+    src = open(os.path.join(B.CSRC, "sf_dg_advect_tensor.cu")).read()
+    body = src[src.index("constexpr TASlabs ta_slabs(int n, int elem, int cpb)"):]
+    body = body[:body.index("default: break;")]
+    rows = re.findall(r"case (\d): return ta_slabs3\(\{([^}]*)\}, \{([^}]*)\}, \{([^}]*)\}, cpb\);", body)
+    assert len(rows) == 8
+    padded = {2: (2, 5, 6), 3: (3, 9, 10), 4: (4, 19, 12), 5: (5, 25, 2), 6: (7, 42, 8), 7: (7, 56, 25),
+              8: (9, 72, 0), 9: (9, 81, 6)}
+    cells = {2: 32, 3: 14, 4: 8, 5: 5, 6: 7, 7: 5, 8: 2, 9: 3}
+    weights = ((1, 1, 1), (1, 1, 0), (1, 0, 1))
+    for case, *slabs in rows:
+        n = int(case)
+        k = cells[n]
+        lanes = B.lane_map(n, (k * n * n + 31) // 32, k, False)
+        table = sum(B.slab_cost(n, 4, lanes, tuple(B._ints(sl)[:4]), w) for sl, w in zip(slabs, weights))
+        p1, p2, skew = padded[n]
+        old = sum(B.slab_cost(n, 4, lanes, (1, p1, p2, 3 * p2 * n + skew), w) for w in weights)
+        assert table < old, (n, table, old)
+        if n == 5:
+            assert table == 190
