@@ -27,8 +27,11 @@
 // convection forms:
 //   z: a = M_z x, b = K_z x;   x-y: y = M_y (K_x a + M_x b) + K_y (M_x a)
 // (6 vector transfers); the mass matrix: a = M_z x, y = M_y M_x a (4).
-// Compared with the cell-by-cell apply there is no colouring, no gather and
-// no scatter; the work vectors are allocated with the handle.
+// Each cell-local product runs in the even-odd form of the 1D kernels (the
+// cell matrices are centro- or anti-centro-symmetric), in FP64 below n = 7
+// as dense rows.  Compared with the cell-by-cell apply there is no
+// colouring, no gather and no scatter; the work vectors are allocated with
+// the handle.
 #include "sf_device.cuh"
 #include "sf_internal.h"
 #include "sf_launch.h"
@@ -51,8 +54,8 @@ struct KronArgs {
   int nn[3];           // nodes per direction
   int nc[3];           // cells per direction
   int dirichlet;
-  long long tasks;     // segments x lines of this pass
-  FastDiv div_a, div_b; // task decomposition (see kron_pass)
+  long long tasks;     // z pass: segment chunks x nodes of a plane
+  FastDiv div_a;       // z pass: division by the nodes of a plane
 };
 
 // row p of a cell matrix times the left cell's nodes (the left cell's share
