@@ -102,6 +102,8 @@ public:
   }
   ~Operator() { if (op_) sf_destroy(op_); }
   sf_op *get() const { return op_; }
+  // SF_KERNEL_AUTO (default) or SF_KERNEL_GENERIC: see sf_set_kernel_variant
+  void set_kernel_variant(int variant) { check(sf_set_kernel_variant(op_, variant)); }
   long long n_dofs() const
   {
     long long n = 0, c = 0;
