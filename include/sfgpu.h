@@ -184,10 +184,10 @@ int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, voi
  * (reserved on every GPU that loads it, until process exit) instead of a
  * cudaMalloc'd buffer; it allocates nothing.  Only for SF_OP_DG_ADVECT
  * handles; nrhs * n_dofs * element size must not exceed 4 MiB
- * (SF_ERR_INVALID otherwise).  The first call on a device looks up the
- * array's device address once, and the first call with each degree and
- * precision loads that kernel.  The address is not looked up again after
- * cudaDeviceReset().
+ * (SF_ERR_INVALID otherwise).  Every call looks up the array's device
+ * address in the current context (so calls after cudaDeviceReset() use the
+ * reloaded array), and the first call with each degree and precision loads
+ * that kernel.
  * All calls share the array (nothing in it needs to start at zero), so
  * calls whose work overlaps on the GPU race: keep them on one stream or
  * synchronise between them. */

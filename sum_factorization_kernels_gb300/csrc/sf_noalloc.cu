@@ -20,7 +20,6 @@
 // Two calls whose work overlaps on the GPU (different streams, or different
 // host threads on the same device) race on the array and corrupt each
 // other's results; order them on one stream or synchronise between them.
-#include <mutex>
 
 #include "sf_internal.h"
 #include "sf_launch.h"
@@ -32,30 +31,15 @@ constexpr size_t kStaticScratchBytes = size_t(4) << 20;
 // device-resident intermediate vector shared by all calls on a device
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mutex;
-void *g_scratch_ptr[kMaxDevices] = {};
-
-// device address of g_static_scratch on the current device; looked up once
-// per device (the name is only a host-side stand-in, not a device address).
-// The table is not refreshed after cudaDeviceReset(), which unloads the
-// library's module: a process that resets a device must not call this entry
-// point on that device again.
+// device address of g_static_scratch in the current context (the name is
+// only a host-side stand-in, not a device address).  Looked up on every call
+// and never cached: cudaDeviceReset() unloads the library's module, and the
+// array can sit at another address once the module is loaded again.
 int scratch_address(void **out)
 {
-  int dev = 0;
-  SF_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) {
-    sf::set_error("device ordinal out of range for the static scratch table");
-    return SF_ERR_UNSUPPORTED;
-  }
-  std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void *p = nullptr;
-    SF_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
-    g_scratch_ptr[dev] = p;
-  }
-  *out = g_scratch_ptr[dev];
+  void *p = nullptr;
+  SF_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+  *out = p;
   return SF_OK;
 }
 
