@@ -19,7 +19,8 @@ CPU leg (``cpu_baseline``, and the whole of ``--impl reference``): the FP64
 oracle port of the reference's cell algorithm (gather -> even-odd sum
 factorisation -> scatter), built -O3 for the host CPU with OpenMP over all
 host threads, timed on the full workload.  The same leg uses the oracle's
-checker build to state the error of every GPU apply of the sweep.
+strict build (-O2, no floating-point contraction) to state the error of every
+GPU apply of the sweep.
 """
 from __future__ import annotations
 
@@ -200,7 +201,7 @@ def check_status(op, what):
 
 # --------------------------------------------------------------------------
 # CPU leg: the oracle port timed on the host cores (cpu_baseline and the
-# reference arm), and the oracle's checker build stating the GPU's errors
+# reference arm), and the oracle's strict build stating the GPU's errors
 # --------------------------------------------------------------------------
 def _cpu_env():
     os.environ.setdefault("OMP_PROC_BIND", "close")
@@ -249,7 +250,7 @@ def cpu_cont_baseline(p, ncells, repeats=CPU_REPEATS):
 
 
 def cpu_check_sweep(sweep, ncells):
-    """relative error of every sweep apply against the FP64 oracle (checker
+    """relative error of every sweep apply against the FP64 oracle (strict
     build) on the same mesh and vector; geometry computed per cell"""
     import numpy as np
 
@@ -378,7 +379,7 @@ def solve_entry(code, st):
 
 
 def cont_cg_sweep(degrees, ncells):
-    """the benchmark spec's target: FP32-inner / FP64-refined CG against plain FP64
+    """the mixed-precision target: FP32-inner / FP64-refined CG against plain FP64
     CG to 1e-10 on the continuous Laplacian of the deformed mesh, Chebyshev(5)
     Jacobi preconditioner for both, right-hand side uniform[-1,1]"""
     import numpy as np

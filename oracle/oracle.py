@@ -1,7 +1,7 @@
 """ctypes bindings of the FP64 CPU oracle (TEST INFRASTRUCTURE ONLY).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` import this module; it is the checker, never the product path.
+``bench.py`` import this module; it is the oracle, never the product path.
 """
 from __future__ import annotations
 
@@ -85,7 +85,7 @@ def _load(path):
 
 
 def lib():
-    """the checker build (-O2, ISO C: no floating-point contraction)"""
+    """the strict build (-O2, ISO C: no floating-point contraction)"""
     global _lib
     if _lib is None:
         _lib = _load(_build.build_oracle())
@@ -169,7 +169,7 @@ def cont_geometry(m: Mesh) -> np.ndarray:
 def cont_apply(m: Mesh, G, x, kappa=None, n_threads=0, y=None, L=None):
     """y = A x; G None computes each cell's geometry on the fly (no
     [cell][6][n^3] array); L selects the library build (default: the
-    checker build)"""
+    strict build)"""
     y = np.zeros(cont_n_dofs(m)) if y is None else y
     k = np.ascontiguousarray(kappa, dtype=np.float64) if kappa is not None else None
     g = None if G is None else np.ascontiguousarray(G).ctypes.data

@@ -1,6 +1,6 @@
 /*
- * Pre-include for compiling the reference's headers as a checker on the
- * build host (TEST INFRASTRUCTURE ONLY).  The standard headers are pulled in
+ * Pre-include for compiling the reference's headers into the golden-vector
+ * generator on the build host (TEST INFRASTRUCTURE ONLY).  The standard headers are pulled in
  * first so that "#define private public" below touches no library header;
  * the reference's evaluator classes keep their tables and vectors private,
  * and the golden-vector generator reads and sets them directly.

@@ -1,7 +1,7 @@
 /*
  * sf_oracle.h -- FP64 CPU oracle for the sum-factorization operators.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests,
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle: the parity tests,
  * smoke() and the CPU-baseline leg of bench.py call it to produce the
  * expected results that the CUDA library must reproduce.  No product code
  * path links, loads or calls it.
