@@ -118,10 +118,10 @@ const char *sf_version(void);
  * evaluation_dg_advect.h:107-180, benchmark_loops.cc:1163-1200): builds the
  * shape tables and, for a deformed mesh, the per-quadrature-point geometry
  * on the device (FP64, plus an FP32 copy).  An affine continuous operator
- * (SF_OP_LAPLACE with deform 0, SF_OP_MASS, SF_OP_CONVECTION) also gets the
- * work vectors of its Kronecker passes: 2 (SF_OP_MASS: 1) vectors of n_dofs
- * entries of the widest prepared precision, so that no apply allocates.
- * Synchronous. */
+ * (SF_OP_LAPLACE with deform 0, SF_OP_MASS, SF_OP_CONVECTION) whose node
+ * grid fits the Kronecker passes (at most 65535 node planes along z) also
+ * gets their work vectors: 2 (SF_OP_MASS: 1) vectors of n_dofs entries of
+ * the widest prepared precision, so that no apply allocates.  Synchronous. */
 int sf_create(const sf_desc *desc, sf_op **op);
 int sf_destroy(sf_op *op);
 
@@ -245,8 +245,8 @@ int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void 
  * products of assembled 1D matrices (a pass along z, then x-y tiles of each
  * node plane) in FP64, and in FP32 where that measured faster (the
  * Laplacian and mass matrix at every degree, convection up to degree 5);
- * everything else (deformed, coefficient,
- * unstructured, the remaining FP32 cases) runs on the packed
+ * everything else (deformed, coefficient, unstructured, more than 65535
+ * node planes along z, the remaining FP32 cases) runs on the packed
  * line-ownership kernel (one thread per line of a cell, several cells per
  * warp group); SF_KERNEL_GENERIC selects the line-ownership kernel for all
  * of them.  Both give the same operator to rounding.  SF_OP_DG_SIPG: SF_KERNEL_AUTO evaluates the operator in its

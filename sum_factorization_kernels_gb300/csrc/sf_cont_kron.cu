@@ -607,10 +607,28 @@ int kron_n(const sf_op *op, int prec, const void *x, void *y, cudaStream_t st)
 
 } // namespace
 
+// affine operators whose node grid fits the launch shapes of both passes:
+// one x-y block per tile and node plane (grid y and z at most 65535) and the
+// z pass's 32-bit task index.  Larger meshes keep the line-ownership kernel.
 bool kron_eligible(const sf_op *op)
 {
   const int k = op->desc.kind;
-  return (k == SF_OP_LAPLACE || k == SF_OP_MASS || k == SF_OP_CONVECTION) && !op->deformed && !op->has_kappa;
+  if (!((k == SF_OP_LAPLACE || k == SF_OP_MASS || k == SF_OP_CONVECTION) && !op->deformed && !op->has_kappa))
+    return false;
+  const long long p = op->desc.degree;
+  if (p < 1 || p > kMaxN - 1) return false;
+  long long nc[3], nn[3];
+  for (int d = 0; d < 3; ++d) {
+    nc[d] = op->desc.n_cells[d];
+    nn[d] = p * nc[d] + 1;
+  }
+  static_assert(KronG<5>::value == 4 && KronG<6>::value == 2, "G below restates KronG");
+  static_assert(KronTile<2>::CY == 32 && KronTile<5>::CY == 8 && KronTile<9>::CY == 4,
+                "cy below restates KronTile::CY");
+  const long long G = p + 1 <= 5 ? 4 : 2;
+  const long long cy = (32 + p - 1) / p;
+  const long long tasks = (nc[2] + G) / G * nn[0] * nn[1];
+  return nn[2] <= 65535 && (nc[1] + cy - 1) / cy <= 65535 && tasks < (1LL << 32);
 }
 
 int kron_work_vectors(const sf_op *op) { return op->desc.kind == SF_OP_MASS ? 1 : 2; }

@@ -57,6 +57,23 @@ def test_continuous_thin_meshes(p, nc):
             _check(torch, op, x, O.cont_apply_op(ma, okind, x, b), p)
 
 
+@pytest.mark.parametrize("nz", [16383, 16384])
+def test_affine_plane_limit_of_kronecker_passes(nz):
+    """the Kronecker passes of affine operators launch one x-y block per node
+    plane, at most 65535 planes along z: p = 4 on 1 x 1 x 16383 cells (65533
+    planes) runs them, 1 x 1 x 16384 (65537 planes) the line-ownership
+    kernel; both precisions equal the oracle either way"""
+    torch = torch_cuda()
+    sf = _sf()
+    p, nc = 4, (1, 1, nz)
+    m = O.mesh(p, nc, length=_length(nc), dirichlet=1)
+    x = np.random.default_rng(nz).uniform(-1, 1, O.cont_n_dofs(m))
+    lap = sf.Operator(sf.OP_LAPLACE, degree=p, n_cells=nc, length=_length(nc))
+    _check(torch, lap, x, O.cont_apply(m, None, x), p)
+    mass = sf.Operator(sf.OP_MASS, degree=p, n_cells=nc, length=_length(nc))
+    _check(torch, mass, x, O.cont_apply_op(m, O.OP_MASS, x), p)
+
+
 @pytest.mark.parametrize("nc", MESHES)
 @pytest.mark.parametrize("p", [1, 4, 8])
 def test_dg_thin_meshes(p, nc):
