@@ -116,11 +116,16 @@ def main(argv=None) -> None:
     ap.add_argument("--transpose", action="store_true", help="time the transposed apply")
     ap.add_argument("--rounds", type=int, default=16, help="sweeps: x and y sweeps per round")
     ap.add_argument("--deform", type=float, default=0.05, help="laplace: mapping amplitude (0: affine)")
+    ap.add_argument("--generic", action="store_true",
+                    help="select SF_KERNEL_GENERIC: the cell-and-face kernels of the DG operators and DO_FACES "
+                         "forms, the line-ownership kernel of the affine continuous operators")
     a = ap.parse_args(argv)
     if a.kind == "sweeps":
         sweeps(a.degree, a.ncells, a.rounds, a.reps, a.warmup)
         return
     op = make_operator(a.kind, a.degree, a.ncells, a.deform)
+    if a.generic:
+        op.set_kernel_variant(sf.KERNEL_GENERIC)
     dt = torch.float32 if a.prec == "fp32" else torch.float64
     n = op.n_dofs
     g = torch.Generator(device="cuda").manual_seed(1)
@@ -148,7 +153,7 @@ def main(argv=None) -> None:
     status = op.device_status()
     print("%s%s p=%d %d^3 %s nrhs=%d: %.3f GDoF/s (summed over right-hand sides), %.1f GB/s of vector "
           "traffic, %.1f us per apply, device status %d"
-          % (a.kind, " (transpose)" if a.transpose else "", a.degree, a.ncells, a.prec, a.nrhs, a.nrhs * n / t / 1e9,
+          % (a.kind + (" (generic)" if a.generic else ""), " (transpose)" if a.transpose else "", a.degree, a.ncells, a.prec, a.nrhs, a.nrhs * n / t / 1e9,
              2 * a.nrhs * n * x.element_size() / t / 1e9, t * 1e6, status))
     if status != 0:
         raise SystemExit("device status %d" % status)
