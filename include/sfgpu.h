@@ -15,7 +15,11 @@
  *    of the calling thread.
  *  - Vector and array pointers are DEVICE pointers unless a parameter name
  *    ends in _host.  They must be aligned to the element size; the library
- *    never frees them.
+ *    never frees them.  An output vector of an operator apply or Chebyshev
+ *    step must not overlap any other vector of the call (checked by
+ *    address range, SF_ERR_INVALID); inputs may share storage.  The
+ *    Runge-Kutta stage and step and sf_vector_update state their own
+ *    aliasing rules beside their declarations.
  *  - Work is ordered on the given stream (0 = legacy default stream) and is
  *    asynchronous unless stated otherwise.  A handle is not re-entrant: calls
  *    on one handle must not overlap; distinct handles are independent.
@@ -223,7 +227,10 @@ int sf_lsrk_step(sf_op *op, int prec, int nrhs, void *sol_new, void *sol_old, vo
                  void *stream);
 /* The same update without the operator, replaces
  * emulate_cheby_vector_updates() (evaluation_dg_laplacian.h:556-601):
- *   t <- c_tm * t + c_np * diag_inv .* (ax - b);  x_new <- x_old - t */
+ *   t <- c_tm * t + c_np * diag_inv .* (ax - b);  x_new <- x_old - t
+ * ax may be x_new itself (the reference's emulation passes sol_new as both);
+ * otherwise the outputs x_new and t overlap neither each other nor an input
+ * (SF_ERR_INVALID).  Inputs may share storage. */
 int sf_vector_update(long long n, int prec, const void *ax, const void *b,
                      const void *diag_inv, const void *x_old, void *x_new, void *t,
                      double c_np, double c_tm, void *stream);

@@ -445,7 +445,8 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream)
   SF_RET(check_prec(op, prec));
   SF_RET(check_ptr(x, prec, "x"));
   SF_RET(check_ptr(y, prec, "y"));
-  if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
+  if (ranges_overlap(x, y, (size_t)op->n_dofs * elem_size(prec)))
+    return fail(SF_ERR_INVALID, "x and y must not overlap");
   cudaStream_t st = (cudaStream_t)stream;
   const Region region(op->region_mv);
   if (is_continuous(op->desc.kind)) return launch_cont_vmult(op, prec, x, y, st);
@@ -476,7 +477,8 @@ int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void
   SF_RET(check_ptr(x, prec, "x"));
   SF_RET(check_ptr(y, prec, "y"));
   if (nrhs < 1 || nrhs > 64) return fail(SF_ERR_INVALID, "nrhs must be 1..64");
-  if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
+  if (ranges_overlap(x, y, (size_t)nrhs * (size_t)op->n_dofs * elem_size(prec)))
+    return fail(SF_ERR_INVALID, "x and y must not overlap");
   cudaStream_t st = (cudaStream_t)stream;
   const Region region(op->region_mv);
   if (is_continuous(op->desc.kind)) {
@@ -507,7 +509,8 @@ int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, voi
   SF_RET(check_ptr(x, prec, "x"));
   SF_RET(check_ptr(y, prec, "y"));
   if (nrhs < 1 || nrhs > 64) return fail(SF_ERR_INVALID, "nrhs must be 1..64");
-  if (x == y) return fail(SF_ERR_INVALID, "x and y must not alias");
+  if (ranges_overlap(x, y, (size_t)nrhs * (size_t)op->n_dofs * elem_size(prec)))
+    return fail(SF_ERR_INVALID, "x and y must not overlap");
   cudaStream_t st = (cudaStream_t)stream;
   const Region region(op->region_mv);
   // line operators: A^T, or A^T M^-1 in one launch
@@ -534,7 +537,19 @@ int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv, 
   SF_RET(check_ptr(x_old, prec, "x_old"));
   SF_RET(check_ptr(x_new, prec, "x_new"));
   SF_RET(check_ptr(t, prec, "t"));
-  if (x_old == x_new) return fail(SF_ERR_INVALID, "x_old and x_new must not alias");
+  {
+    // the outputs x_new and t overlap neither each other nor an input
+    const size_t bytes = (size_t)op->n_dofs * elem_size(prec);
+    const void *in[3] = {x_old, b, diag_inv};
+    const char *in_name[3] = {"x_old", "b", "diag_inv"};
+    if (ranges_overlap(x_new, t, bytes)) return fail(SF_ERR_INVALID, "x_new and t must not overlap");
+    for (int i = 0; i < 3; ++i) {
+      if (ranges_overlap(x_new, in[i], bytes))
+        return fail(SF_ERR_INVALID, std::string("x_new and ") + in_name[i] + " must not overlap");
+      if (ranges_overlap(t, in[i], bytes))
+        return fail(SF_ERR_INVALID, std::string("t and ") + in_name[i] + " must not overlap");
+    }
+  }
   if (is_cell_faces(op->desc.kind))
     return fail(SF_ERR_UNSUPPORTED, "Chebyshev steps: not for the face-term operators");
   cudaStream_t st = (cudaStream_t)stream;
@@ -608,6 +623,21 @@ int sf_vector_update(long long n, int prec, const void *ax, const void *b, const
   SF_RET(check_ptr(x_old, prec, "x_old"));
   SF_RET(check_ptr(x_new, prec, "x_new"));
   SF_RET(check_ptr(t, prec, "t"));
+  {
+    // the outputs x_new and t overlap neither each other nor an input, except
+    // that ax may be x_new itself (the reference's emulation passes sol_new as
+    // both; each entry of ax is read before the same entry of x_new is written)
+    const size_t bytes = (size_t)n * elem_size(prec);
+    const void *in[4] = {ax, b, diag_inv, x_old};
+    const char *in_name[4] = {"ax", "b", "diag_inv", "x_old"};
+    if (ranges_overlap(x_new, t, bytes)) return fail(SF_ERR_INVALID, "x_new and t must not overlap");
+    for (int i = 0; i < 4; ++i) {
+      if (ranges_overlap(x_new, in[i], bytes) && !(i == 0 && ax == x_new))
+        return fail(SF_ERR_INVALID, std::string("x_new and ") + in_name[i] + " must not overlap");
+      if (ranges_overlap(t, in[i], bytes))
+        return fail(SF_ERR_INVALID, std::string("t and ") + in_name[i] + " must not overlap");
+    }
+  }
   if (n == 0) return SF_OK;
   return launch_vector_update(n, prec, ax, b, diag_inv, x_old, x_new, t, c_np, c_tm,
                               (cudaStream_t)stream);

@@ -38,6 +38,15 @@ int fill_shape(int degree, int basis, Shape1D &s);
 // thread-local error text for sf_last_error()
 void set_error(const std::string &msg);
 
+// the byte ranges [a, a + bytes) and [b, b + bytes) share an address: an
+// output that overlaps an input of an apply is read by other threads after
+// they wrote it (neighbour values, the fused epilogues), so it is rejected
+inline bool ranges_overlap(const void *a, const void *b, size_t bytes)
+{
+  const uintptr_t pa = reinterpret_cast<uintptr_t>(a), pb = reinterpret_cast<uintptr_t>(b);
+  return pa < pb + bytes && pb < pa + bytes;
+}
+
 // drops the cached preconditioner state of a handle (sf_solver.cu)
 void release_solver_cache(sf_op *op);
 

@@ -73,8 +73,8 @@ extern "C" int sf_vmult_transpose_static(sf_op *op, int prec, int nrhs, const vo
     sf::set_error("nrhs must be 1..64");
     return SF_ERR_INVALID;
   }
-  if (x == y) {
-    sf::set_error("x and y must not alias");
+  if (sf::ranges_overlap(x, y, (size_t)nrhs * (size_t)op->n_dofs * es)) {
+    sf::set_error("x and y must not overlap");
     return SF_ERR_INVALID;
   }
   cudaStream_t st = (cudaStream_t)stream;

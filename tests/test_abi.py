@@ -57,6 +57,25 @@ def test_validation_without_gpu():
     assert L.sf_vector_update(-1, 0, 8, 8, 8, 8, 8, 8, 0.0, 0.0, None) == -1
 
 
+def test_vector_update_overlap_rules_without_gpu():
+    """outputs that overlap each other or an input are refused by address
+    range before anything is launched (the addresses are never touched)"""
+    _, L = _lib()
+    n, es = 100, 8
+    ax, b, dinv, xo, xn, t = (0x100000 + k * 0x1000 for k in range(6))
+
+    def call(ax=ax, b=b, dinv=dinv, xo=xo, xn=xn, t=t):
+        return L.sf_vector_update(n, 0, ax, b, dinv, xo, xn, t, 0.5, 0.5, None)
+
+    assert call(t=xn) == -1 and b"x_new and t" in L.sf_last_error()
+    assert call(t=xn + (n - 1) * es) == -1                     # last entry of x_new
+    assert call(b=t + es) == -1 and b"t and b" in L.sf_last_error()
+    assert call(xo=xn - es) == -1 and b"x_new and x_old" in L.sf_last_error()
+    assert call(dinv=xn) == -1 and b"x_new and diag_inv" in L.sf_last_error()
+    assert call(ax=xn + es) == -1 and b"x_new and ax" in L.sf_last_error()
+    assert call(ax=t) == -1 and b"t and ax" in L.sf_last_error()
+
+
 def test_shape_tables_match_oracle():
     import numpy as np
     from oracle import oracle as O

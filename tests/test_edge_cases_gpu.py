@@ -4,7 +4,8 @@ kind.  On the continuous meshes most colour classes are then empty, the
 packed kernels run partly filled cell groups, and with Dirichlet conditions
 on a single cell of degree 1 every node is fixed (y = x).  On the periodic DG
 meshes a cell is its own neighbour across the faces of a one-cell direction.
-Unstructured meshes of one cell, and a batch of one right-hand side."""
+Unstructured meshes of one cell, a batch of one right-hand side, and calls
+whose output overlaps another vector of the call."""
 import numpy as np
 import pytest
 
@@ -130,3 +131,46 @@ def test_batch_of_one_equals_single_apply():
             op.vmult_batched(x, yb, 1)
             assert torch.equal(y1, yb), (kind, dtype)
         assert op.device_status() == 0
+
+
+def test_overlapping_outputs_are_rejected():
+    """an output that overlaps another vector of the call is refused with
+    SF_ERR_INVALID before anything is launched (views into one buffer); the
+    reference's in-place vector update (ax the same vector as x_new) runs
+    and follows its formula"""
+    torch = torch_cuda()
+    sf = _sf()
+    dev = "cuda:0"
+    for kind, kw in ((sf.OP_LAPLACE, {"deform": 0.05}), (sf.OP_LAPLACE, {}), (sf.OP_DG_SIPG, {}),
+                     (sf.OP_DG_ADVECT, {"inverse_mass": 1})):
+        op = sf.Operator(kind, degree=2, n_cells=(2, 2, 2), **kw)
+        n = op.n_dofs
+        buf = torch.zeros(4 * n, dtype=torch.float64, device=dev)
+        rejected = [
+            lambda: op.vmult(buf[:n], buf[n // 2:n // 2 + n]),                 # y starts inside x
+            lambda: op.vmult_transpose(buf[n // 2:n // 2 + n], buf[:n]),       # x starts inside y
+            lambda: op.vmult_batched(buf[:2 * n], buf[n:3 * n], 2),            # second x is first y
+        ]
+        if kind == sf.OP_DG_ADVECT:
+            rejected.append(lambda: op.vmult_transpose_batched(buf[:2 * n], buf[n:3 * n], 2))
+        if kind != sf.OP_DG_ADVECT:
+            b, d, t = (torch.ones(n, dtype=torch.float64, device=dev) for _ in range(3))
+            x = buf[:n]
+            rejected += [lambda: op.chebyshev_step(b, d, x, b, t, 0.5, 0.5),   # x_new is b
+                         lambda: op.chebyshev_step(b, d, x, buf[n:2 * n], x, 0.5, 0.5),  # t is x_old
+                         lambda: op.chebyshev_step(b, d, x, t, t, 0.5, 0.5)]   # x_new is t
+        for call in rejected:
+            with pytest.raises(sf.SFError) as e:
+                call()
+            assert e.value.code == sf.SF_ERR_INVALID and "overlap" in str(e.value)
+        assert op.device_status() == 0
+    g = torch.Generator(device=dev).manual_seed(5)
+    ax, b, d, xo, t = (torch.rand(1000, dtype=torch.float64, device=dev, generator=g) for _ in range(5))
+    t_ref = 0.6 * t + 0.45 * d * (ax - b)
+    x_ref = xo - t_ref
+    sf.vector_update(ax, b, d, xo, ax, t, 0.45, 0.6)
+    torch.cuda.synchronize()
+    assert float((t - t_ref).abs().max()) < 4e-15 and float((ax - x_ref).abs().max()) < 4e-15
+    with pytest.raises(sf.SFError) as e:
+        sf.vector_update(ax, b, d, xo, t, t, 0.45, 0.6)
+    assert e.value.code == sf.SF_ERR_INVALID

@@ -1,9 +1,10 @@
 """sf_vmult_transpose_static: the transposed advection apply for callers that
 cannot allocate device memory while they run (applications that hand out all
 device memory from their own pool or a fixed budget).  Its intermediate
-vector lives in a fixed 4 MiB array inside the library.  The results must match sf_vmult_transpose_batched, which uses a
-cudaMalloc'd buffer, on two calls in a row (the shared array keeps the
-previous call's contents), and sizes beyond the array must be refused.
+vector lives in a fixed 4 MiB array inside the library.  The results must
+match sf_vmult_transpose_batched on two calls in a row (the shared array
+keeps the previous call's contents); sizes beyond the array and overlapping
+vectors must be refused.
 
 This file is collected last (test_zz_*) so that a failing run that stops at
 the first failure has already run every other test."""
@@ -48,5 +49,8 @@ def test_static_scratch_rejects_oversized_requests():
     code = sf.lib().sf_vmult_transpose_static(op._h, sf.FP64, 8, x.data_ptr(), y.data_ptr(), None)
     assert code == -1
     assert b"exceeds the static scratch" in sf.lib().sf_last_error()
+    # y starting one entry into x
+    assert sf.lib().sf_vmult_transpose_static(op._h, sf.FP64, 1, x.data_ptr(), x.data_ptr() + 8, None) == -1
+    assert b"overlap" in sf.lib().sf_last_error()
     lap = sf.Operator(sf.OP_LAPLACE, degree=2, n_cells=(2, 2, 2))
     assert sf.lib().sf_vmult_transpose_static(lap._h, sf.FP64, 1, x.data_ptr(), y.data_ptr(), None) == -9
