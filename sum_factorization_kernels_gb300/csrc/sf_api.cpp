@@ -576,9 +576,20 @@ int sf_rk_stage(sf_op *op, int prec, int nrhs, const void *src, const void *upd,
   SF_RET(check_ptr(vec_np, prec, "vec_np"));
   if (c_tm != 0.0) SF_RET(check_ptr(vec_tm, prec, "vec_tm"));
   if (nrhs < 1 || nrhs > 64) return fail(SF_ERR_INVALID, "nrhs must be 1..64");
-  if (src == vec_np || (c_tm != 0.0 && src == vec_tm))
-    return fail(SF_ERR_INVALID, "src must not be an output vector");
-  if (c_tm != 0.0 && vec_np == vec_tm) return fail(SF_ERR_INVALID, "vec_np and vec_tm must differ");
+  {
+    // src and the outputs are disjoint; upd is one of the other vectors
+    // itself (as in the reference's do_time_step) or disjoint from it
+    const size_t bytes = (size_t)nrhs * (size_t)op->n_dofs * elem_size(prec);
+    const bool tm = c_tm != 0.0;
+    if (ranges_overlap(src, vec_np, bytes) || (tm && ranges_overlap(src, vec_tm, bytes)))
+      return fail(SF_ERR_INVALID, "src must not overlap an output vector");
+    if (tm && ranges_overlap(vec_np, vec_tm, bytes))
+      return fail(SF_ERR_INVALID, "vec_np and vec_tm must not overlap");
+    const void *other[3] = {src, vec_np, tm ? vec_tm : nullptr};
+    for (const void *v : other)
+      if (v && v != upd && ranges_overlap(upd, v, bytes))
+        return fail(SF_ERR_INVALID, "upd must be src, vec_np, vec_tm itself or not overlap them");
+  }
   const Region region(op->region_ch);
   if (advect_tensor(op))
     return launch_dg_advect_tensor(op, prec, nrhs, false, src, nullptr, nullptr, nullptr, nullptr, c_np, c_tm,
@@ -594,8 +605,14 @@ int sf_lsrk_step(sf_op *op, int prec, int nrhs, void *sol_new, void *sol_old, vo
 {
   if (!op) return fail(SF_ERR_NULL, "op is NULL");
   if (!sol_new || !sol_old || !sol_tmp) return fail(SF_ERR_NULL, "sol_new/sol_old/sol_tmp is NULL");
-  if (sol_new == sol_old || sol_new == sol_tmp || sol_old == sol_tmp)
-    return fail(SF_ERR_INVALID, "sol_new, sol_old and sol_tmp must be distinct");
+  if (nrhs < 1 || nrhs > 64) return fail(SF_ERR_INVALID, "nrhs must be 1..64");
+  SF_RET(check_prec(op, prec));
+  {
+    const size_t bytes = (size_t)nrhs * (size_t)op->n_dofs * elem_size(prec);
+    if (ranges_overlap(sol_new, sol_old, bytes) || ranges_overlap(sol_new, sol_tmp, bytes) ||
+        ranges_overlap(sol_old, sol_tmp, bytes))
+      return fail(SF_ERR_INVALID, "sol_new, sol_old and sol_tmp must not overlap");
+  }
   const double a21 = 970286171893. / 4311952581923.;
   const double a32 = 6584761158862. / 12103376702013.;
   const double a43 = 2251764453980. / 15575788980749.;

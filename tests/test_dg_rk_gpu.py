@@ -98,6 +98,17 @@ def test_rk_stage_batched_and_errors(golden):
         op.rk_stage(src, upd, vnp, vnp, 0.02, -0.01, nrhs=8)      # vec_np == vec_tm
     with pytest.raises(sf.SFError):
         op.lsrk_step(vnp, vnp, vtm, 0.01, nrhs=8)                 # registers must differ
+    # partial overlaps (views one right-hand side apart in one buffer)
+    big = torch.zeros(10 * N, dtype=torch.float64, device="cuda:0")
+    for call in (lambda: op.rk_stage(src, upd, big[:8 * N], big[N:9 * N], 0.02, -0.01, nrhs=8),
+                 lambda: op.rk_stage(big[N:9 * N], upd, big[:8 * N], vtm, 0.02, -0.01, nrhs=8),
+                 lambda: op.rk_stage(src, big[N:9 * N], big[:8 * N], vtm, 0.02, -0.01, nrhs=8),
+                 lambda: op.lsrk_step(big[:8 * N], big[N:9 * N], vtm, 0.01, nrhs=8)):
+        with pytest.raises(sf.SFError) as e:
+            call()
+        assert e.value.code == sf.SF_ERR_INVALID and "overlap" in str(e.value)
+    op.rk_stage(src, vnp, vnp, vtm, 0.02, -0.01, nrhs=8)          # upd is vec_np itself: allowed
+    assert op.device_status() == 0
     lap = sf.Operator(sf.OP_LAPLACE, degree=2, n_cells=(2, 2, 2))
     x = torch.zeros(lap.n_dofs, dtype=torch.float64, device="cuda:0")
     with pytest.raises(sf.SFError):
