@@ -213,7 +213,8 @@ int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv,
  *   vec_np = upd + c_np * r   and, when c_tm != 0,   vec_tm = vec_np + c_tm * r
  * (vec_tm is not touched when c_tm == 0 and may then be NULL).  upd may be the
  * same vector as src, vec_np or vec_tm, as in the reference's do_time_step;
- * src must not be vec_np or vec_tm.  nrhs vectors of n_dofs entries each,
+ * any other overlap (src with an output, vec_np with vec_tm, upd partly
+ * over another vector) is refused with SF_ERR_INVALID.  nrhs vectors of n_dofs entries each,
  * contiguous.  The reference's current_time argument only names the exact
  * solution's transport direction, which here is the handle's velocity. */
 int sf_rk_stage(sf_op *op, int prec, int nrhs, const void *src, const void *upd, void *vec_np,
@@ -222,7 +223,7 @@ int sf_rk_stage(sf_op *op, int prec, int nrhs, const void *src, const void *upd,
  * do_time_step (evaluation_dg_advect.h:190-214) with step dt: five fused
  * stages with the reference's coefficients and register rotation; sol_new
  * is advanced in place, sol_old and sol_tmp are the scheme's two registers
- * (contents on entry are not used; three distinct vectors). */
+ * (contents on entry are not used; three vectors that do not overlap). */
 int sf_lsrk_step(sf_op *op, int prec, int nrhs, void *sol_new, void *sol_old, void *sol_tmp, double dt,
                  void *stream);
 /* The same update without the operator, replaces
