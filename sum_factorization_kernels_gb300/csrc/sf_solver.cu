@@ -745,6 +745,10 @@ extern "C" int sf_cg_solve(sf_op *op, const double *b, double *x, const sf_solve
     set_error("op/b/x/opts is NULL");
     return SF_ERR_NULL;
   }
+  if (reinterpret_cast<uintptr_t>(b) % sizeof(double) || reinterpret_cast<uintptr_t>(x) % sizeof(double)) {
+    set_error("b/x not aligned to the element size");
+    return SF_ERR_ALIGN;
+  }
   const sf_solve_opts o = *opts;
   if (o.mode != SF_SOLVE_FP64 && o.mode != SF_SOLVE_MIXED) {
     set_error("unknown solve mode");

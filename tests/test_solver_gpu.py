@@ -101,3 +101,8 @@ def test_invalid_options_and_advection_rejected():
     code, _ = op2.cg_solve(b[: op2.n_dofs].contiguous(), x[: op2.n_dofs].contiguous(),
                            sf.default_solve_opts(cheb_range=0.5))
     assert code == -1
+    # vectors off the element alignment are refused before anything runs
+    code, _ = op2.cg_solve(b.data_ptr() + 4, x)
+    assert code == sf.SF_ERR_ALIGN
+    code, _ = op2.cg_solve(b, x.data_ptr() + 4)
+    assert code == sf.SF_ERR_ALIGN
