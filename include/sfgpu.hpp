@@ -51,6 +51,17 @@ public:
   DeviceVector(const DeviceVector &) = delete;
   DeviceVector &operator=(const DeviceVector &) = delete;
   DeviceVector(DeviceVector &&o) noexcept : ptr_(o.ptr_), n_(o.n_) { o.ptr_ = nullptr; o.n_ = 0; }
+  DeviceVector &operator=(DeviceVector &&o) noexcept
+  {
+    if (this != &o) {
+      if (ptr_) cudaFree(ptr_);
+      ptr_ = o.ptr_;
+      n_ = o.n_;
+      o.ptr_ = nullptr;
+      o.n_ = 0;
+    }
+    return *this;
+  }
   ~DeviceVector() { if (ptr_) cudaFree(ptr_); }
   void resize(std::size_t n)
   {

@@ -166,3 +166,22 @@ def test_operator_kinds_without_gpu():
         d.kind = kind
         assert L.sf_create(C.byref(d), C.byref(h)) == sfgpu.SF_ERR_UNSUPPORTED, kind
     assert not h.value
+
+
+def test_cpp_layer_builds_without_gpu(tmp_path):
+    """the C++ driver of include/sfgpu.hpp (the reference's evaluator-class
+    pattern) compiles without warnings and links against the library and
+    the oracle; running it needs a GPU"""
+    import subprocess
+    from oracle import build as obuild
+    sfgpu, _ = _lib()
+    olib = obuild.build_oracle()
+    cuda = "/usr/local/cuda"
+    exe = str(tmp_path / "cpp_api_check")
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(ROOT, "oracle"), "-I", cuda + "/include",
+           os.path.join(ROOT, "tests", "cpp", "cpp_api_check.cc"), "-o", exe,
+           sfgpu.LIB_PATH, olib, "-L", cuda + "/lib64", "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert os.path.exists(exe)
