@@ -203,6 +203,12 @@ def check_status(op, what):
 # CPU leg: the oracle port timed on the host cores (cpu_baseline and the
 # reference arm), and the oracle's strict build stating the GPU's errors
 # --------------------------------------------------------------------------
+def perf_build_flags():
+    """the gcc flags of the timed oracle build (recorded when it was built)"""
+    from oracle import build as obuild
+    return obuild.perf_build_flags()
+
+
 def _cpu_env():
     os.environ.setdefault("OMP_PROC_BIND", "close")
     os.environ.setdefault("OMP_PLACES", "cores")
@@ -245,7 +251,7 @@ def cpu_cont_baseline(p, ncells, repeats=CPU_REPEATS):
     return {"value": round(n / best / 1e9, 4), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "the full %d^3 deformed p=%d workload (%d DoFs), FP64, precomputed geometry, best of %d "
                       "applies (%s s)" % (ncells, p, n, repeats, ", ".join("%.3f" % t for t in ts)),
-            "build": "gcc -O3 -mcpu/-march=native -ffp-contract=fast -fopenmp, OMP_PROC_BIND=close",
+            "build": "gcc " + perf_build_flags() + ", OMP_PROC_BIND=close",
             "host": host_cpu()}
 
 
@@ -341,7 +347,7 @@ def run_reference(args):
     base = {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "the full %d^3 deformed p=%d workload (%d DoFs) every step, FP64, precomputed geometry; "
                       "value from the best of %d steps (median %.4f s, best %.4f s)" % (nc, p, n, len(ts), med, best),
-            "build": "gcc -O3 -mcpu/-march=native -ffp-contract=fast -fopenmp, OMP_PROC_BIND=close",
+            "build": "gcc " + perf_build_flags() + ", OMP_PROC_BIND=close",
             "host": host_cpu()}
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,

@@ -98,21 +98,57 @@ def build_oracle(force: bool = False) -> str:
     return out
 
 
+# named CPU targets of the timing build, by the "CPU part" field of
+# /proc/cpuinfo on Arm hosts (0xd4f: Neoverse V2, the Grace CPU); a fixed
+# target instead of -mcpu=native keeps the flags the same on every host of a
+# kind and recordable.  Other hosts get generic -O3 code.
+ARM_PARTS = {"0xd4f": "neoverse-v2"}
+PERF_FLAGS = ["-O3", "-ffp-contract=fast", "-std=gnu11", "-fopenmp"]
+
+
+def perf_target() -> list[str]:
+    import platform
+    if platform.machine() not in ("aarch64", "arm64"):
+        return []
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("cpu part"):
+                    part = line.split(":", 1)[1].strip().lower()
+                    return ["-mcpu=" + ARM_PARTS[part]] if part in ARM_PARTS else []
+    except OSError:
+        pass
+    return []
+
+
+def perf_build_flags() -> str:
+    """the gcc flags liboracle_perf.so was built with (written beside it)"""
+    path = os.path.join(HERE, "liboracle_perf.flags")
+    return open(path).read().strip() if os.path.exists(path) else "unknown"
+
+
 def build_oracle_perf(force: bool = False) -> str:
     """the oracle source compiled for timing as the CPU baseline: -O3, tuned
-    for the host CPU, floating-point contraction allowed (the flags the
-    reference's drivers are benchmarked with), OpenMP"""
-    import platform
+    for the host CPU where it is a known target, floating-point contraction
+    allowed (the flags the reference's drivers are benchmarked with), OpenMP"""
     out = os.path.join(HERE, "liboracle_perf.so")
+    flags_file = os.path.join(HERE, "liboracle_perf.flags")
     src = os.path.join(HERE, "sf_oracle.c")
-    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(
+    if not force and os.path.exists(out) and os.path.exists(flags_file) and os.path.getmtime(out) >= max(
             os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "sf_oracle.h"))):
         return out
-    tune = "-mcpu=native" if platform.machine() in ("aarch64", "arm64") else "-march=native"
     tmp = out + ".tmp%d" % os.getpid()
-    _run(["gcc", "-O3", tune, "-ffp-contract=fast", "-std=gnu11", "-fopenmp", "-fPIC", "-shared", "-o", tmp,
-          src, "-lm"])
+    flags = PERF_FLAGS + perf_target()
+    try:
+        _run(["gcc"] + flags + ["-fPIC", "-shared", "-o", tmp, src, "-lm"])
+    except RuntimeError:
+        if flags == PERF_FLAGS:
+            raise
+        flags = list(PERF_FLAGS)  # the compiler does not know the target: generic code
+        _run(["gcc"] + flags + ["-fPIC", "-shared", "-o", tmp, src, "-lm"])
     os.replace(tmp, out)
+    with open(flags_file, "w") as f:
+        f.write(" ".join(flags) + "\n")
     return out
 
 
