@@ -98,27 +98,18 @@ def build_oracle(force: bool = False) -> str:
     return out
 
 
-# named CPU targets of the timing build, by the "CPU part" field of
-# /proc/cpuinfo on Arm hosts (0xd4f: Neoverse V2, the Grace CPU); a fixed
-# target instead of -mcpu=native keeps the flags the same on every host of a
-# kind and recordable.  Other hosts get generic -O3 code.
-ARM_PARTS = {"0xd4f": "neoverse-v2"}
 PERF_FLAGS = ["-O3", "-ffp-contract=fast", "-std=gnu11", "-fopenmp"]
 
 
 def perf_target() -> list[str]:
+    """CPU target of the timing build.  Arm hosts: -mcpu=native, the
+    extensions the host reports (the named target -mcpu=neoverse-v2 enables
+    extensions that the Grace hosts here do not expose, and its build died
+    with SIGILL); other hosts: generic code.  The timed build is the CPU
+    baseline only; the oracle build that results are checked against uses
+    no CPU-specific flags."""
     import platform
-    if platform.machine() not in ("aarch64", "arm64"):
-        return []
-    try:
-        with open("/proc/cpuinfo") as f:
-            for line in f:
-                if line.lower().startswith("cpu part"):
-                    part = line.split(":", 1)[1].strip().lower()
-                    return ["-mcpu=" + ARM_PARTS[part]] if part in ARM_PARTS else []
-    except OSError:
-        pass
-    return []
+    return ["-mcpu=native"] if platform.machine() in ("aarch64", "arm64") else []
 
 
 def perf_build_flags() -> str:

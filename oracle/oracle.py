@@ -96,7 +96,7 @@ _perf = None
 
 
 def perf_lib():
-    """the same source built for timing (-O3, a named CPU target, contraction
+    """the same source built for timing (-O3, host CPU tuning, contraction
     allowed): the CPU baseline; results agree with lib() to rounding"""
     global _perf
     if _perf is None:
