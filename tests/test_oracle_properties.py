@@ -380,3 +380,34 @@ def test_affine_continuous_operators_are_assembled_kronecker_products(p, basis):
         for name, ref, Y in cases:
             Y = np.where(bnd, X, Y).ravel()
             assert np.linalg.norm(Y - ref) / np.linalg.norm(ref) < 1e-13, (name, nc)
+
+
+@pytest.mark.parametrize("p", [1, 2, 4, 7])
+def test_continuous_null_space_boundary_rows_and_volume(p):
+    """GLL basis, deformed box: without Dirichlet conditions the Laplacian
+    annihilates constants (the nodal basis sums to one) and its quadratic
+    form, the Dirichlet energy, is positive off the constants; with them the
+    boundary rows are the identity and the interior rows ignore boundary
+    values; the mass matrix integrates one to the box volume"""
+    nc, length = (3, 2, 2), (0.9, 0.6, 0.5)
+    rng = np.random.default_rng(p)
+    m0 = O.mesh(p, nc, length=length, deform=0.05, dirichlet=0)
+    G = O.cont_geometry(m0)
+    n = O.cont_n_dofs(m0)
+    x = rng.uniform(-1, 1, n)
+    ax = O.cont_apply(m0, G, x)
+    assert np.abs(O.cont_apply(m0, G, np.ones(n))).max() < 1e-13 * np.abs(ax).max()
+    assert x @ ax > 0
+    nn = [p * c + 1 for c in nc]
+    Z, Y, X = np.meshgrid(*(np.arange(k) for k in nn[::-1]), indexing="ij")
+    bnd = ((X == 0) | (X == nn[0] - 1) | (Y == 0) | (Y == nn[1] - 1) | (Z == 0) | (Z == nn[2] - 1)).ravel()
+    m1 = O.mesh(p, nc, length=length, deform=0.05, dirichlet=1)
+    y1 = O.cont_apply(m1, G, x)
+    assert np.array_equal(y1[bnd], x[bnd])
+    x0 = np.where(bnd, 0.0, x)
+    assert np.allclose(y1[~bnd], O.cont_apply(m1, G, x0)[~bnd], rtol=0, atol=1e-14 * np.abs(y1).max())
+    assert np.allclose(y1[~bnd], ax[~bnd] - O.cont_apply(m0, G, x - x0)[~bnd], rtol=0,
+                       atol=1e-13 * np.abs(y1).max())
+    ma = O.mesh(p, nc, length=length, dirichlet=0)
+    one = np.ones(O.cont_n_dofs(ma))
+    assert abs(one @ O.cont_apply_op(ma, O.OP_MASS, one) - np.prod(length)) < 1e-14
