@@ -4,7 +4,9 @@ advection p=4 on 48^3 periodic cells (forward with the inverse mass, the
 transpose with the inverse mass in one launch), the DO_FACES Laplacian and
 convection forms on 48^3 cells, and the affine continuous Laplacian and mass
 matrix on 64^3 cells with Dirichlet conditions.  At these sizes the grids run
-many blocks per SM and the z pass of the Kronecker form walks long lines."""
+many blocks per SM and the z pass of the Kronecker form walks long lines.
+The advection kernels also keep two size-independent properties there:
+conservation and constants transported unchanged."""
 import os
 
 import numpy as np
@@ -67,3 +69,27 @@ def test_affine_continuous_64c_vs_oracle():
     mass = sf.Operator(sf.OP_MASS, degree=p, n_cells=nc)
     _check(torch, mass.vmult, x, O.cont_apply_op(m, O.OP_MASS, x), p)
     assert lap.device_status() == 0 and mass.device_status() == 0
+
+
+def test_advect_48c_conserves_and_transports_constants():
+    """size-independent properties at the bench's size, both kernels, FP64:
+    the entries of A u sum to zero and A 1 = 0 on the periodic mesh (without
+    and with the inverse mass)"""
+    torch = torch_cuda()
+    sf = _sf()
+    p, nc, vel = 4, (48, 48, 48), (1.0, 0.5, 0.25)
+    for invm in (0, 1):
+        op = sf.Operator(sf.OP_DG_ADVECT, degree=p, n_cells=nc, velocity=vel, inverse_mass=invm)
+        gen = torch.Generator(device="cuda:0").manual_seed(invm)
+        u = torch.rand(op.n_dofs, dtype=torch.float64, device="cuda:0", generator=gen) * 2 - 1
+        one = torch.ones_like(u)
+        for variant in (sf.KERNEL_AUTO, sf.KERNEL_GENERIC):
+            op.set_kernel_variant(variant)
+            au, a1 = torch.empty_like(u), torch.empty_like(u)
+            op.vmult(u, au)
+            op.vmult(one, a1)
+            torch.cuda.synchronize()
+            if not invm:
+                assert abs(float(au.sum())) < 1e-12 * float(au.abs().sum()), variant
+            assert float(a1.abs().max()) < 1e-12 * float(au.abs().max()), (invm, variant)
+        assert op.device_status() == 0

@@ -411,3 +411,20 @@ def test_continuous_null_space_boundary_rows_and_volume(p):
     ma = O.mesh(p, nc, length=length, dirichlet=0)
     one = np.ones(O.cont_n_dofs(ma))
     assert abs(one @ O.cont_apply_op(ma, O.OP_MASS, one) - np.prod(length)) < 1e-14
+
+
+@pytest.mark.parametrize("p", [1, 3, 5, 8])
+def test_advect_conserves_and_transports_constants(p):
+    """periodic mesh, constant velocity, GLL nodal basis: the upwind fluxes
+    cancel across faces and the basis sums to one, so the entries of A u sum
+    to zero (conservation, 1^T A = 0) and A 1 = 0 (a constant state does not
+    change), also with the inverse mass"""
+    d = O.dg(p, (3, 2, 2), (0.3, 0.5, 0.2), velocity=(1.0, -0.5, 0.25), inverse_mass=0)
+    u = np.random.default_rng(p).uniform(-1, 1, O.dg_n_dofs(d))
+    one = np.ones_like(u)
+    au = O.dg_advect_apply(d, u)
+    assert abs(au.sum()) < 1e-14 * np.abs(au).sum()
+    assert np.abs(O.dg_advect_apply(d, one)).max() < 1e-14 * np.abs(au).max()
+    assert abs(O.dg_advect_apply_transpose(d, u).sum()) < 1e-14 * np.abs(au).sum()
+    di = O.dg(p, (3, 2, 2), (0.3, 0.5, 0.2), velocity=(1.0, -0.5, 0.25), inverse_mass=1)
+    assert np.abs(O.dg_advect_apply(di, one)).max() < 1e-13 * np.abs(O.dg_advect_apply(di, u)).max()
