@@ -428,3 +428,18 @@ def test_advect_conserves_and_transports_constants(p):
     assert abs(O.dg_advect_apply_transpose(d, u).sum()) < 1e-14 * np.abs(au).sum()
     di = O.dg(p, (3, 2, 2), (0.3, 0.5, 0.2), velocity=(1.0, -0.5, 0.25), inverse_mass=1)
     assert np.abs(O.dg_advect_apply(di, one)).max() < 1e-13 * np.abs(O.dg_advect_apply(di, u)).max()
+
+
+@pytest.mark.parametrize("p", [1, 3, 5, 8])
+def test_dg_laplacians_periodic_null_space(p):
+    """periodic meshes: the SIPG operator and its precomputed tensor-product
+    form annihilate constants (the Hermite-like basis sums to one), so the
+    entries of A u sum to zero as well (symmetry), and u^T A u > 0 off the
+    constants"""
+    mesh, h = (3, 2, 2), (0.3, 0.5, 0.2)
+    for d, apply in ((O.dg(p, mesh, h, penalty=1.5), O.dg_sipg_apply), (O.dg(p, mesh, h), O.dg_precomputed_apply)):
+        u = np.random.default_rng(p).uniform(-1, 1, O.dg_n_dofs(d))
+        au = apply(d, u)
+        assert np.abs(apply(d, np.ones_like(u))).max() < 1e-14 * np.abs(au).max()
+        assert abs(au.sum()) < 1e-14 * np.abs(au).sum()
+        assert u @ au > 0
