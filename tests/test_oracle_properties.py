@@ -1,7 +1,9 @@
 """Mathematical identities of the oracle itself (size-independent checks that
 complement the golden vectors): symmetry, explicit transposes and diagonals,
-the analytic advection derivative of the reference's self-check, and central
-finite differences for the kappa gradient."""
+the analytic advection derivative of the reference's self-check, central
+finite differences for the kappa gradient, null spaces, boundary rows and
+conservation, and the Kronecker-product and line-operator forms that the
+structured kernels evaluate."""
 import numpy as np
 import pytest
 
