@@ -1,9 +1,10 @@
 """ctypes binding of the sfgpu C ABI (include/sfgpu.h).
 
 Loads the in-tree ``libsfgpu.so`` built for sm_103a and fails loudly when it
-is missing: there is no CPU fallback.  Arrays are passed as device pointers;
-anything with ``data_ptr()`` (a CUDA ``torch.Tensor``) or an integer address
-works.  PyTorch is only the allocator here.
+is missing: there is no CPU fallback.  Arrays are passed as device pointers:
+a CUDA ``torch.Tensor`` (checked to be contiguous, of the call's precision
+and long enough, since the library cannot see buffer sizes) or an integer
+address (passed on unchecked).  PyTorch is only the allocator here.
 """
 from __future__ import annotations
 
@@ -131,6 +132,25 @@ def prec_of(t):
     raise TypeError("vectors must be float32 or float64, got %s" % t.dtype)
 
 
+def vec(t, n, prec, name):
+    """device address of a vector argument.  The library cannot see buffer
+    sizes (a short buffer would be written past its end), so a tensor must
+    be a contiguous CUDA tensor of the call's precision with at least n
+    entries; None and integer addresses are passed on unchecked."""
+    if t is None or isinstance(t, int):
+        return t
+    if not t.is_cuda:
+        raise ValueError("%s must be a CUDA tensor" % name)
+    if not t.is_contiguous():
+        raise ValueError("%s must be contiguous" % name)
+    if prec_of(t) != prec:
+        raise TypeError("%s is %s; this call computes in %s" % (name, t.dtype, "float64" if prec == FP64
+                                                                 else "float32"))
+    if t.numel() < n:
+        raise ValueError("%s holds %d entries; this call needs %d" % (name, t.numel(), n))
+    return t.data_ptr()
+
+
 def stream_ptr(stream):
     if stream is None:
         import torch
@@ -200,58 +220,73 @@ class Operator:
         except Exception:
             pass
 
+    def _cell_points(self):
+        return self.n_cells * (self.degree + 1) ** 3
+
     def vmult(self, x, y, stream=None):
-        check(lib().sf_vmult(self._h, prec_of(x), ptr(x), ptr(y), stream_ptr(stream)))
+        pr, n = prec_of(x), self.n_dofs
+        check(lib().sf_vmult(self._h, pr, vec(x, n, pr, "x"), vec(y, n, pr, "y"), stream_ptr(stream)))
         return y
 
     def vmult_transpose(self, x, y, stream=None):
-        check(lib().sf_vmult_transpose(self._h, prec_of(x), ptr(x), ptr(y), stream_ptr(stream)))
+        pr, n = prec_of(x), self.n_dofs
+        check(lib().sf_vmult_transpose(self._h, pr, vec(x, n, pr, "x"), vec(y, n, pr, "y"), stream_ptr(stream)))
         return y
 
     def vmult_batched(self, x, y, nrhs, stream=None):
-        check(lib().sf_vmult_batched(self._h, prec_of(x), nrhs, ptr(x), ptr(y), stream_ptr(stream)))
+        pr, n = prec_of(x), int(nrhs) * self.n_dofs
+        check(lib().sf_vmult_batched(self._h, pr, nrhs, vec(x, n, pr, "x"), vec(y, n, pr, "y"), stream_ptr(stream)))
         return y
 
     def vmult_transpose_batched(self, x, y, nrhs, stream=None):
-        check(lib().sf_vmult_transpose_batched(self._h, prec_of(x), nrhs, ptr(x), ptr(y),
+        pr, n = prec_of(x), int(nrhs) * self.n_dofs
+        check(lib().sf_vmult_transpose_batched(self._h, pr, nrhs, vec(x, n, pr, "x"), vec(y, n, pr, "y"),
                                                stream_ptr(stream)))
         return y
 
     def vmult_transpose_static(self, x, y, nrhs=1, stream=None):
         """transposed advection apply that allocates nothing (see sfgpu.h)"""
-        check(lib().sf_vmult_transpose_static(self._h, prec_of(x), nrhs, ptr(x), ptr(y),
+        pr, n = prec_of(x), int(nrhs) * self.n_dofs
+        check(lib().sf_vmult_transpose_static(self._h, pr, nrhs, vec(x, n, pr, "x"), vec(y, n, pr, "y"),
                                               stream_ptr(stream)))
         return y
 
     def chebyshev_step(self, b, diag_inv, x_old, x_new, t, c_np, c_tm, stream=None):
-        check(lib().sf_chebyshev_step(self._h, prec_of(x_old), ptr(b), ptr(diag_inv), ptr(x_old),
-                                      ptr(x_new), ptr(t), float(c_np), float(c_tm),
-                                      stream_ptr(stream)))
+        pr, n = prec_of(x_old), self.n_dofs
+        check(lib().sf_chebyshev_step(self._h, pr, vec(b, n, pr, "b"), vec(diag_inv, n, pr, "diag_inv"),
+                                      vec(x_old, n, pr, "x_old"), vec(x_new, n, pr, "x_new"), vec(t, n, pr, "t"),
+                                      float(c_np), float(c_tm), stream_ptr(stream)))
 
     def rk_stage(self, src, upd, vec_np, vec_tm, c_np, c_tm, nrhs=1, stream=None):
         """do_rk_stage<true>: vec_np = upd + c_np A src, vec_tm = vec_np + c_tm A src"""
-        check(lib().sf_rk_stage(self._h, prec_of(src), int(nrhs), ptr(src), ptr(upd), ptr(vec_np), ptr(vec_tm),
+        pr, n = prec_of(src), int(nrhs) * self.n_dofs
+        check(lib().sf_rk_stage(self._h, pr, int(nrhs), vec(src, n, pr, "src"), vec(upd, n, pr, "upd"),
+                                vec(vec_np, n, pr, "vec_np"), vec(vec_tm, n, pr, "vec_tm"),
                                 float(c_np), float(c_tm), stream_ptr(stream)))
 
     def lsrk_step(self, sol_new, sol_old, sol_tmp, dt, nrhs=1, stream=None):
         """do_time_step: one LSRK(5,4) step, sol_new advanced in place"""
-        check(lib().sf_lsrk_step(self._h, prec_of(sol_new), int(nrhs), ptr(sol_new), ptr(sol_old), ptr(sol_tmp),
+        pr, n = prec_of(sol_new), int(nrhs) * self.n_dofs
+        check(lib().sf_lsrk_step(self._h, pr, int(nrhs), vec(sol_new, n, pr, "sol_new"),
+                                 vec(sol_old, n, pr, "sol_old"), vec(sol_tmp, n, pr, "sol_tmp"),
                                  float(dt), stream_ptr(stream)))
 
     def diagonal(self, out, stream=None):
-        check(lib().sf_diagonal(self._h, prec_of(out), ptr(out), stream_ptr(stream)))
+        pr = prec_of(out)
+        check(lib().sf_diagonal(self._h, pr, vec(out, self.n_dofs, pr, "out"), stream_ptr(stream)))
         return out
 
     def kappa_gradient(self, u, lam, out, stream=None):
-        check(lib().sf_kappa_gradient(self._h, prec_of(u), ptr(u), ptr(lam), ptr(out),
-                                      stream_ptr(stream)))
+        pr, n = prec_of(u), self.n_dofs
+        check(lib().sf_kappa_gradient(self._h, pr, vec(u, n, pr, "u"), vec(lam, n, pr, "lam"),
+                                      vec(out, self._cell_points(), pr, "out"), stream_ptr(stream)))
         return out
 
     def set_geometry(self, G):
-        check(lib().sf_set_geometry(self._h, ptr(G)))
+        check(lib().sf_set_geometry(self._h, vec(G, 6 * self._cell_points(), FP64, "G")))
 
     def set_coefficient(self, kappa):
-        check(lib().sf_set_coefficient(self._h, ptr(kappa)))
+        check(lib().sf_set_coefficient(self._h, vec(kappa, self._cell_points(), FP64, "kappa")))
 
     def set_kernel_variant(self, variant):
         check(lib().sf_set_kernel_variant(self._h, int(variant)))
@@ -264,7 +299,8 @@ class Operator:
     def cg_solve(self, b, x, opts=None, stream=None):
         o = default_solve_opts() if opts is None else opts
         st = SolveStats()
-        code = lib().sf_cg_solve(self._h, ptr(b), ptr(x), C.byref(o), C.byref(st), stream_ptr(stream))
+        code = lib().sf_cg_solve(self._h, vec(b, self.n_dofs, FP64, "b"), vec(x, self.n_dofs, FP64, "x"),
+                                 C.byref(o), C.byref(st), stream_ptr(stream))
         return code, st
 
 
@@ -277,19 +313,24 @@ def default_solve_opts(**kw):
 
 
 def dot(x, y, out, stream=None):
-    check(lib().sf_dot(x.numel(), prec_of(x), ptr(x), ptr(y), ptr(out), stream_ptr(stream)))
+    pr, n = prec_of(x), x.numel()
+    check(lib().sf_dot(n, pr, vec(x, n, pr, "x"), vec(y, n, pr, "y"), vec(out, 1, FP64, "out"),
+                       stream_ptr(stream)))
     return out
 
 
 def convert(x, y, stream=None):
-    check(lib().sf_convert(x.numel(), prec_of(x), ptr(x), prec_of(y), ptr(y), stream_ptr(stream)))
+    n = x.numel()
+    check(lib().sf_convert(n, prec_of(x), vec(x, n, prec_of(x), "x"), prec_of(y), vec(y, n, prec_of(y), "y"),
+                           stream_ptr(stream)))
     return y
 
 
 def vector_update(ax, b, dinv, x_old, x_new, t, c_np, c_tm, stream=None):
-    check(lib().sf_vector_update(x_old.numel(), prec_of(x_old), ptr(ax), ptr(b), ptr(dinv),
-                                 ptr(x_old), ptr(x_new), ptr(t), float(c_np), float(c_tm),
-                                 stream_ptr(stream)))
+    pr, n = prec_of(x_old), x_old.numel()
+    check(lib().sf_vector_update(n, pr, vec(ax, n, pr, "ax"), vec(b, n, pr, "b"), vec(dinv, n, pr, "dinv"),
+                                 vec(x_old, n, pr, "x_old"), vec(x_new, n, pr, "x_new"), vec(t, n, pr, "t"),
+                                 float(c_np), float(c_tm), stream_ptr(stream)))
 
 
 def shape_tables(degree, basis=BASIS_GLL):

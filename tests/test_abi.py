@@ -185,3 +185,40 @@ def test_cpp_layer_builds_without_gpu(tmp_path):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert os.path.exists(exe)
+
+
+def test_python_vector_checks_without_gpu():
+    """the Python layer refuses vectors the library could write past or
+    misread (it cannot see buffer sizes): host tensors, non-contiguous views,
+    the wrong precision, too few entries; None and integer addresses pass"""
+    torch = pytest.importorskip("torch")
+    sfgpu, _ = _lib()
+
+    class FakeCuda:  # the attributes of a CUDA tensor that the check reads
+        is_cuda = True
+
+        def __init__(self, n, dtype, contiguous=True):
+            self.n, self.dtype, self.contig = n, dtype, contiguous
+
+        def is_contiguous(self):
+            return self.contig
+
+        def numel(self):
+            return self.n
+
+        def data_ptr(self):
+            return 0x7000
+
+    f64, f32 = torch.float64, torch.float32
+    assert sfgpu.vec(None, 10, sfgpu.FP64, "x") is None
+    assert sfgpu.vec(0x1234, 10, sfgpu.FP64, "x") == 0x1234
+    assert sfgpu.vec(FakeCuda(10, f64), 10, sfgpu.FP64, "x") == 0x7000
+    assert sfgpu.vec(FakeCuda(12, f32), 10, sfgpu.FP32, "x") == 0x7000
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        sfgpu.vec(torch.zeros(10, dtype=f64), 10, sfgpu.FP64, "x")
+    with pytest.raises(ValueError, match="contiguous"):
+        sfgpu.vec(FakeCuda(10, f64, contiguous=False), 10, sfgpu.FP64, "x")
+    with pytest.raises(TypeError, match="computes in float64"):
+        sfgpu.vec(FakeCuda(10, f32), 10, sfgpu.FP64, "y")
+    with pytest.raises(ValueError, match="holds 9 entries; this call needs 10"):
+        sfgpu.vec(FakeCuda(9, f64), 10, sfgpu.FP64, "y")
