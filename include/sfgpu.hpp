@@ -96,6 +96,16 @@ private:
   std::size_t n_ = 0;
 };
 
+// a vector handed in by the caller must hold at least n entries: the C ABI
+// cannot see buffer sizes, and a short one would be written past its end
+template <typename Number>
+inline void check_size(const DeviceVector<Number> &v, long long n, const char *name)
+{
+  if ((long long)v.size() < n)
+    throw Error(SF_ERR_INVALID, std::string(name) + " holds " + std::to_string(v.size()) +
+                                    " entries, the operator needs " + std::to_string(n));
+}
+
 // owning handle of one operator
 class Operator {
 public:
@@ -236,6 +246,14 @@ public:
                      DeviceVector<Number> &vec_tm, Number coefficient_np, Number coefficient_tm,
                      cudaStream_t s = 0)
   {
+    const long long n = op_.n_dofs();
+    check_size(sol_old_, n, "sol_old");
+    check_size(sol_new_, n, "sol_new");
+    if (evaluate_chebyshev) {
+      check_size(src, n, "src");
+      check_size(mat_diagonal_, n, "mat_diagonal");
+      check_size(vec_tm, n, "vec_tm");
+    }
     if (!evaluate_chebyshev)
       check(sf_vmult(op_.get(), precision_of<Number>(), sol_old_.begin(), sol_new_.begin(), s));
     else
@@ -358,6 +376,13 @@ public:
                    DeviceVector<Number> &vec_np, DeviceVector<Number> &vec_tm, double /*current_time*/,
                    Number c_np, Number c_tm, cudaStream_t s = 0)
   {
+    const long long n = op_.n_dofs();
+    check_size(src, n, "src");
+    check_size(vec_np, n, "vec_np");
+    if (evaluate_stage) {
+      check_size(upd, n, "upd");
+      if (c_tm != Number(0)) check_size(vec_tm, n, "vec_tm");
+    }
     if (evaluate_stage)
       check(sf_rk_stage(op_.get(), precision_of<Number>(), 1, src.begin(), upd.begin(), vec_np.begin(),
                         vec_tm.begin(), double(c_np), double(c_tm), s));

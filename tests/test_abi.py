@@ -185,6 +185,21 @@ def test_cpp_layer_builds_without_gpu(tmp_path):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert os.path.exists(exe)
+    # the member templates that take the caller's vectors, in both modes
+    src = tmp_path / "members.cc"
+    src.write_text('#include "sfgpu.hpp"\n'
+                   "void use(sfgpu::EvaluationDGAdvection<4, double> &e, sfgpu::EvaluationDGLaplacian<3, float> &l,\n"
+                   "         sfgpu::DeviceVector<double> &v, sfgpu::DeviceVector<float> &w)\n"
+                   "{\n"
+                   "  e.do_rk_stage<true>(v, v, v, v, 0.0, 0.1, 0.2);\n"
+                   "  e.do_rk_stage<false>(v, v, v, v, 0.0, 0.1, 0.2);\n"
+                   "  l.do_cheby_iter<true>(w, w, w, w, w, 0.5f, 0.5f);\n"
+                   "  l.do_cheby_iter<false>(w, w, w, w, w, 0.5f, 0.5f);\n"
+                   "}\n")
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror", "-I",
+                        os.path.join(ROOT, "include"), "-I", cuda + "/include", str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
 
 
 def test_python_vector_checks_without_gpu():
