@@ -169,8 +169,10 @@ int sf_vmult(sf_op *op, int prec, const void *x, void *y, void *stream);
 /* y = A^T x.  The Laplacians are symmetric (A^T = A); for advection this is
  * the transpose-upwind adjoint.  No reference counterpart. */
 int sf_vmult_transpose(sf_op *op, int prec, const void *x, void *y, void *stream);
-/* y[r] = A x[r] for r < nrhs; x and y hold nrhs vectors of n_dofs entries
- * back to back.  One launch for all right-hand sides. */
+/* y[r] = A x[r] for r < nrhs (1..64); x and y hold nrhs vectors of n_dofs
+ * entries back to back.  The DG and face-term operators treat all
+ * right-hand sides in one launch; the continuous operators apply them one
+ * after another on the stream. */
 int sf_vmult_batched(sf_op *op, int prec, int nrhs, const void *x, void *y, void *stream);
 int sf_vmult_transpose_batched(sf_op *op, int prec, int nrhs, const void *x, void *y,
                                void *stream);
