@@ -216,9 +216,10 @@ int sf_chebyshev_step(sf_op *op, int prec, const void *b, const void *diag_inv,
  * (vec_tm is not touched when c_tm == 0 and may then be NULL).  upd may be the
  * same vector as src, vec_np or vec_tm, as in the reference's do_time_step;
  * any other overlap (src with an output, vec_np with vec_tm, upd partly
- * over another vector) is refused with SF_ERR_INVALID.  nrhs vectors of n_dofs entries each,
- * contiguous.  The reference's current_time argument only names the exact
- * solution's transport direction, which here is the handle's velocity. */
+ * over another vector) is refused with SF_ERR_INVALID.  nrhs vectors of
+ * n_dofs entries each, contiguous.  The reference's current_time argument
+ * only names the exact solution's transport direction, which here is the
+ * handle's velocity. */
 int sf_rk_stage(sf_op *op, int prec, int nrhs, const void *src, const void *upd, void *vec_np,
                 void *vec_tm, double c_np, double c_tm, void *stream);
 /* One step of the five-stage fourth-order low-storage Runge-Kutta scheme of
@@ -259,8 +260,8 @@ int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void 
  * node planes along z, the remaining FP32 cases) runs on the packed
  * line-ownership kernel (one thread per line of a cell, several cells per
  * warp group); SF_KERNEL_GENERIC selects the line-ownership kernel for all
- * of them.  Both give the same operator to rounding.  SF_OP_DG_SIPG: SF_KERNEL_AUTO evaluates the operator in its
- * tensor-product form (on these Cartesian meshes the SIPG bilinear form is
+ * of them.  Both give the same operator to rounding.  SF_OP_DG_SIPG:
+ * SF_KERNEL_AUTO evaluates the operator in its tensor-product form (on these Cartesian meshes the SIPG bilinear form is
  * exactly L (x) M (x) M + M (x) L (x) M + M (x) M (x) L with 1D stiffness-
  * plus-face matrices L of penalty * (p+1)^2 and 1D mass matrices M: the
  * kernel of SF_OP_DG_PRECOMPUTED), SF_KERNEL_GENERIC the cell-and-face
@@ -271,10 +272,12 @@ int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void 
  * velocity, Cartesian cells), and A and A^T as M times such a sum;
  * SF_KERNEL_GENERIC the cell-and-face kernel that follows the reference's
  * EvaluationDGAdvection step by step; the same operator to rounding.
- * SF_OP_CONVECTION_FACES: SF_KERNEL_AUTO evaluates the cell operator as
- * sum_f L_f (x) M1 (x) M1 (1D convection-plus-own-face matrices L_f, 1D mass
- * M1), SF_KERNEL_GENERIC the face-array kernel.  Other values are rejected
- * with SF_ERR_INVALID.  No reference counterpart. */
+ * SF_OP_LAPLACE_FACES and SF_OP_CONVECTION_FACES: SF_KERNEL_AUTO evaluates
+ * the cell operator as sum_f L_f (x) M1 (x) M1 (1D stiffness- or
+ * convection-plus-own-face matrices L_f, 1D mass M1; for the Laplacian plus
+ * a rank-one face term per direction), SF_KERNEL_GENERIC the face-array
+ * kernel.  Other values are rejected with SF_ERR_INVALID.  No reference
+ * counterpart. */
 typedef enum {
   SF_KERNEL_AUTO = 0,
   SF_KERNEL_GENERIC = 1
@@ -288,8 +291,9 @@ int sf_device_status(sf_op *op, int *flags);
 /* ---------------- conjugate gradients ---------------- */
 typedef enum {
   SF_SOLVE_FP64 = 0,        /* plain CG, FP64 operator                          */
-  SF_SOLVE_MIXED = 1        /* FP64 outer iterative refinement around an FP32
-                               preconditioned CG inner solve                   */
+  SF_SOLVE_MIXED = 1        /* FP32 preconditioned CG with reliable updates by
+                               the true FP64 residual, FP64 refinement steps
+                               as the fallback                                 */
 } sf_solve_mode;
 
 typedef enum { SF_PRECOND_NONE = 0, SF_PRECOND_JACOBI = 1, SF_PRECOND_CHEBYSHEV = 2 } sf_precond;
