@@ -262,9 +262,10 @@ int sf_kappa_gradient(sf_op *op, int prec, const void *u, const void *lam, void 
  * warp group); SF_KERNEL_GENERIC selects the line-ownership kernel for all
  * of them.  Both give the same operator to rounding.  SF_OP_DG_SIPG:
  * SF_KERNEL_AUTO evaluates the operator in its tensor-product form (on
- * these Cartesian meshes the SIPG bilinear form is exactly L (x) M (x) M + M (x) L (x) M + M (x) M (x) L with 1D stiffness-
- * plus-face matrices L of penalty * (p+1)^2 and 1D mass matrices M: the
- * kernel of SF_OP_DG_PRECOMPUTED), SF_KERNEL_GENERIC the cell-and-face
+ * these Cartesian meshes the SIPG bilinear form is exactly
+ * L (x) M (x) M + M (x) L (x) M + M (x) M (x) L with 1D stiffness-plus-face
+ * matrices L of penalty * (p+1)^2 and 1D mass matrices M: the kernel of
+ * SF_OP_DG_PRECOMPUTED), SF_KERNEL_GENERIC the cell-and-face
  * kernel that follows the reference's EvaluationDGLaplacian step by step;
  * both give the same operator to rounding.  SF_OP_DG_ADVECT: SF_KERNEL_AUTO
  * evaluates M^-1 A as a sum of 1D line operators, sum_d B_d (x) I (x) I
