@@ -26,3 +26,16 @@ def test_reference_arm_contract():
     sys.path.insert(0, ROOT)
     import bench
     assert d["config"] == bench.workload_config(4, 64)
+    assert d["cpu_baseline"]["build"].startswith("gcc -O3")
+
+
+def test_headline_algorithmic_bytes():
+    """p=4 on 64^3 deformed cells in FP32: x read and y written once (16.97 M
+    nodes) plus 6 geometry entries per Gauss point of 262,144 cells:
+    922,228,744 bytes per apply, the roofline's numerator"""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    cfg = bench.workload_config(4, 64)
+    assert cfg["n_dofs"] == 257 ** 3 == 16974593
+    assert bench.algorithmic_bytes(4, cfg["n_dofs"], 64 ** 3, 4) == 922228744
