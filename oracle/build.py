@@ -23,6 +23,8 @@ baseline of ``bench.py``).
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
+import glob
 import os
 import shutil
 import subprocess
@@ -120,7 +122,7 @@ def perf_build_flags() -> str:
 
 def build_oracle_perf(force: bool = False) -> str:
     """the oracle source compiled for timing as the CPU baseline: -O3, tuned
-    for the host CPU where it is a known target, floating-point contraction
+    for the host CPU on Arm hosts (perf_target), floating-point contraction
     allowed (the flags the reference's drivers are benchmarked with), OpenMP"""
     out = os.path.join(HERE, "liboracle_perf.so")
     flags_file = os.path.join(HERE, "liboracle_perf.flags")
@@ -156,8 +158,12 @@ def _patch_headers() -> str:
             if old not in lines[line - 1]:
                 raise RuntimeError("reference %s:%d does not contain %r" % (fname, line, old))
             lines[line - 1] = lines[line - 1].replace(old, new)
-        with open(os.path.join(pdir, fname), "w") as f:
-            f.writelines(lines)
+        path, text = os.path.join(pdir, fname), "".join(lines)
+        # rewritten only when the text changes, so that the adapters built on
+        # it stay up to date
+        if not os.path.exists(path) or open(path).read() != text:
+            with open(path, "w") as f:
+                f.write(text)
     return pdir
 
 
@@ -171,7 +177,7 @@ def build_ref() -> list[str]:
     flags = ["g++", "-O2", "-std=c++14", "-fPIC", "-shared", "-w",
              "-U__SSE2__", "-U__SSE__", "-U__AVX__", "-U__AVX2__", "-U__AVX512F__",
              "-I", shim]
-    outs = []
+    jobs = []
     # the DG headers put an OpenMP 'private' clause that the access macro of
     # ref_shim.h would rewrite, so they are built without OpenMP (serial)
     # the cell Laplacian's mass-matrix, convection and face variants are the
@@ -193,9 +199,24 @@ def build_ref() -> list[str]:
         for d in extra:
             inc += ["-I", d]
         out = os.path.join(OUT_REF, "lib%s.so" % name)
-        _run(flags + inc + defs + ["-o", out, os.path.join(shim, src + ".cc")])
-        outs.append(out)
-    return outs
+        source = os.path.join(shim, src + ".cc")
+        # inputs: the adapter, the shim headers, the included reference (and
+        # patched) headers and this recipe
+        deps = [source, os.path.abspath(__file__)] + glob.glob(os.path.join(shim, "*.h"))
+        for d in extra:
+            deps += glob.glob(os.path.join(d, "*.h"))
+        jobs.append((out, flags + inc + defs + ["-o", out + ".tmp", source], deps))
+
+    def one(job):
+        out, cmd, deps = job
+        if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
+            return out
+        _run(cmd)
+        os.replace(out + ".tmp", out)
+        return out
+
+    with cf.ThreadPoolExecutor(min(len(jobs), os.cpu_count() or 1)) as ex:
+        return list(ex.map(one, jobs))
 
 
 if __name__ == "__main__":
