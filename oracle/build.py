@@ -26,7 +26,6 @@ from __future__ import annotations
 import concurrent.futures as cf
 import glob
 import os
-import shutil
 import subprocess
 import sys
 

@@ -6,7 +6,6 @@ Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 from __future__ import annotations
 
 import ctypes as C
-import os
 
 import numpy as np
 

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.gpu_util import rel, to_dev, to_np, torch_cuda
+from tests.gpu_util import torch_cuda
 
 pytestmark = pytest.mark.gpu
 

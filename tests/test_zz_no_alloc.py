@@ -8,9 +8,6 @@ vectors must be refused.
 
 This file is collected last (test_zz_*) so that a failing run that stops at
 the first failure has already run every other test."""
-import ctypes as C
-
-import numpy as np
 import pytest
 
 from tests.gpu_util import FP32_TOL, FP64_TOL, rel, to_np, torch_cuda
