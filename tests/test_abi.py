@@ -237,3 +237,23 @@ def test_python_vector_checks_without_gpu():
         sfgpu.vec(FakeCuda(10, f32), 10, sfgpu.FP64, "y")
     with pytest.raises(ValueError, match="holds 9 entries; this call needs 10"):
         sfgpu.vec(FakeCuda(9, f64), 10, sfgpu.FP64, "y")
+
+
+def test_binding_arity_matches_header():
+    """every ctypes signature of the Python layer has as many parameters as
+    the prototype in include/sfgpu.h (a mismatch would shift arguments)"""
+    _, L = _lib()
+    src = open(os.path.join(ROOT, "include", "sfgpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    protos = re.findall(r"\b(sf_[a-z_0-9]+)\s*\(([^;{]*?)\)\s*;", src)
+    assert len(protos) >= 20
+    checked = 0
+    for name, params in protos:
+        params = " ".join(params.split())
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        argtypes = getattr(getattr(L, name), "argtypes", None)
+        if argtypes is None:
+            continue
+        assert len(argtypes) == n, (name, len(argtypes), n)
+        checked += 1
+    assert checked >= 20, checked
